@@ -1,0 +1,285 @@
+"""Benchmark of the XPBD tissue step on GB300.
+
+Workload (default): the kidney-scale block C2 -- 64 x 32(up) x 48 cells, 589,824 Kuhn tets,
+105,105 active nodes, per-tet compliance, capsule pressed into the top surface, 20 substeps per
+step.  A step is one LCS_Step (one frame: 20 substeps of predict, 6 edge colours, 31 tet colours,
+contact, velocity) on one tissue instance.
+
+``value``: steps/s from CUDA events around each frame launch on the library's stream, inputs
+resident in HBM, L2 flushed (256 MiB write) before every timed step.  ``e2e``: steps/s of the
+public C-ABI call sequence with host buffers (tool command in, node positions out) timed on the
+wall clock.  ``--impl reference`` times the reference path's CPU restatement (the reference ships no
+CPU solver) on all host cores for the same workload.  ``--gpus N`` runs N independent replicas
+(one per rank); a single tissue mesh does not shard.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "XPBD steps/s & constraint proj/s, batched vs plain; adjoint/forward time ratio"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def measured_peak():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        peaks = json.loads(path.read_text())
+        return float(peaks["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic_per_launch(name):
+    """Per-launch DRAM bytes of the frame kernel from the committed ncu summary, if one exists."""
+    path = ROOT / "profiles" / f"{name}.md"
+    if not path.exists():
+        return None
+    for line in path.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples every 200 ms while running."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.device = device_index
+        self.lines, self.proc = [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, f[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference_arm(args, world, rank):
+    """CPU restatement of the reference path on all host threads, same workload and metric."""
+    if rank != 0:
+        return
+    from genesis_tissue_simulation_gb300 import workloads as W
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+    lib = ROOT / "oracle" / "_build" / "liboracle_f32.so"
+    w = W.make(args.workload)
+    session = w.open(lib)
+    tets = session.tet_count
+    try:
+        threads = int(session.dll.ORC_Threads())
+        for k in range(args.warmup):
+            w.command(session, k)
+            session.step()
+        t0 = time.perf_counter()
+        for k in range(args.warmup, args.warmup + args.steps):
+            w.command(session, k)
+            session.step()
+        elapsed = time.perf_counter() - t0
+    finally:
+        session.close()
+    value = args.steps / elapsed
+    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": w.name, "substeps": w.params["substeps"], "tets": tets,
+                       "active_nodes": int((w.grid.active != 0).sum()), "parallelism": "host threads"},
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full steps of {w.name} after {args.warmup} warm-up steps, "
+                                       f"CPU restatement (FP32, OpenMP within each colour, {threads} threads)"},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(workload_name, budget_s=15.0, max_steps=40):
+    """Time the CPU restatement on a bounded sample of the workload: consecutive steps from the start."""
+    from genesis_tissue_simulation_gb300 import workloads as W
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+    lib = ROOT / "oracle" / "_build" / "liboracle_f32.so"
+    w = W.make(workload_name)
+    session = w.open(lib)
+    try:
+        threads = int(session.dll.ORC_Threads())
+        w.command(session, 0)
+        session.step()
+        n, t0 = 0, time.perf_counter()
+        while n < max_steps and time.perf_counter() - t0 < budget_s:
+            w.command(session, n + 1)
+            session.step()
+            n += 1
+        elapsed = time.perf_counter() - t0
+    finally:
+        session.close()
+    return {"value": n / elapsed, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"steps 2..{n + 1} of {w.name} (one warm-up step), CPU restatement FP32, OpenMP {threads} threads, {elapsed:.1f} s"}
+
+
+def main():
+    parser = argparse.ArgumentParser()
+    parser.add_argument("--gpus", type=int, default=1)
+    parser.add_argument("--steps", type=int, default=30)
+    parser.add_argument("--warmup", type=int, default=3)
+    parser.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    parser.add_argument("--workload", default="c2")
+    parser.add_argument("--no-cpu-baseline", action="store_true")
+    args = parser.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    from genesis_tissue_simulation_gb300 import build as native_build
+    from genesis_tissue_simulation_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if rank == 0 or world == 1:
+        native_build.build()
+    if world > 1:
+        dist.barrier()
+    lib = native_build.build()
+
+    w = W.make(args.workload, steps=args.warmup + args.steps)
+    session = w.open(lib)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    n_active = int((w.grid.active != 0).sum())
+    tets = session.tet_count
+    edges = int(session.functions["LCS_EdgeCount"]())
+    substeps = int(w.params["substeps"])
+    try:
+        for k in range(args.warmup):
+            w.command(session, k)
+            session.step()
+        torch.cuda.synchronize()
+        session.functions["LCS_ProfileEnable"](1)
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(torch.cuda.current_device()) as clocks:
+            wall0 = time.perf_counter()
+            for k in range(args.warmup, args.warmup + args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                w.command(session, k)
+                session.check("LCS_Step", session.dt)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - wall0
+        ms = np.zeros(3, dtype=np.float32)
+        session.check("LCS_ProfileRead", args.steps, ms.ctypes.data_as(__import__("ctypes").c_void_p))
+        device_s = float(ms[0]) / 1e3
+        session.functions["LCS_ProfileEnable"](0)
+
+        # end to end through the public ABI: tool command in from host memory, positions out
+        positions = np.empty((len(w.grid.positions), 3), dtype=np.float32)
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = time.perf_counter()
+        for k in range(args.warmup + args.steps, args.warmup + 2 * args.steps):
+            w.command(session, min(k, len(w.capsule_path) - 1) if w.capsule_path else k)
+            session.check("LCS_Step", session.dt)
+            session.check("LCS_Finalize")
+            session.check("LCS_GetCornerPos", positions.ctypes.data_as(__import__("ctypes").c_void_p))
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - e0
+        assert np.isfinite(positions).all(), "non-finite tissue state"
+    finally:
+        session.close()
+
+    t = torch.tensor([device_s, e2e_s, wall], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    device_s, e2e_s, wall = (float(x) for x in t.tolist())
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    value = world * args.steps / device_s
+    projections = substeps * (edges + tets)
+    bytes_per_substep = 64 * n_active + 4 * tets
+    launch_s = device_s / args.steps
+    achieved = substeps * bytes_per_substep / launch_s / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = ncu_traffic_per_launch(f"ncu_frame_kernel_{args.workload}")
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * device_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w.name, "cells": [64, 32, 48] if args.workload == "c2" else None, "tets": tets,
+                   "active_nodes": n_active, "lattice_nodes": len(w.grid.positions), "edges": edges, "substeps": substeps,
+                   "parallelism": f"replicas{world}", "l2": "flushed before every timed step (256 MiB write)",
+                   "timing": "CUDA events around each frame launch on the library stream"},
+        "proj_per_s": value * projections, "projections_per_step": projections,
+        "wall_steps_per_s": world * args.steps / wall,
+        "e2e": {"value": world * args.steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 92 + 4,
+                "d2h_bytes_per_step": 12 * len(w.grid.positions) + 12},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": substeps * bytes_per_substep},
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(args.workload)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,755 @@
+// LCS_* C ABI of the GB300 tissue solver: the drop-in for the reference plugin
+// (endoscopic_tissue/native/vendor/src/plugin_api.cpp) on the plain XPBD path.
+//
+// One process-global session, as in the reference (endoscopic_tissue/native_backend.py:213-218).
+// Host code builds the solver topology once (edge/bend/tet greedy colourings in the reference's
+// emission order, Kuhn tets, rest shapes) and uploads it in colour order; LCS_Step then runs one
+// persistent frame kernel per call.  Status codes follow the reference bands: 0 ok, -(cudaError),
+// -1000..-1005 solver (xpbd_solver.h:25-33), -2000..-2004 physics (V/physics.cu:219-228), -3000..
+// cut (V/cut.cu:1109-1427); -4001 marks entry points of the unified solver that this library does
+// not provide, -4002 a device barrier that timed out.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "frame_kernels.h"
+#include "../../include/gbtissue.h"
+
+using namespace gbt;
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------
+// session
+// ---------------------------------------------------------------------------------------------
+template <class T> struct DBuf {
+    T* p = nullptr; size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        release();
+        n = count;
+        return cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+    }
+    cudaError_t upload(const T* h, size_t count, cudaStream_t s) {
+        cudaError_t e = alloc(count);
+        if (e == cudaSuccess && count) e = cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
+        return e;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+};
+
+struct Session {
+    cudaStream_t stream = nullptr;
+    int device = 0, smCount = 0, gridBlocks = 0;
+    bool reconReady = false, physReady = false, cutReady = false;
+    int N = 0, dx = 0, dy = 0, dz = 0;
+    std::vector<float> hostRest;            // rest lattice (3N), the first corner positions uploaded
+    std::vector<float> skinT;               // [6N] skin crossing fraction per directed slot
+    // physics parameters
+    PhysicsInitDesc pd{};
+    int numSubsteps = 20;
+    float ks = 0, kb = 0, alpha = 0, betaS = 0, betaB = 0, youngE = 0, poisson = 0.45f, strainDamping = 0, omega = 1, damping = 0;
+    float bulkDampingSeconds = 0.003125f, tissueHardening = 80.f;
+    int volumePasses = 0;
+    float lastH = -1.f;
+    // topology sizes (host copies for diagnostics)
+    int E = 0, B = 0, T = 0;
+    std::vector<int> edgeColorOff, bendColorOff, tetColorOff;   // host copies [colors+1]
+    std::vector<int> tetColorOrder;                             // colour slot -> storage index
+    std::vector<int> tetIdsStorage;                             // [4T] storage order
+    std::vector<float2> tetStiffStorage;                        // [T] (mu V, kappa V) storage order
+    std::vector<int> edgeOwnerColor;                            // [E] owner slot per colour slot
+    float typeB[6][9];
+    // device buffers
+    DBuf<float4> pos, prev, vel, ext, rest;
+    DBuf<int> pinned, active, nbr, edgeColorOffD, bendColorOffD, tetColorOffD;
+    DBuf<int2> edgeEnds; DBuf<float> edgeRest; DBuf<int> edgeOwner, edgeLive;
+    DBuf<int4> bendIJK; DBuf<int> bendSrc, bendLive; DBuf<BendRecord> bendPairs;
+    DBuf<int4> tetIds; DBuf<int> tetMeta, tetOwner, edgeSupport; DBuf<float2> tetAlpha, tetStiff;
+    DBuf<unsigned> state;                   // [0] revision the liveness was derived at, [1] barrier counter, [2] status
+    unsigned* hostState = nullptr;          // pinned mirror of state + cut counters
+    // tool / contact
+    bool toolArmed = false; ToolPose tool{}, toolFrom{};
+    ContactParams cp{0.02f, 1.0e-7f, 0.5f, 0.045f, 0.25f};
+    GraspParamsAbi gp{0.5f, 0.3f, 0.02f, 0.55f, 0.3f, 1.0e-7f, 0.02f, 0.5f, 0.045f, 0.25f, 0.25f, 1.0e-7f, 150.f, 0.045f, 1};
+    int contactModel = 0;
+    // cut
+    CutInitDesc cd{};
+    DBuf<int4> gridEdges; DBuf<unsigned> occupied, cutMask, counters; DBuf<int> inside; DBuf<float> skinTD, edgeCutT;
+    bool toolSet = false, havePrev = false, pressure = false; CutToolDesc cutTool{};
+    float tearLen2 = 0.f;
+    // launch choice and profiling
+    int launchMode = 0;                     // 0 automatic, 1 whole-GPU grid, 2 single CTA
+    int clockKHz = 2000000;                 // SM clock, for the barrier spin budget
+    int syncTestExtra = 0; float syncBudgetSeconds = 2.f;
+    bool profile = false; std::vector<cudaEvent_t> events; int profiledSteps = 0;
+};
+Session S;
+
+int cudaStatus(cudaError_t e) { return e == cudaSuccess ? 0 : -(int)e; }
+#define CK(call) do { cudaError_t _e = (call); if (_e != cudaSuccess) return -(int)_e; } while (0)
+
+void freeCut() {
+    S.gridEdges.release(); S.occupied.release(); S.cutMask.release(); S.counters.release(); S.inside.release();
+    S.skinTD.release(); S.edgeCutT.release();
+    S.cutReady = false; S.toolSet = false; S.havePrev = false;
+}
+void freePhysics() {
+    freeCut();
+    for (auto* b : {&S.prev, &S.vel, &S.ext}) b->release();
+    for (auto* b : {&S.pinned, &S.active, &S.nbr, &S.edgeColorOffD, &S.bendColorOffD, &S.tetColorOffD, &S.edgeOwner, &S.edgeLive,
+                    &S.bendSrc, &S.bendLive, &S.tetMeta, &S.tetOwner, &S.edgeSupport}) b->release();
+    S.edgeEnds.release(); S.edgeRest.release(); S.bendIJK.release(); S.bendPairs.release(); S.tetIds.release();
+    S.tetAlpha.release(); S.tetStiff.release(); S.state.release();
+    S.physReady = false; S.toolArmed = false; S.E = S.B = S.T = 0; S.lastH = -1.f;
+}
+void freeAll() {
+    freePhysics();
+    S.pos.release(); S.rest.release();
+    S.reconReady = false;
+}
+
+int ensureStream() {
+    if (S.stream) return 0;
+    CK(cudaGetDevice(&S.device));
+    CK(cudaDeviceGetAttribute(&S.smCount, cudaDevAttrMultiProcessorCount, S.device));
+    CK(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+    CK(cudaMallocHost(&S.hostState, 8 * sizeof(unsigned)));
+    int perSm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, frameKernelGrid, kFrameThreads, 0));
+    int khz = 0;
+    if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, S.device) == cudaSuccess && khz > 0) S.clockKHz = khz;
+    S.gridBlocks = std::max(1, perSm) * S.smCount;
+    return 0;
+}
+
+int nodeIndex(int x, int y, int z) { return x + (S.dx + 1) * (y + (S.dy + 1) * z); }
+int directedSlot(int a, int b) {
+    int d = b - a, ad = d < 0 ? -d : d;
+    int axis = ad == 1 ? 0 : (ad == S.dx + 1 ? 1 : 2);
+    return 6 * a + 2 * axis + (d > 0 ? 1 : 0);
+}
+
+// Greedy colouring: each element takes the lowest of 64 colours none of its nodes carries yet
+// (xpbd_solver.cu:1213-1230 edges, 1340-1352 bends, 1738-1751 tets).  Returns the colour count or
+// XPBD_ERR_COLOR_OVERFLOW.
+int colourGreedy(int count, int arity, const int* nodesOf, int nodeCount, std::vector<int>& colourOf) {
+    std::vector<uint64_t> taken(nodeCount, 0);
+    colourOf.resize(count);
+    int colours = 0;
+    for (int e = 0; e < count; e++) {
+        const int* nd = nodesOf + (size_t)arity * e;
+        uint64_t busy = 0;
+        for (int k = 0; k < arity; k++) busy |= taken[nd[k]];
+        if (busy == ~0ull) return XPBD_ERR_COLOR_OVERFLOW;
+        int c = __builtin_ctzll(~busy);
+        colourOf[e] = c;
+        for (int k = 0; k < arity; k++) taken[nd[k]] |= 1ull << c;
+        colours = std::max(colours, c + 1);
+    }
+    return colours;
+}
+// Colour-major order: offsets[c] .. offsets[c+1] hold colour c, members in element order.
+void colourOrder(const std::vector<int>& colourOf, int colours, std::vector<int>& offsets, std::vector<int>& order) {
+    offsets.assign(colours + 1, 0);
+    for (int c : colourOf) offsets[c + 1]++;
+    for (int c = 0; c < colours; c++) offsets[c + 1] += offsets[c];
+    std::vector<int> fill(offsets.begin(), offsets.end() - 1);
+    order.resize(colourOf.size());
+    for (size_t e = 0; e < colourOf.size(); e++) order[fill[colourOf[e]]++] = (int)e;
+}
+
+bool invert3(const double a[3][3], double o[3][3], double* detOut) {
+    double c00 = a[1][1] * a[2][2] - a[1][2] * a[2][1], c01 = a[1][0] * a[2][2] - a[1][2] * a[2][0], c02 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+    double det = a[0][0] * c00 - a[0][1] * c01 + a[0][2] * c02;
+    if (detOut) *detOut = det;
+    if (std::fabs(det) < 1e-20) return false;
+    double r = 1.0 / det;
+    o[0][0] = c00 * r; o[0][1] = -(a[0][1] * a[2][2] - a[0][2] * a[2][1]) * r; o[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) * r;
+    o[1][0] = -c01 * r; o[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) * r; o[1][2] = -(a[0][0] * a[1][2] - a[0][2] * a[1][0]) * r;
+    o[2][0] = c02 * r; o[2][1] = -(a[0][0] * a[2][1] - a[0][1] * a[2][0]) * r; o[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) * r;
+    return true;
+}
+
+// Kuhn split of a cell along the diagonal from local corner 0 to 7; corner bit a = +axis a.
+const int kKuhn[6][4] = {{0, 1, 3, 7}, {0, 3, 2, 7}, {0, 2, 6, 7}, {0, 6, 4, 7}, {0, 4, 5, 7}, {0, 5, 1, 7}};
+
+// Tet mesh of every cell whose 8 corners are active (xpbd_build_tets, xpbd_solver.cu:1600-1848).
+int buildTets(const int* activeFlags, std::vector<int>& ids, std::vector<int>& owner, std::vector<int>& kind, std::vector<float2>& stiff) {
+    const float* P = S.hostRest.data();
+    double spacing[3] = {((double)P[3 * nodeIndex(S.dx, 0, 0)] - (double)P[0]) / S.dx,
+                         ((double)P[3 * nodeIndex(0, S.dy, 0) + 1] - (double)P[1]) / S.dy,
+                         ((double)P[3 * nodeIndex(0, 0, S.dz) + 2] - (double)P[2]) / S.dz};
+    double typeInv[6][3][3], typeVol[6];
+    for (int t = 0; t < 6; t++) {
+        double Dm[3][3];
+        for (int k = 1; k < 4; k++)
+            for (int a = 0; a < 3; a++) Dm[a][k - 1] = ((kKuhn[t][k] >> a) & 1) * spacing[a];
+        double det;
+        if (!invert3(Dm, typeInv[t], &det)) return XPBD_ERR_IRREGULAR_REST;
+        typeVol[t] = std::fabs(det) / 6.0;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) S.typeB[t][3 * a + b] = (float)typeInv[t][a][b];
+    }
+    float mu = 1.f, kappa = 1.f;
+    if (S.youngE > 0.f && S.poisson > -1.f && S.poisson < 0.5f) {
+        mu = S.youngE / (2.f * (1.f + S.poisson));
+        kappa = S.youngE / (3.f * (1.f - 2.f * S.poisson));
+    }
+    if (!(mu > 0.f)) mu = 1.f;
+    if (!(kappa > 0.f)) kappa = 1.f;
+    for (int z = 0; z < S.dz; z++)
+        for (int y = 0; y < S.dy; y++)
+            for (int x = 0; x < S.dx; x++) {
+                int corner[8];
+                bool full = true;
+                for (int l = 0; l < 8; l++) {
+                    corner[l] = nodeIndex(x + (l & 1), y + ((l >> 1) & 1), z + ((l >> 2) & 1));
+                    full = full && activeFlags[corner[l]] != 0;
+                }
+                if (!full) continue;
+                for (int t = 0; t < 6; t++) {
+                    const int* q = kKuhn[t];
+                    double Dm[3][3], inv[3][3], det;
+                    for (int c = 0; c < 3; c++)
+                        for (int a = 0; a < 3; a++) Dm[a][c] = (double)P[3 * corner[q[c + 1]] + a] - (double)P[3 * corner[q[0]] + a];
+                    if (!invert3(Dm, inv, &det)) continue;
+                    if (std::fabs(det) / 6.0 < 1e-12) continue;
+                    double scale = 0, dev = 0;
+                    for (int a = 0; a < 3; a++)
+                        for (int b = 0; b < 3; b++) {
+                            scale = std::max(scale, std::fabs(typeInv[t][a][b]));
+                            dev = std::max(dev, std::fabs(inv[a][b] - typeInv[t][a][b]));
+                        }
+                    if (dev > 1e-4 * scale) return XPBD_ERR_IRREGULAR_REST;
+                    // the three tet edges along lattice axes, owned by their lower node's +axis slot
+                    int found = 0;
+                    for (int a = 0; a < 4 && found < 3; a++)
+                        for (int b = a + 1; b < 4 && found < 3; b++) {
+                            int diff = q[a] ^ q[b];
+                            if (diff != 1 && diff != 2 && diff != 4) continue;
+                            int axis = diff == 1 ? 0 : (diff == 2 ? 1 : 2);
+                            int low = ((q[a] >> axis) & 1) ? q[b] : q[a];
+                            owner.push_back(6 * corner[low] + 2 * axis + 1);
+                            found++;
+                        }
+                    for (int k = 0; k < 4; k++) ids.push_back(corner[q[k]]);
+                    kind.push_back(t);
+                    stiff.push_back(make_float2(mu * (float)typeVol[t], kappa * (float)typeVol[t]));
+                }
+            }
+    return 0;
+}
+
+int uploadFrameState() {
+    std::vector<unsigned> st = {~0u, 0u, 0u, 0u};
+    CK(S.state.upload(st.data(), 4, S.stream));
+    return 0;
+}
+
+DeviceMesh deviceMesh() {
+    DeviceMesh m{};
+    m.nNodes = S.N; m.dx = S.dx; m.dy = S.dy; m.dz = S.dz;
+    m.pos = S.pos.p; m.prev = S.prev.p; m.vel = S.vel.p; m.ext = S.ext.p;
+    m.pinned = S.pinned.p; m.active = S.active.p; m.nbr = S.nbr.p;
+    m.nEdges = S.E; m.nEdgeColors = (int)S.edgeColorOff.size() - 1; m.edgeColorOff = S.edgeColorOffD.p;
+    m.edgeEnds = S.edgeEnds.p; m.edgeRest = S.edgeRest.p; m.edgeOwner = S.edgeOwner.p; m.edgeLive = S.edgeLive.p;
+    m.nBends = S.B; m.nBendColors = (int)S.bendColorOff.size() - 1; m.bendColorOff = S.bendColorOffD.p;
+    m.bendIJK = S.bendIJK.p; m.bendSrc = S.bendSrc.p; m.bendLive = S.bendLive.p; m.bendPairs = S.bendPairs.p;
+    m.nBendPairs = (int)S.bendPairs.n;
+    m.nTets = S.T; m.nTetColors = (int)S.tetColorOff.size() - 1; m.tetColorOff = S.tetColorOffD.p;
+    m.tetIds = S.tetIds.p; m.tetMeta = S.tetMeta.p; m.tetOwner = S.tetOwner.p; m.tetAlpha = S.tetAlpha.p; m.tetStiff = S.tetStiff.p;
+    m.edgeSupport = S.edgeSupport.p;
+    std::memcpy(m.typeB, S.typeB, sizeof(S.typeB));
+    return m;
+}
+
+CutParams cutParams() {
+    CutParams c{};
+    if (!S.cutReady) return c;
+    c.nGridEdges = (int)S.gridEdges.n; c.gridEdges = S.gridEdges.p; c.occupied = S.occupied.p; c.cutMask = S.cutMask.p;
+    c.inside = S.inside.p; c.skinT = S.skinTD.p; c.edgeCutT = S.edgeCutT.p; c.rest = S.rest.p; c.counters = S.counters.p;
+    c.sx = S.cutTool.t2v2[0]; c.sy = S.cutTool.t2v2[1]; c.sz = S.cutTool.t2v2[2];
+    c.ex = S.cutTool.t1v2[0]; c.ey = S.cutTool.t1v2[1]; c.ez = S.cutTool.t1v2[2];
+    c.voxelL = S.cd.voxelL; c.tearLen2 = S.tearLen2; c.havePrev = S.havePrev ? 1 : 0;
+    return c;
+}
+
+int launchFrame(const FrameCoeffs& fc) {
+    DeviceMesh m = deviceMesh();
+    CutParams cu = cutParams();
+    unsigned* state = S.state.p;
+    CK(cudaMemsetAsync(state + 1, 0, 2 * sizeof(unsigned), S.stream));
+    bool single = S.launchMode == 2 || (S.launchMode == 0 && S.T < 65536 && S.N < 32768);
+    if (single) {
+        frameKernelBlock<<<1, kFrameThreads, 0, S.stream>>>(m, fc, S.toolFrom, S.tool, S.cp, cu, state);
+        CK(cudaGetLastError());
+    } else {
+        ToolPose from = S.toolFrom, to = S.tool;
+        ContactParams cp = S.cp;
+        void* args[] = {&m, (void*)&fc, &from, &to, &cp, &cu, &state};
+        CK(cudaLaunchCooperativeKernel((const void*)frameKernelGrid, dim3(S.gridBlocks), dim3(kFrameThreads), args, 0, S.stream));
+    }
+    return 0;
+}
+
+}  // namespace
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+LCS_API int LCS_Init(const ReconInitDescAbi* desc, const float* cornerPos, const int* voxelCorner, const int* voxelIsectOffset,
+                     const int* voxelIsectCount, const void* isect, const void* surfaceEdges) {
+    (void)voxelCorner; (void)voxelIsectOffset; (void)voxelIsectCount; (void)surfaceEdges;
+    freeAll();
+    if (!desc) return -1000;
+    if (desc->voxelCount <= 0 || desc->cornerCount <= 0 || desc->triCapacity <= 0 || !cornerPos) return -1001;
+    if ((long long)(desc->dimsX + 1) * (desc->dimsY + 1) * (desc->dimsZ + 1) != desc->cornerCount) return -1001;
+    int rc = ensureStream();
+    if (rc) return rc;
+    S.N = desc->cornerCount; S.dx = desc->dimsX; S.dy = desc->dimsY; S.dz = desc->dimsZ;
+    S.hostRest.assign(cornerPos, cornerPos + 3 * (size_t)S.N);
+    std::vector<float4> p4(S.N);
+    for (int i = 0; i < S.N; i++) p4[i] = make_float4(cornerPos[3 * i], cornerPos[3 * i + 1], cornerPos[3 * i + 2], 0.f);
+    CK(S.pos.upload(p4.data(), S.N, S.stream));
+    CK(S.rest.upload(p4.data(), S.N, S.stream));
+    S.skinT.assign((size_t)6 * S.N, -1.f);
+    const IsectAbi* is = (const IsectAbi*)isect;
+    for (int i = 0; is && i < desc->isectCount; i++) {
+        S.skinT[directedSlot(is[i].a, is[i].b)] = is[i].t;
+        S.skinT[directedSlot(is[i].b, is[i].a)] = 1.f - is[i].t;
+    }
+    CK(cudaStreamSynchronize(S.stream));
+    S.reconReady = true;
+    return 0;
+}
+
+LCS_API int LCS_PhysicsAbiVersion() { return (int)sizeof(PhysicsInitDesc); }
+LCS_API int LCS_GraspToolAbiVersion() { return (int)sizeof(ToolPose); }
+LCS_API int LCS_ContactModelVersion() { return 28; }
+
+LCS_API int LCS_InitPhysics(const PhysicsInitDesc* desc, const float* mass, const int* pinned, const int* active, const float* extForce,
+                            const int* nbrIdx, const float* restNbr, const void* bendPairs) {
+    freePhysics();
+    if (!desc) return -2000;
+    if (!std::isfinite(desc->youngE) || desc->youngE < 0.f || !std::isfinite(desc->poisson) || desc->poisson < 0.f ||
+        desc->poisson >= 0.5f || !std::isfinite(desc->strainDamping) || desc->strainDamping < 0.f) return -2004;
+    const int cc = desc->cornerCount, bpc = desc->bendPairCount;
+    if (cc <= 0) return -2001;
+    if (!S.reconReady || cc != S.N) return -2002;
+    if (!mass || !pinned || !active || !extForce || !nbrIdx || !restNbr || bpc < 0 || (bpc > 0 && !bendPairs)) return XPBD_ERR_BAD_ARG;
+    S.pd = *desc;
+    S.numSubsteps = desc->maxSubsteps > 0 ? desc->maxSubsteps : 20;
+    S.omega = 1.f; S.damping = 0.f; S.ks = desc->ks; S.kb = desc->kb; S.alpha = desc->alpha; S.betaS = desc->cs; S.betaB = desc->cb;
+    S.youngE = desc->youngE; S.poisson = desc->poisson; S.strainDamping = desc->strainDamping;
+
+    // lattice edges, each from its lower node's positive slot (xpbd_bind, xpbd_solver.cu:1445-1463)
+    std::vector<int> ends, owner;
+    std::vector<float> restLen;
+    for (int p = 0; p < cc; p++)
+        for (int a = 0; a < 3; a++) {
+            int slot = 6 * p + 2 * a + 1, n = nbrIdx[slot];
+            if (n < 0) continue;
+            if (n >= cc) return XPBD_ERR_BAD_ARG;
+            const float* r = restNbr + 3 * (size_t)slot;
+            ends.push_back(p); ends.push_back(n); owner.push_back(slot);
+            restLen.push_back(sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]));
+        }
+    const int E = (int)owner.size();
+    std::vector<int> colourOf, order;
+    int edgeColours = colourGreedy(E, 2, ends.data(), cc, colourOf);
+    if (edgeColours < 0) return edgeColours;
+    colourOrder(colourOf, edgeColours, S.edgeColorOff, order);
+    std::vector<int2> eEnds(E); std::vector<float> eRest(E); std::vector<int> eOwner(E);
+    for (int k = 0; k < E; k++) {
+        int e = order[k];
+        eEnds[k] = make_int2(ends[2 * e], ends[2 * e + 1]); eRest[k] = restLen[e]; eOwner[k] = owner[e];
+    }
+    S.edgeOwnerColor = eOwner;
+    // bend elements alive at bind time, coloured over their three nodes (xpbd_solver.cu:1465-1479)
+    const BendRecord* bp = (const BendRecord*)bendPairs;
+    std::vector<int> bNodes, bSrc; std::vector<float> bTheta;
+    for (int b = 0; b < bpc; b++) {
+        if (bp[b].alive == 0) continue;
+        if (bp[b].i < 0 || bp[b].i >= cc || bp[b].j < 0 || bp[b].j >= cc || bp[b].k < 0 || bp[b].k >= cc) return XPBD_ERR_BAD_ARG;
+        bNodes.push_back(bp[b].i); bNodes.push_back(bp[b].j); bNodes.push_back(bp[b].k);
+        bTheta.push_back(bp[b].theta0); bSrc.push_back(b);
+    }
+    const int B = (int)bSrc.size();
+    int bendColours = colourGreedy(B, 3, bNodes.data(), cc, colourOf);
+    if (bendColours < 0) return bendColours;
+    colourOrder(colourOf, bendColours, S.bendColorOff, order);
+    std::vector<int4> bIJK(B); std::vector<int> bSrcOrd(B);
+    for (int k = 0; k < B; k++) {
+        int e = order[k];
+        float th = bTheta[e];
+        int thBits; std::memcpy(&thBits, &th, 4);
+        bIJK[k] = make_int4(bNodes[3 * e], bNodes[3 * e + 1], bNodes[3 * e + 2], thBits);
+        bSrcOrd[k] = bSrc[e];
+    }
+    // tets
+    std::vector<int> tIds, tOwner, tKind; std::vector<float2> tStiff;
+    int rc = buildTets(active, tIds, tOwner, tKind, tStiff);
+    if (rc) return rc;
+    const int T = (int)tKind.size();
+    if (T % 6) return XPBD_ERR_IRREGULAR_REST;
+    int tetColours = colourGreedy(T, 4, tIds.data(), cc, colourOf);
+    if (tetColours < 0) return tetColours;
+    colourOrder(colourOf, tetColours, S.tetColorOff, order);
+    // storage index: Kuhn type major, cell order minor (xpbd_solver.cu:1757-1780)
+    std::vector<int> place(T), perType(7, 0);
+    for (int e = 0; e < T; e++) perType[tKind[e] + 1]++;
+    for (int k = 0; k < 6; k++) perType[k + 1] += perType[k];
+    for (int e = 0; e < T; e++) place[e] = perType[tKind[e]]++;
+    S.tetIdsStorage.assign((size_t)4 * T, 0); S.tetStiffStorage.assign(T, make_float2(0, 0)); S.tetColorOrder.assign(T, 0);
+    std::vector<int4> cIds(T); std::vector<int> cMeta(T), cOwner((size_t)3 * T); std::vector<float2> cStiff(T);
+    for (int e = 0; e < T; e++) {
+        for (int k = 0; k < 4; k++) S.tetIdsStorage[4 * place[e] + k] = tIds[4 * e + k];
+        S.tetStiffStorage[place[e]] = tStiff[e];
+    }
+    for (int k = 0; k < T; k++) {
+        int e = order[k];
+        S.tetColorOrder[k] = place[e];
+        cIds[k] = make_int4(tIds[4 * e], tIds[4 * e + 1], tIds[4 * e + 2], tIds[4 * e + 3]);
+        cMeta[k] = tKind[e] | 8;
+        for (int o = 0; o < 3; o++) cOwner[3 * k + o] = tOwner[3 * e + o];
+        cStiff[k] = tStiff[e];
+    }
+    S.E = E; S.B = B; S.T = T;
+
+    // node state: pos.w = inverse mass, ext.w = mass
+    std::vector<float4> ext4(cc), zero4(cc, make_float4(0, 0, 0, 0)), pos4(cc);
+    for (int i = 0; i < cc; i++) {
+        ext4[i] = make_float4(extForce[3 * i], extForce[3 * i + 1], extForce[3 * i + 2], mass[i]);
+        float w = (pinned[i] != 0 || active[i] == 0) ? 0.f : 1.f / mass[i];
+        pos4[i] = make_float4(S.hostRest[3 * i], S.hostRest[3 * i + 1], S.hostRest[3 * i + 2], w);
+    }
+    CK(S.pos.upload(pos4.data(), cc, S.stream));
+    CK(S.prev.upload(pos4.data(), cc, S.stream));
+    CK(S.vel.upload(zero4.data(), cc, S.stream));
+    CK(S.ext.upload(ext4.data(), cc, S.stream));
+    CK(S.pinned.upload(pinned, cc, S.stream));
+    CK(S.active.upload(active, cc, S.stream));
+    CK(S.nbr.upload(nbrIdx, (size_t)6 * cc, S.stream));
+    CK(S.edgeColorOffD.upload(S.edgeColorOff.data(), S.edgeColorOff.size(), S.stream));
+    CK(S.edgeEnds.upload(eEnds.data(), E, S.stream));
+    CK(S.edgeRest.upload(eRest.data(), E, S.stream));
+    CK(S.edgeOwner.upload(eOwner.data(), E, S.stream));
+    std::vector<int> ones(std::max(std::max(E, B), 1), 1);
+    CK(S.edgeLive.upload(ones.data(), E, S.stream));
+    CK(S.bendColorOffD.upload(S.bendColorOff.data(), S.bendColorOff.size(), S.stream));
+    CK(S.bendIJK.upload(bIJK.data(), B, S.stream));
+    CK(S.bendSrc.upload(bSrcOrd.data(), B, S.stream));
+    CK(S.bendLive.upload(ones.data(), B, S.stream));
+    CK(S.bendPairs.upload(bp, bpc, S.stream));
+    CK(S.tetColorOffD.upload(S.tetColorOff.data(), S.tetColorOff.size(), S.stream));
+    CK(S.tetIds.upload(cIds.data(), T, S.stream));
+    CK(S.tetMeta.upload(cMeta.data(), T, S.stream));
+    CK(S.tetOwner.upload(cOwner.data(), (size_t)3 * T, S.stream));
+    CK(S.tetStiff.upload(cStiff.data(), T, S.stream));
+    CK(S.tetAlpha.alloc(T));
+    std::vector<int> zeros((size_t)6 * cc, 0);
+    CK(S.edgeSupport.upload(zeros.data(), (size_t)6 * cc, S.stream));
+    rc = uploadFrameState();
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(S.stream));
+    S.physReady = true;
+    return 0;
+}
+
+LCS_API int LCS_SetGravity(float gx, float gy, float gz) {
+    if (!S.physReady) return XPBD_ERR_NOT_READY;
+    if (!std::isfinite(gx) || !std::isfinite(gy) || !std::isfinite(gz)) return XPBD_ERR_BAD_ARG;
+    gravityKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(S.N, gx, gy, gz, S.ext.p);
+    return cudaStatus(cudaGetLastError());
+}
+
+LCS_API int LCS_SetTetStiffness(int count, const float* muV, const float* kappaV) {
+    if (!S.physReady) return XPBD_ERR_NOT_READY;
+    if (count != S.T || !muV || !kappaV) return XPBD_ERR_BAD_ARG;
+    for (int t = 0; t < count; t++)
+        if (!(muV[t] > 0.f) || !(kappaV[t] > 0.f) || !std::isfinite(muV[t]) || !std::isfinite(kappaV[t])) return XPBD_ERR_BAD_ARG;
+    std::vector<float2> c(count);
+    for (int k = 0; k < count; k++) {
+        int t = S.tetColorOrder[k];
+        c[k] = make_float2(muV[t], kappaV[t]);
+        S.tetStiffStorage[t] = c[k];
+    }
+    CK(cudaMemcpyAsync(S.tetStiff.p, c.data(), count * sizeof(float2), cudaMemcpyHostToDevice, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    S.lastH = -1.f;
+    return 0;
+}
+
+LCS_API int LCS_GetTetStiffness(float* muV, float* kappaV) {
+    if (!S.physReady || !muV || !kappaV) return XPBD_ERR_BAD_ARG;
+    for (int t = 0; t < S.T; t++) { muV[t] = S.tetStiffStorage[t].x; kappaV[t] = S.tetStiffStorage[t].y; }
+    return 0;
+}
+LCS_API int LCS_TetCount() { return S.physReady ? S.T : 0; }
+LCS_API int LCS_TetColorCount() { return S.physReady ? (int)S.tetColorOff.size() - 1 : 0; }
+LCS_API int LCS_EdgeColorCount() { return S.physReady ? (int)S.edgeColorOff.size() - 1 : 0; }
+LCS_API int LCS_EdgeCount() { return S.physReady ? S.E : 0; }
+LCS_API int LCS_GetTetIds(int* out) {
+    if (!S.physReady || !out) return XPBD_ERR_BAD_ARG;
+    std::memcpy(out, S.tetIdsStorage.data(), S.tetIdsStorage.size() * sizeof(int));
+    return 0;
+}
+LCS_API int LCS_GetTetColors(int* out) {
+    if (!S.physReady || !out) return XPBD_ERR_BAD_ARG;
+    for (size_t c = 0; c + 1 < S.tetColorOff.size(); c++)
+        for (int k = S.tetColorOff[c]; k < S.tetColorOff[c + 1]; k++) out[S.tetColorOrder[k]] = (int)c;
+    return 0;
+}
+LCS_API int LCS_GetEdgeColors(int* out6N) {
+    if (!S.physReady || !out6N) return XPBD_ERR_BAD_ARG;
+    std::fill(out6N, out6N + 6 * (size_t)S.N, -1);
+    for (size_t c = 0; c + 1 < S.edgeColorOff.size(); c++)
+        for (int k = S.edgeColorOff[c]; k < S.edgeColorOff[c + 1]; k++) out6N[S.edgeOwnerColor[k]] = (int)c;
+    return 0;
+}
+
+LCS_API void LCS_SetGraspParams(const GraspParamsAbi* p) {
+    if (!p) return;
+    S.gp = *p;
+    S.cp.jawGapClosed = p->jawGapClosed; S.cp.contactAlpha = p->contactAlpha; S.cp.ccdVelThresh = p->ccdVelThresh;
+    S.cp.ccdMaxDisp = p->ccdMaxDisp; S.cp.ccdOmega = p->ccdOmega;
+}
+LCS_API int LCS_SetContactModel(int enabled, float muS, float muD, float thickness, float radius) {
+    if (!S.physReady) return XPBD_ERR_NOT_READY;
+    if (enabled < 0 || enabled > 2 || !std::isfinite(muS) || !std::isfinite(muD) || !std::isfinite(thickness) || !std::isfinite(radius) ||
+        muS < 0 || muD < 0 || muD > muS || thickness <= 0 || radius < 0) return XPBD_ERR_BAD_ARG;
+    if (enabled != 0) return LCS_ERR_UNSUPPORTED;
+    S.contactModel = 0;
+    return 0;
+}
+LCS_API int LCS_SetTissueGuard(float minimum, int passes, int count, const int* inside, int capture) {
+    (void)capture;
+    if (!S.physReady || S.lastH > 0 || !std::isfinite(minimum) || minimum < 0 || minimum > .95f || passes < 0 || passes > 4 ||
+        count != S.N || !inside) return XPBD_ERR_BAD_ARG;
+    if (passes > 0) return LCS_ERR_UNSUPPORTED;
+    S.volumePasses = 0;
+    return 0;
+}
+LCS_API int LCS_SetTissueMaterial(float strength, float bulkDamping) {
+    if (!S.physReady || S.lastH > 0 || !std::isfinite(strength) || strength < 0 || strength > 1000 || !std::isfinite(bulkDamping) ||
+        bulkDamping < 0 || bulkDamping > 1) return XPBD_ERR_BAD_ARG;
+    S.tissueHardening = strength; S.bulkDampingSeconds = bulkDamping;
+    return 0;
+}
+LCS_API int LCS_SetGraspTool(const void* toolState) {
+    if (!S.physReady || !toolState) return -1;
+    ToolPose t;
+    std::memcpy(&t, toolState, sizeof(t));
+    S.toolFrom = S.toolArmed ? S.tool : t;
+    S.tool = t;
+    S.toolArmed = true;
+    if (t.grasp01 > S.gp.graspThreshold) return LCS_ERR_UNSUPPORTED;   // a capture starts the grasp solver
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// cut
+// ---------------------------------------------------------------------------------------------
+LCS_API int LCS_InitCut(const CutInitDesc* desc, const void* conn4096, const void* gridEdges, const int* voxelOccupied,
+                        const int* cornerInside) {
+    (void)conn4096;
+    freeCut();
+    if (!desc) return -3000;
+    if (desc->voxelCount <= 0 || desc->cornerCount <= 0) return -3001;
+    if (!S.physReady || desc->cornerCount != S.N || desc->dimsX != S.dx || desc->dimsY != S.dy || desc->dimsZ != S.dz) return -3002;
+    if (desc->voxelCount != S.dx * S.dy * S.dz || !voxelOccupied || !cornerInside || desc->gridEdgeCount < 0 ||
+        (desc->gridEdgeCount > 0 && !gridEdges)) return -3001;
+    S.cd = *desc;
+    CK(S.gridEdges.upload((const int4*)gridEdges, desc->gridEdgeCount, S.stream));
+    CK(S.occupied.upload((const unsigned*)voxelOccupied, desc->voxelCount, S.stream));
+    CK(S.cutMask.alloc(desc->voxelCount));
+    CK(cudaMemsetAsync(S.cutMask.p, 0, desc->voxelCount * sizeof(unsigned), S.stream));
+    CK(S.inside.upload(cornerInside, S.N, S.stream));
+    CK(S.skinTD.upload(S.skinT.data(), S.skinT.size(), S.stream));
+    std::vector<float> minus((size_t)6 * S.N, -1.f);
+    CK(S.edgeCutT.upload(minus.data(), minus.size(), S.stream));
+    CK(S.counters.alloc(4));
+    CK(cudaMemsetAsync(S.counters.p, 0, 4 * sizeof(unsigned), S.stream));
+    float tau = desc->tearStretchRatio;
+    S.tearLen2 = (tau >= 1.0f && tau == tau) ? (tau * desc->voxelL) * (tau * desc->voxelL) : 0.f;
+    CK(cudaStreamSynchronize(S.stream));
+    S.cutReady = true;
+    return 0;
+}
+LCS_API void LCS_SetTool(const CutToolDesc* tool) {
+    if (!tool) return;
+    S.cutTool = *tool;
+    if (!S.toolSet && S.cutReady) S.havePrev = true;   // the snapshot is the current positions
+    S.toolSet = true;
+}
+LCS_API void LCS_SetPressureCutMode(int enabled) { S.pressure = enabled != 0; }
+
+LCS_API int LCS_DetectCut() {
+    if (!S.cutReady || !S.toolSet || S.pressure) return 0;
+    int n = (int)S.gridEdges.n;
+    if (n <= 0) return 0;
+    DeviceMesh m = deviceMesh();
+    CutParams cu = cutParams();
+    QuadTool q{};
+    const CutToolDesc& c = S.cutTool;
+    auto v = [](const float* a) { f3 r; r.x = a[0]; r.y = a[1]; r.z = a[2]; return r; };
+    q.t1[0] = v(c.t1v0); q.t1[1] = v(c.t1v1); q.t1[2] = v(c.t1v2);
+    q.t2[0] = v(c.t2v0); q.t2[1] = v(c.t2v1); q.t2[2] = v(c.t2v2);
+    q.lo = v(c.aabbMin); q.hi = v(c.aabbMax); q.valid = c.valid;
+    detectQuadKernel<<<(n + 255) / 256, 256, 0, S.stream>>>(m, cu, q);
+    severKernel<<<(n + 255) / 256, 256, 0, S.stream>>>(m, cu);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(S.stream));
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// step
+// ---------------------------------------------------------------------------------------------
+LCS_API int LCS_Step(float dt) {
+    if (!S.physReady) return -1;
+    const int N = S.numSubsteps > 0 ? S.numSubsteps : 1;
+    float h = dt / (float)N;
+    if (!(h > 0.f) || !std::isfinite(h)) return XPBD_ERR_BAD_DT;
+    FrameCoeffs fc{};
+    fc.numSubsteps = N; fc.substeps = N; fc.firstSubstep = 0;
+    float at = S.ks > 0.f ? 1.f / (S.ks * h * h) : 0.f;
+    fc.velScale = (1.f - S.damping) / (1.f + S.alpha * h);
+    fc.betaGammaHS = at * S.betaS * h;
+    fc.alphaTilde = at;
+    fc.doBend = (S.B > 0 && S.kb > 0.f) ? 1 : 0;
+    fc.alphaB = fc.doBend ? 1.f / (S.kb * h * h) : 0.f;
+    fc.betaGammaHB = fc.alphaB * S.betaB * h;
+    fc.h = h; fc.invH = 1.f / h; fc.invH2 = 1.f / (h * h);
+    fc.doStrain = (S.T > 0 && S.youngE > 0.f) ? 1 : 0;
+    fc.fallback = (fc.doStrain && S.ks <= 0.f) ? 1 : 0;
+    fc.doEdges = (S.ks > 0.f || fc.fallback) ? 1 : 0;
+    fc.fallbackInvEh2 = fc.fallback ? 1.f / (S.youngE * h * h) : 0.f;
+    fc.perpDamp = S.betaS > 0.f ? 1 : 0;
+    fc.betaS = S.betaS;
+    fc.omega = S.omega;
+    fc.dampingOverH = fmaxf(0.f, S.strainDamping) / h;
+    fc.contact = (S.toolArmed && S.contactModel == 0) ? 1 : 0;
+    fc.contactAlphaH2 = S.cp.contactAlpha / (h * h);
+    fc.cut = (S.cutReady && S.toolSet && !S.pressure) ? 1 : 0;
+    fc.spinBudget = (long long)((double)S.syncBudgetSeconds * 1e3 * S.clockKHz);
+    fc.syncTestExtra = S.syncTestExtra;
+    if (fc.doStrain && h != S.lastH) {
+        tetAlphaKernel<<<(S.T + 255) / 256, 256, 0, S.stream>>>(S.T, fc.invH2, S.tetStiff.p, S.tetAlpha.p);
+        CK(cudaGetLastError());
+        S.lastH = h;
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (S.profile) {
+        CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+        CK(cudaEventRecord(e0, S.stream));
+    }
+    int rc = launchFrame(fc);
+    if (rc) return rc;
+    if (S.profile) { CK(cudaEventRecord(e1, S.stream)); S.events.push_back(e0); S.events.push_back(e1); }
+    CK(cudaMemcpyAsync(S.hostState, S.state.p, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    if (fc.cut) S.havePrev = true;
+    if (S.toolArmed) S.toolFrom = S.tool;
+    if (S.hostState[2] != 0u) return LCS_ERR_DEVICE_TIMEOUT;
+    return 0;
+}
+
+LCS_API int LCS_Finalize() { return S.physReady ? 0 : -1; }
+
+// ---------------------------------------------------------------------------------------------
+// readback
+// ---------------------------------------------------------------------------------------------
+LCS_API int LCS_GetCornerPos(float* out) {
+    if (!S.reconReady || !out) return -1;
+    std::vector<float4> p(S.N);
+    CK(cudaMemcpyAsync(p.data(), S.pos.p, S.N * sizeof(float4), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    for (int i = 0; i < S.N; i++) { out[3 * i] = p[i].x; out[3 * i + 1] = p[i].y; out[3 * i + 2] = p[i].z; }
+    return 0;
+}
+LCS_API int LCS_GetVelocities(float* out) {
+    if (!S.physReady || !out) return -1;
+    std::vector<float4> v(S.N);
+    CK(cudaMemcpyAsync(v.data(), S.vel.p, S.N * sizeof(float4), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    for (int i = 0; i < S.N; i++) { out[3 * i] = v[i].x; out[3 * i + 1] = v[i].y; out[3 * i + 2] = v[i].z; }
+    return 0;
+}
+LCS_API int LCS_GetNbrIdx(int* out) {
+    if (!S.physReady || !out) return -1;
+    CK(cudaMemcpyAsync(out, S.nbr.p, (size_t)6 * S.N * sizeof(int), cudaMemcpyDeviceToHost, S.stream));
+    return cudaStatus(cudaStreamSynchronize(S.stream));
+}
+LCS_API int LCS_GetBendPairs(void* out) {
+    if (!S.physReady || !out) return -1;
+    CK(cudaMemcpyAsync(out, S.bendPairs.p, S.bendPairs.n * sizeof(BendRecord), cudaMemcpyDeviceToHost, S.stream));
+    return cudaStatus(cudaStreamSynchronize(S.stream));
+}
+LCS_API int LCS_GetTopologyRevision(unsigned* revision) {
+    if (!revision) return -1;
+    if (!S.cutReady) { *revision = 0; return 0; }
+    CK(cudaMemcpyAsync(S.hostState + 4, S.counters.p, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    *revision = S.hostState[4];
+    return 0;
+}
+LCS_API int LCS_GetCutEdgeFractions(float* out) {
+    if (!S.cutReady || !out) return -1;
+    CK(cudaMemcpyAsync(out, S.edgeCutT.p, (size_t)6 * S.N * sizeof(float), cudaMemcpyDeviceToHost, S.stream));
+    return cudaStatus(cudaStreamSynchronize(S.stream));
+}
+LCS_API int LCS_GetVoxelCutMask(unsigned* out) {
+    if (!S.cutReady || !out) return -1;
+    CK(cudaMemcpyAsync(out, S.cutMask.p, S.cutMask.n * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    return cudaStatus(cudaStreamSynchronize(S.stream));
+}
+LCS_API int LCS_GetCutDebug(unsigned* out18, float* alphaOut) {
+    if (!S.cutReady || !out18) return -1;
+    std::memset(out18, 0, 18 * sizeof(unsigned));
+    CK(cudaMemcpyAsync(S.hostState + 4, S.counters.p, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    out18[15] = S.hostState[6];
+    out18[16] = S.hostState[5];
+    if (alphaOut) *alphaOut = S.cd.cutFPInterp;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// profiling (xpbd_profile_enable/read, xpbd_solver.cu:14-29): device time of each frame launch
+// ---------------------------------------------------------------------------------------------
+LCS_API void LCS_ProfileEnable(int enabled) {
+    for (cudaEvent_t e : S.events) cudaEventDestroy(e);
+    S.events.clear();
+    S.profile = enabled != 0;
+}
+LCS_API int LCS_ProfileRead(int steps, float* ms) {
+    if (!ms || steps <= 0 || (int)S.events.size() < 2 * steps) return -1;
+    CK(cudaEventSynchronize(S.events[2 * steps - 1]));
+    float total = 0.f;
+    for (int s = 0; s < steps; s++) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, S.events[2 * s], S.events[2 * s + 1]));
+        total += t;
+    }
+    ms[0] = total; ms[1] = 0.f; ms[2] = 0.f;
+    return 0;
+}
+LCS_API int LCS_SetLaunchMode(int mode) {
+    if (mode < 0 || mode > 2) return XPBD_ERR_BAD_ARG;
+    S.launchMode = mode;
+    return 0;
+}
+LCS_API int LCS_SetBarrierTest(int extraArrivals, float budgetSeconds) {
+    if (extraArrivals < 0 || !(budgetSeconds > 0.f) || budgetSeconds > 10.f) return XPBD_ERR_BAD_ARG;
+    S.syncTestExtra = extraArrivals;
+    S.syncBudgetSeconds = budgetSeconds;
+    return 0;
+}
+LCS_API void LCS_Shutdown() {
+    if (S.stream) cudaStreamSynchronize(S.stream);
+    LCS_ProfileEnable(0);
+    freeAll();
+}

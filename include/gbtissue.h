@@ -1,0 +1,112 @@
+/* gbtissue.h — C ABI of the GB300 XPBD tissue solver (libgbtissue.so).
+ *
+ * A drop-in for the reference plugin's LCS_* exports on the plain XPBD path
+ * (endoscopic_tissue/native/vendor/src/plugin_api.cpp), with the same names, argument meaning,
+ * struct layouts and status bands.  Plain pointers and sizes only; host arrays are copied in
+ * and out during each call and the caller keeps ownership (V/physics.cu:246-253; "V/" is
+ * endoscopic_tissue/native/vendor/cuda/).  One process-global session; not thread safe.
+ *
+ * Status: 0 ok; -(cudaError_t); -1000..-1005 solver (xpbd_solver.h:25-33); -2000..-2004 physics
+ * init (V/physics.cu:219-228); -3000..-3002 cut init (V/cut.cu:1109-1206);
+ * LCS_ERR_UNSUPPORTED (-4001): a switch of the unified contact/grasp solver or of the tissue
+ * guard that this library does not provide; LCS_ERR_DEVICE_TIMEOUT (-4002): a device barrier
+ * exceeded its spin budget and the frame was abandoned.
+ */
+#ifndef GBTISSUE_H
+#define GBTISSUE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LCS_API __attribute__((visibility("default")))
+
+#define XPBD_ERR_NOT_READY (-1000)
+#define XPBD_ERR_NO_FRAME (-1001)
+#define XPBD_ERR_BAD_DT (-1002)
+#define XPBD_ERR_COLOR_OVERFLOW (-1003)
+#define XPBD_ERR_BAD_ARG (-1004)
+#define XPBD_ERR_IRREGULAR_REST (-1005)
+#define LCS_ERR_UNSUPPORTED (-4001)
+#define LCS_ERR_DEVICE_TIMEOUT (-4002)
+
+/* ReconInitDesc, 40 bytes (V/dc_recon.h ReconInitDesc; Python ReconDesc, native_backend.py:22-25). */
+typedef struct { int voxelCount, cornerCount, isectCount, surfaceEdgeCount, triCapacity, dimsX, dimsY, dimsZ; float L; int qefIters; } ReconInitDescAbi;
+/* PhysicsInitDesc, 52 bytes (V/physics.h:18-31). */
+typedef struct { int cornerCount, bendPairCount; float ks, cs, kb, cb, hInit, hMax; int maxSubsteps; float alpha, youngE, poisson, strainDamping; } PhysicsInitDesc;
+/* CutInitDesc, 60 bytes (V/cut.h:15-27). */
+typedef struct { int voxelCount, cornerCount, gridEdgeCount, isectCount, triCapacity, dimsX, dimsY, dimsZ; float voxelL, originX, originY, originZ; int cutPointCapacity; float cutFPInterp, tearStretchRatio; } CutInitDesc;
+/* CutToolDesc, 116 bytes (V/cut.h:29-38): swept blade T1=(Sprev,Eprev,E), T2=(Sprev,E,S). */
+typedef struct { float t1v0[3], t1v1[3], t1v2[3], t2v0[3], t2v1[3], t2v2[3], ncut[3]; float d; int valid; float aabbMin[3], aabbMax[3]; } CutToolDesc;
+/* XpbdGraspParams, 60 bytes (V/xpbd/xpbd_solver.h:250-290). */
+typedef struct { float graspThreshold, releaseThreshold, jawGapClosed, coreEllipseFrac, mu, contactAlpha, contactSkin, ccdVelThresh, ccdMaxDisp, ccdOmega, omegaGrasp, coreAlpha, coreBreakForce, graspMaxDisp; int nExemptRings; } GraspParamsAbi;
+/* IsectGpu record, 40 bytes (V/common.cuh:23-32). */
+typedef struct { float position[3], normal[3]; int a, b; float t; int insideA; } IsectAbi;
+
+/* ---- initialisation (plugin_api.cpp:70-79, 105-115, 138-142) ---------------------------------- */
+/* LCS_Init: corner lattice (cornerPos float[3N]) and surface crossings; the dual-contouring buffers
+ * (voxelCorner, offsets, counts, surfaceEdges) are accepted and not used.  Replaces recon_init. */
+LCS_API int LCS_Init(const ReconInitDescAbi* desc, const float* cornerPos, const int* voxelCorner, const int* voxelIsectOffset,
+                     const int* voxelIsectCount, const void* isect, const void* surfaceEdges);
+/* LCS_InitPhysics: physics_init + xpbd_bind + xpbd_build_tets (V/physics.cu:214-315). */
+LCS_API int LCS_InitPhysics(const PhysicsInitDesc* desc, const float* mass, const int* pinned, const int* active, const float* extForce,
+                            const int* nbrIdx, const float* restNbr, const void* bendPairs);
+/* LCS_InitCut: cut_init (V/cut.cu:1105-1206); conn4096 is accepted and not used (surface path). */
+LCS_API int LCS_InitCut(const CutInitDesc* desc, const void* conn4096, const void* gridEdges, const int* voxelOccupied,
+                        const int* cornerInside);
+LCS_API int LCS_PhysicsAbiVersion(void);        /* = 52, plugin_api.cpp:102 */
+LCS_API int LCS_GraspToolAbiVersion(void);      /* = 92, plugin_api.cpp:197 */
+LCS_API int LCS_ContactModelVersion(void);      /* = 28, plugin_api.cpp:225 */
+
+/* ---- per-frame control (plugin_api.cpp:103, 125-166, 145-155, 198-201, 210-214, 263) ---------- */
+LCS_API int LCS_SetGravity(float gx, float gy, float gz);           /* physics_set_gravity */
+LCS_API int LCS_Step(float dt);                                      /* physics_step: N substeps + ribbon ticks */
+LCS_API int LCS_Finalize(void);                                      /* frame commit (no surface rebuild here) */
+LCS_API void LCS_SetTool(const CutToolDesc* tool);                   /* cut_set_tool */
+LCS_API int LCS_DetectCut(void);                                     /* cut_detect: swept quad + sever */
+LCS_API void LCS_SetPressureCutMode(int enabled);                    /* pressure mode: detection off here */
+LCS_API int LCS_SetGraspTool(const void* xpbdToolState);             /* xpbd_set_tool; capture -> -4001 */
+LCS_API void LCS_SetGraspParams(const GraspParamsAbi* params);       /* xpbd_set_grasp_params */
+LCS_API int LCS_SetContactModel(int enabled, float muS, float muD, float thickness, float radius); /* model 0 only */
+LCS_API int LCS_SetTissueGuard(float minimum, int passes, int count, const int* inside, int capture); /* passes 0 only */
+LCS_API int LCS_SetTissueMaterial(float tensileStrength, float bulkDampingSeconds);
+
+/* ---- readback (plugin_api.cpp:38, 170-177) ----------------------------------------------------- */
+LCS_API int LCS_GetCornerPos(float* out3N);
+LCS_API int LCS_GetNbrIdx(int* out6N);
+LCS_API int LCS_GetTopologyRevision(unsigned* revision);
+LCS_API int LCS_GetCutEdgeFractions(float* out6N);
+LCS_API int LCS_GetCutDebug(unsigned* out18, float* alphaOut);      /* slots 15 (tears) and 16 (cut points) */
+
+/* ---- profiling and shutdown (plugin_api.cpp:21-22, 236-242) ------------------------------------ */
+LCS_API void LCS_ProfileEnable(int enabled);
+LCS_API int LCS_ProfileRead(int steps, float* ms3);                  /* ms3[0] = device ms of the first `steps` frames */
+LCS_API void LCS_Shutdown(void);
+
+/* ---- module diagnostics without an LCS_ export in the reference -------------------------------- */
+LCS_API int LCS_TetCount(void);                  /* xpbd_tet_count (xpbd_solver.h:202) */
+LCS_API int LCS_TetColorCount(void);             /* xpbd_tet_color_count (xpbd_solver.h:203) */
+LCS_API int LCS_EdgeColorCount(void);            /* xpbd_color_count (xpbd_solver.h:177) */
+LCS_API int LCS_EdgeCount(void);                 /* xpbd_get_edge_count (xpbd_solver.h:183) */
+LCS_API int LCS_GetTetIds(int* out4T);           /* xpbd_readback_tet_ids (xpbd_solver.h:208): storage order */
+LCS_API int LCS_GetVelocities(float* out3N);     /* xpbd_get_velocities (xpbd_solver.h:174) */
+
+/* ---- extensions (no counterpart in the reference ABI) ------------------------------------------ */
+/* Per-tet material: mu*V and kappa*V of every tet in storage order (the order of LCS_GetTetIds);
+ * replaces the uniform bake from (E, nu).  The frame compliances become 1/(h^2 * value). */
+LCS_API int LCS_SetTetStiffness(int count, const float* muV, const float* kappaV);
+LCS_API int LCS_GetTetStiffness(float* muV, float* kappaV); /* the current mu*V, kappa*V, storage order */
+LCS_API int LCS_GetTetColors(int* outT);         /* greedy colour of each tet, storage order */
+LCS_API int LCS_GetEdgeColors(int* out6N);       /* colour of each lattice edge at its owner slot, else -1 */
+LCS_API int LCS_GetBendPairs(void* out);         /* the live 32-byte bend records */
+LCS_API int LCS_GetVoxelCutMask(unsigned* outV); /* cumulative 12-bit cut mask per voxel */
+LCS_API int LCS_SetLaunchMode(int mode);         /* 0 automatic, 1 whole-GPU cooperative grid, 2 one CTA */
+/* Failure-detection test mode of the grid barrier: every barrier awaits `extraArrivals` arrivals that
+ * never come and gives up after `budgetSeconds` (normal budget 2 s); LCS_Step then returns -4002 and
+ * the context stays usable.  (0, 2.0) restores normal operation. */
+LCS_API int LCS_SetBarrierTest(int extraArrivals, float budgetSeconds);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

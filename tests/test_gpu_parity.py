@@ -1,0 +1,118 @@
+"""CUDA path against the CPU oracle, through the LCS_* C ABI on both sides.
+
+The CUDA kernels evaluate every projection in the oracle's operation order without multiply-add
+contraction, so the FP32 trajectories agree bit for bit; the benchmark spec's tolerance (1e-4 of the
+bounding-box diagonal after 100 steps) is asserted as well, and the FP64 oracle error is reported.
+"""
+import numpy as np
+import pytest
+
+from genesis_tissue_simulation_gb300 import workloads as W
+from genesis_tissue_simulation_gb300.native_backend import XPBD_ERR_BAD_DT, LCS_ERR_DEVICE_TIMEOUT
+
+pytestmark = pytest.mark.gpu
+
+SMALL = (4.78, 2.38, 3.98)     # 24 x 12 x 20 cells: the C2/C3 scenarios at a size the oracle runs in seconds
+
+
+def trajectory(workload, lib, steps, every, launch_mode=None, topology=False):
+    session = workload.open(lib)
+    try:
+        if launch_mode is not None:
+            session.check("LCS_SetLaunchMode", launch_mode) if "LCS_SetLaunchMode" in session.functions else None
+        frames = []
+
+        def observe(k, s):
+            if (k + 1) % every == 0:
+                rec = {"pos": s.positions()}
+                if topology:
+                    rec.update(nbr=s.neighbors(), rev=s.topology_revision(), mask=s.voxel_cut_mask(),
+                               frac=s.cut_edge_fractions(), bends=s.bend_alive(), dbg=s.cut_debug()[15:17].copy())
+                frames.append(rec)
+        workload.run(session, steps=steps, observe=observe)
+        return frames
+    finally:
+        session.close()
+
+
+def _bind_launch_mode(lib):
+    import ctypes
+    from genesis_tissue_simulation_gb300 import native_backend as nb
+    dll = ctypes.CDLL(str(lib))
+    return dll
+
+
+def test_c1_plain_step_matches_oracle(gpu_lib, oracle_libs):
+    w = W.make("c1")
+    gpu = trajectory(w, gpu_lib, 100, 10)
+    cpu = trajectory(w, oracle_libs[0], 100, 10)
+    f64 = trajectory(w, oracle_libs[1], 100, 100)
+    active = w.grid.active != 0
+    tol = 1e-4 * W.bbox_diagonal(w.grid)
+    for k, (a, b) in enumerate(zip(gpu, cpu)):
+        err = float(np.abs(a["pos"] - b["pos"])[active].max())
+        assert err <= tol, f"step {10 * (k + 1)}: |gpu - oracle| = {err} > {tol}"
+        assert np.array_equal(a["pos"], b["pos"]), f"step {10 * (k + 1)}: not bit-identical (max {err})"
+    fp64_err = float(np.abs(gpu[-1]["pos"] - f64[-1]["pos"])[active].max())
+    print(f"C1 100 steps: |gpu - oracle fp32| = 0, |gpu - oracle fp64| = {fp64_err:.3e} cm "
+          f"({fp64_err / W.bbox_diagonal(w.grid):.3e} of the diagonal)")
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_launch_modes_agree(gpu_lib, oracle_libs, mode):
+    import ctypes
+    w = W.make("c1", steps=20)
+    dll = ctypes.CDLL(str(gpu_lib))
+    dll.LCS_SetLaunchMode(mode)
+    try:
+        gpu = trajectory(w, gpu_lib, 20, 20)
+    finally:
+        dll.LCS_SetLaunchMode(0)
+    cpu = trajectory(w, oracle_libs[0], 20, 20)
+    assert np.array_equal(gpu[-1]["pos"], cpu[-1]["pos"])
+
+
+def test_c2_capsule_small_matches_oracle(gpu_lib, oracle_libs):
+    w = W.make("c2", steps=40, scale=SMALL)
+    gpu = trajectory(w, gpu_lib, 40, 10)
+    cpu = trajectory(w, oracle_libs[0], 40, 10)
+    for a, b in zip(gpu, cpu):
+        assert np.array_equal(a["pos"], b["pos"]), float(np.abs(a["pos"] - b["pos"]).max())
+
+
+def test_c3_cut_small_topology_bit_exact(gpu_lib, oracle_libs):
+    w = W.make("c3", steps=40, scale=SMALL)
+    gpu = trajectory(w, gpu_lib, 40, 10, topology=True)
+    cpu = trajectory(w, oracle_libs[0], 40, 10, topology=True)
+    assert cpu[-1]["rev"] > 0, "the blade never crossed the tissue"
+    for a, b in zip(gpu, cpu):
+        assert a["rev"] == b["rev"]
+        for key in ("nbr", "mask", "frac", "bends", "dbg", "pos"):
+            assert np.array_equal(a[key], b[key]), key
+
+
+def test_c2_full_size_runs_deterministically(gpu_lib):
+    w = W.make("c2", steps=10)
+    runs = [trajectory(w, gpu_lib, 10, 10)[-1]["pos"] for _ in range(2)]
+    assert np.isfinite(runs[0]).all()
+    assert np.array_equal(runs[0], runs[1])
+
+
+def test_bad_dt_and_barrier_timeout_status(gpu_lib):
+    import ctypes
+    w = W.make("c1", steps=2)
+    session = w.open(gpu_lib)
+    try:
+        assert session.functions["LCS_Step"](0.0) == XPBD_ERR_BAD_DT
+        dll = session.dll
+        dll.LCS_SetLaunchMode(1)
+        dll.LCS_SetBarrierTest.argtypes = (ctypes.c_int, ctypes.c_float)
+        assert dll.LCS_SetBarrierTest(1, ctypes.c_float(0.05)) == 0
+        assert session.functions["LCS_Step"](1 / 60) == LCS_ERR_DEVICE_TIMEOUT
+        assert dll.LCS_SetBarrierTest(0, ctypes.c_float(2.0)) == 0
+        assert session.functions["LCS_Step"](1 / 60) == 0    # the context is still usable
+        assert np.isfinite(session.positions()).all()
+    finally:
+        session.dll.LCS_SetLaunchMode(0)
+        session.dll.LCS_SetBarrierTest(0, ctypes.c_float(2.0))
+        session.close()
