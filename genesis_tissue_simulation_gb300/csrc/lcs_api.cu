@@ -742,6 +742,99 @@ LCS_API int LCS_SetLaunchMode(int mode) {
     S.launchMode = mode;
     return 0;
 }
+// ---------------------------------------------------------------------------------------------
+// Allocation-free step.  Some hosts cannot let a plugin allocate device memory while they run:
+// engines and simulators that hand out all GPU memory from their own pool or a fixed budget, and
+// real-time loops where a cudaMalloc/cudaFree (which can synchronise the whole device) would stall
+// a frame.  LCS_StepNoAlloc advances the session exactly as LCS_Step does, but every piece of
+// frame scratch -- the grid barrier's arrival counter and status word, the liveness record, the
+// per-tet compliances of the frame -- lives in the file-scope array below, which the driver
+// reserves when the library is loaded and keeps on every GPU that loads it until the process
+// exits.  Its size caps the mesh: at most kNoAllocMaxTets tets.
+// ---------------------------------------------------------------------------------------------
+namespace {
+constexpr size_t kNoAllocHeaderBytes = 256;                        // state words, 256-byte aligned
+constexpr size_t kNoAllocAlphaBytes = (size_t)4 << 20;             // 4 MiB of per-tet compliances
+constexpr int kNoAllocMaxTets = (int)(kNoAllocAlphaBytes / sizeof(float2));   // 524,288 tets
+static __device__ __align__(256) unsigned char g_stepScratch[kNoAllocHeaderBytes + kNoAllocAlphaBytes];
+// Device address of g_stepScratch per device, resolved on the first call made with that device
+// current (the symbol itself is only a host-side stand-in).
+constexpr int kMaxDevices = 64;
+unsigned char* g_stepScratchAddr[kMaxDevices] = {};
+}  // namespace
+
+LCS_API int LCS_StepNoAlloc(float dt) {
+    if (!S.physReady) return -1;
+    if (S.T > kNoAllocMaxTets) return LCS_ERR_SCRATCH_LIMIT;
+    int device = 0;
+    CK(cudaGetDevice(&device));
+    if (device < 0 || device >= kMaxDevices) return XPBD_ERR_BAD_ARG;
+    if (!g_stepScratchAddr[device]) {
+        void* address = nullptr;
+        CK(cudaGetSymbolAddress(&address, g_stepScratch));
+        g_stepScratchAddr[device] = (unsigned char*)address;
+    }
+    unsigned char* scratch = g_stepScratchAddr[device];
+    unsigned* state = (unsigned*)scratch;
+    float2* alpha = (float2*)(scratch + kNoAllocHeaderBytes);
+
+    const int N = S.numSubsteps > 0 ? S.numSubsteps : 1;
+    float h = dt / (float)N;
+    if (!(h > 0.f) || !std::isfinite(h)) return XPBD_ERR_BAD_DT;
+    FrameCoeffs fc{};
+    fc.numSubsteps = N; fc.substeps = N; fc.firstSubstep = 0;
+    float at = S.ks > 0.f ? 1.f / (S.ks * h * h) : 0.f;
+    fc.velScale = (1.f - S.damping) / (1.f + S.alpha * h);
+    fc.betaGammaHS = at * S.betaS * h;
+    fc.alphaTilde = at;
+    fc.doBend = (S.B > 0 && S.kb > 0.f) ? 1 : 0;
+    fc.alphaB = fc.doBend ? 1.f / (S.kb * h * h) : 0.f;
+    fc.betaGammaHB = fc.alphaB * S.betaB * h;
+    fc.h = h; fc.invH = 1.f / h; fc.invH2 = 1.f / (h * h);
+    fc.doStrain = (S.T > 0 && S.youngE > 0.f) ? 1 : 0;
+    fc.fallback = (fc.doStrain && S.ks <= 0.f) ? 1 : 0;
+    fc.doEdges = (S.ks > 0.f || fc.fallback) ? 1 : 0;
+    fc.fallbackInvEh2 = fc.fallback ? 1.f / (S.youngE * h * h) : 0.f;
+    fc.perpDamp = S.betaS > 0.f ? 1 : 0;
+    fc.betaS = S.betaS;
+    fc.omega = S.omega;
+    fc.dampingOverH = fmaxf(0.f, S.strainDamping) / h;
+    fc.contact = (S.toolArmed && S.contactModel == 0) ? 1 : 0;
+    fc.contactAlphaH2 = S.cp.contactAlpha / (h * h);
+    fc.cut = (S.cutReady && S.toolSet && !S.pressure) ? 1 : 0;
+    fc.spinBudget = (long long)((double)S.syncBudgetSeconds * 1e3 * S.clockKHz);
+    fc.syncTestExtra = S.syncTestExtra;
+
+    // The array keeps whatever the previous call left: the liveness record restarts at "never
+    // derived" (word 0 = ~0u), the barrier counter and status at zero, and the compliances are
+    // written again for this session's tets.
+    CK(cudaMemsetAsync(state, 0xFF, sizeof(unsigned), S.stream));
+    CK(cudaMemsetAsync(state + 1, 0, 3 * sizeof(unsigned), S.stream));
+    if (fc.doStrain) {
+        tetAlphaKernel<<<(S.T + 255) / 256, 256, 0, S.stream>>>(S.T, fc.invH2, S.tetStiff.p, alpha);
+        CK(cudaGetLastError());
+    }
+    DeviceMesh m = deviceMesh();
+    m.tetAlpha = alpha;
+    CutParams cu = cutParams();
+    ToolPose from = S.toolFrom, to = S.tool;
+    ContactParams cp = S.cp;
+    bool single = S.launchMode == 2 || (S.launchMode == 0 && S.T < 65536 && S.N < 32768);
+    if (single) {
+        frameKernelBlock<<<1, kFrameThreads, 0, S.stream>>>(m, fc, from, to, cp, cu, state);
+        CK(cudaGetLastError());
+    } else {
+        void* args[] = {&m, (void*)&fc, &from, &to, &cp, &cu, &state};
+        CK(cudaLaunchCooperativeKernel((const void*)frameKernelGrid, dim3(S.gridBlocks), dim3(kFrameThreads), args, 0, S.stream));
+    }
+    unsigned status = 0;
+    CK(cudaMemcpyAsync(&status, state + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    if (fc.cut) S.havePrev = true;
+    if (S.toolArmed) S.toolFrom = S.tool;
+    return status != 0u ? LCS_ERR_DEVICE_TIMEOUT : 0;
+}
+
 LCS_API int LCS_SetBarrierTest(int extraArrivals, float budgetSeconds) {
     if (extraArrivals < 0 || !(budgetSeconds > 0.f) || budgetSeconds > 10.f) return XPBD_ERR_BAD_ARG;
     S.syncTestExtra = extraArrivals;

@@ -29,6 +29,7 @@ extern "C" {
 #define XPBD_ERR_IRREGULAR_REST (-1005)
 #define LCS_ERR_UNSUPPORTED (-4001)
 #define LCS_ERR_DEVICE_TIMEOUT (-4002)
+#define LCS_ERR_SCRATCH_LIMIT (-4003)
 
 /* ReconInitDesc, 40 bytes (V/dc_recon.h ReconInitDesc; Python ReconDesc, native_backend.py:22-25). */
 typedef struct { int voxelCount, cornerCount, isectCount, surfaceEdgeCount, triCapacity, dimsX, dimsY, dimsZ; float L; int qefIters; } ReconInitDescAbi;
@@ -105,6 +106,20 @@ LCS_API int LCS_SetLaunchMode(int mode);         /* 0 automatic, 1 whole-GPU coo
  * never come and gives up after `budgetSeconds` (normal budget 2 s); LCS_Step then returns -4002 and
  * the context stays usable.  (0, 2.0) restores normal operation. */
 LCS_API int LCS_SetBarrierTest(int extraArrivals, float budgetSeconds);
+
+/* LCS_StepNoAlloc has no counterpart in the reference.  It advances the session by one frame
+ * exactly as LCS_Step does, for hosts that cannot let a plugin allocate GPU memory while they run
+ * (engines that own every device allocation through their own pool or budget, and real-time
+ * loops where an allocation, which may synchronise the device, would stall a frame).  It calls no
+ * cudaMalloc, cudaFree or other allocating routine: the frame's scratch (barrier counter, status,
+ * liveness record, per-tet compliances) is a fixed 4 MiB + 256 B array inside the library, which
+ * every GPU that loads the library holds until the process exits.  Limit: meshes of at most
+ * 524,288 tets; larger ones return LCS_ERR_SCRATCH_LIMIT (-4003) without stepping.  The first call
+ * on a device looks up that array's device address, so make it before any stream capture.  All
+ * calls share the one array (each call re-initialises what it needs), so calls that overlap on the
+ * GPU, e.g. from two processes' sessions on one device, race.  The inputs and outputs are the
+ * session's buffers set up by LCS_Init/LCS_InitPhysics/LCS_InitCut; the status is LCS_Step's. */
+LCS_API int LCS_StepNoAlloc(float dt);
 
 #ifdef __cplusplus
 }
