@@ -1,0 +1,192 @@
+"""Batched tissue instances through the GBT_Batch* C ABI (one persistent launch per frame for all).
+
+Each instance is a lattice from :func:`grid.build_grid` with the topology its own plain session
+would build, so instance i of a batch evolves exactly as a :class:`native_backend.PlainTissue` of
+the same grid and commands.  The C4 workload (``make_c4``) draws 256 instances of uneven size.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+from dataclasses import dataclass
+
+import numpy as np
+
+from .grid import METERS_PER_UNIT, TissueGrid, build_grid
+from .native_backend import DEFAULT_DLL, Capsule, Grasper, GraspParams, V3, pointer
+
+F, I, P = ct.c_float, ct.c_int32, ct.c_void_p
+
+
+class GbtInstanceDesc(ct.Structure):
+    _fields_ = [("dims_x", I), ("dims_y", I), ("dims_z", I), ("corner_pos", P), ("mass", P), ("pinned", P), ("active", P),
+                ("nbr_idx", P), ("rest_nbr", P), ("bend_pairs", P), ("bend_pair_count", I), ("tet_mu_v", P),
+                ("tet_kappa_v", P), ("stiffness_scale", F)]
+
+
+class GbtBatchParams(ct.Structure):
+    _fields_ = [("substeps", I)] + [(n, F) for n in ("ks", "cs", "kb", "cb", "alpha", "young", "poisson", "strain_damping")]
+
+
+SIGNATURES = (
+    ("GBT_BatchInit", (I, P, P), I), ("GBT_BatchSetGravity", (F, F, F), I), ("GBT_BatchSetGraspParams", (P,), None),
+    ("GBT_BatchSetTools", (P,), I), ("GBT_BatchStep", (F,), I), ("GBT_BatchStepMany", (F, I, P, I), I),
+    ("GBT_BatchGetPositions", (P,), I), ("GBT_BatchNodeRange", (I, P, P), I), ("GBT_BatchInfo", (P,), I),
+    ("GBT_BatchSetLaunch", (I, I), I), ("GBT_BatchAutotune", (F, I, P, P, P), I), ("GBT_BatchProfileEnable", (I,), None),
+    ("GBT_BatchProfileRead", (P,), I), ("GBT_BatchShutdown", (), None),
+)
+
+
+def capsule_tool(c: Capsule) -> Grasper:
+    """XpbdToolState of a contact model 0 capsule; the jaw box is parked far away (zero size)."""
+    far = (0.0, 1.0e4, 0.0)
+    return Grasper(V3(*c.a), V3(*c.b), c.radius, V3(*far), V3(0, 0, 1), V3(*far), V3(1, 0, 0), 0.0, 0.0, 0.0, 0.0)
+
+
+class TissueBatch:
+    """Many tissue instances advanced together.  ``tet_stiffness[i]`` = (mu*V, kappa*V) per tet in storage
+    order, or None for the (E, nu) bake; ``stiffness_scale[i]`` multiplies an instance's stiffnesses."""
+
+    def __init__(self, grids, dt=1 / 60, substeps=10, ks=1e6, young_pa=6000.0, poisson=0.25, strain_damping_s=0.04,
+                 tet_stiffness=None, stiffness_scale=None, grasp_params: GraspParams | None = None, dll_path=None):
+        self.grids, self.dt = list(grids), float(dt)
+        self.dll = ct.CDLL(str(dll_path or DEFAULT_DLL))
+        self.f = {}
+        for name, args, res in SIGNATURES:
+            fn = self.dll[name]
+            fn.argtypes, fn.restype = args, res
+            self.f[name] = fn
+        self._keep = []
+        descs = (GbtInstanceDesc * len(self.grids))()
+        for i, g in enumerate(self.grids):
+            mu = kappa = None
+            if tet_stiffness is not None and tet_stiffness[i] is not None:
+                mu = np.ascontiguousarray(tet_stiffness[i][0], dtype=np.float32)
+                kappa = np.ascontiguousarray(tet_stiffness[i][1], dtype=np.float32)
+                self._keep += [mu, kappa]
+            descs[i] = GbtInstanceDesc(*g.dims, pointer(g.positions), pointer(g.mass), pointer(g.pinned), pointer(g.active),
+                                       pointer(g.neighbors), pointer(g.rest_neighbors), pointer(g.bends), len(g.positions) * 15,
+                                       pointer(mu) if mu is not None else None, pointer(kappa) if kappa is not None else None,
+                                       float(stiffness_scale[i]) if stiffness_scale is not None else 0.0)
+        params = GbtBatchParams(int(substeps), ks, 0.0, 0.0, 0.0, 0.0, young_pa * METERS_PER_UNIT, poisson, strain_damping_s)
+        self.check("GBT_BatchInit", len(self.grids), ct.byref(descs), ct.byref(params))
+        self.closed = False
+        if grasp_params is not None:
+            self.f["GBT_BatchSetGraspParams"](ct.byref(grasp_params))
+        self.ranges = []
+        for i in range(len(self.grids)):
+            base, count = I(), I()
+            self.check("GBT_BatchNodeRange", i, ct.byref(base), ct.byref(count))
+            self.ranges.append((base.value, count.value))
+        self.total_nodes = sum(c for _, c in self.ranges)
+
+    def check(self, name, *args):
+        rc = self.f[name](*args)
+        if rc != 0:
+            raise RuntimeError(f"{name} failed with native status {rc}")
+
+    def info(self):
+        out = np.zeros(8, dtype=np.int32)
+        self.check("GBT_BatchInfo", pointer(out))
+        keys = ("instances", "nodes", "edges", "tets", "edge_colours", "tet_colours", "mode", "threads")
+        return dict(zip(keys, (int(v) for v in out)))
+
+    def set_gravity(self, gx, gy, gz):
+        self.check("GBT_BatchSetGravity", gx, gy, gz)
+
+    def set_capsules(self, capsules):
+        tools = (Grasper * len(self.grids))(*(capsule_tool(c) for c in capsules))
+        self.check("GBT_BatchSetTools", ct.byref(tools))
+
+    def step(self):
+        self.check("GBT_BatchStep", self.dt)
+
+    def step_many(self, capsules_per_step=None, steps=None, use_graph=True):
+        """Advance ``steps`` frames (or ``len(capsules_per_step)``), one capsule per instance per frame."""
+        if capsules_per_step is not None:
+            steps = len(capsules_per_step)
+            tools = (Grasper * (steps * len(self.grids)))(*(capsule_tool(c) for frame in capsules_per_step for c in frame))
+            self.check("GBT_BatchStepMany", self.dt, steps, ct.byref(tools), int(use_graph))
+        else:
+            self.check("GBT_BatchStepMany", self.dt, int(steps), None, int(use_graph))
+
+    def set_launch(self, mode, threads=256):
+        self.check("GBT_BatchSetLaunch", mode, threads)
+
+    def autotune(self, trial_steps=3):
+        mode, threads, ms = I(), I(), (F * 3)()
+        self.check("GBT_BatchAutotune", self.dt, trial_steps, ct.byref(mode), ct.byref(threads), ms)
+        return {"mode": mode.value, "threads": threads.value, "ms_per_frame": [float(v) for v in ms]}
+
+    def positions(self):
+        out = np.empty((self.total_nodes, 3), dtype=np.float32)
+        self.check("GBT_BatchGetPositions", pointer(out))
+        return out
+
+    def instance_positions(self, all_positions, i):
+        base, count = self.ranges[i]
+        return all_positions[base:base + count]
+
+    def profile(self, enabled):
+        self.f["GBT_BatchProfileEnable"](int(enabled))
+
+    def profile_read(self):
+        ms = F()
+        self.check("GBT_BatchProfileRead", ct.byref(ms))
+        return ms.value
+
+    def close(self):
+        if not getattr(self, "closed", True):
+            self.f["GBT_BatchShutdown"]()
+            self.closed = True
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+@dataclass
+class BatchWorkload:
+    grids: list
+    compliance: np.ndarray            # per instance, 1/Pa (Young's modulus 1/c)
+    capsule_paths: list               # per instance: [initial, step 1, ..., step n]
+    steps: int
+    substeps: int = 10
+
+    def stiffness_scale(self, young_pa=6000.0):
+        """Per-instance multiplier of the (E, nu) bake: Young's modulus 1/c (Pa) over E, in FP32."""
+        return (np.float32(1) / (self.compliance.astype(np.float32) * np.float32(young_pa))).astype(np.float32)
+
+    def capsules_at(self, step):
+        return [path[min(step, len(path) - 1)] for path in self.capsule_paths]
+
+
+def make_c4(count=256, seed=4, steps=100, substeps=10, low=1e-7, high=1e-5, size_range=((8, 32), (4, 16), (8, 32))):
+    """256 instances with cells x, y(up), z drawn uniformly from [8,32] x [4,16] x [8,32], one log-uniform
+    compliance per instance, and a capsule per instance pressed into its top face over ``steps`` steps."""
+    rng = np.random.default_rng(seed)
+    grids, paths = [], []
+    for _ in range(count):
+        cells = [int(rng.integers(lo, hi + 1)) for lo, hi in size_range]
+        size = tuple(np.float64(c) * 0.2 - 0.02 for c in cells)
+        g = build_grid(0.2, size=size, density=1000.0)
+        grids.append(g)
+        p = g.positions[g.active != 0]
+        lo, hi = p.min(axis=0), p.max(axis=0)
+        mid, half = (lo + hi) / 2, (hi - lo) / 2
+        angle = rng.uniform(0.0, np.pi)
+        axis = np.array((np.cos(angle), 0.0, np.sin(angle)))
+        length = 0.6 * float(min(half[0], half[2])) * 2
+        r = 0.25
+        cx = mid[0] + rng.uniform(-0.2, 0.2) * half[0]
+        cz = mid[2] + rng.uniform(-0.2, 0.2) * half[2]
+        y0, y1 = hi[1] + r + 0.05, hi[1] + r - 0.25 * (hi[1] - lo[1])
+
+        def pose(y, cx=cx, cz=cz, axis=axis, length=length, r=r):
+            c = np.array((cx, y, cz))
+            return Capsule(tuple(c - axis * length / 2), tuple(c + axis * length / 2), r)
+
+        paths.append([pose(y0)] + [pose(y0 + (y1 - y0) * (k + 1) / steps) for k in range(steps)])
+    compliance = np.exp(rng.uniform(np.log(low), np.log(high), count))
+    return BatchWorkload(grids, compliance, paths, steps, substeps)

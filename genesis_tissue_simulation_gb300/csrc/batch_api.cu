@@ -1,0 +1,575 @@
+// Batched tissue instances: many independent meshes of uneven size advanced by one persistent launch
+// per frame over a packed instance table.  No counterpart in the reference, which runs one global
+// session per process (endoscopic_tissue/native_backend.py:213-218).
+//
+// Every instance gets exactly the topology of its own plain session (mesh_build.h: the reference's
+// greedy colourings), so a batched instance evolves bit for bit as it would alone.  The packed
+// table stores colour c of every instance together (colour-major, instances in table order), which
+// gives two ways to run a frame, picked by GBT_BatchAutotune:
+//   lockstep   all instances advance colour by colour in one cooperative grid (frameKernelGrid);
+//   instances  one CTA per instance at a time, longest-processing-time packing over the CTAs, with
+//              only __syncthreads between colours (frameKernelInstances<256|512>).
+// GBT_BatchStepMany advances several frames with one CUDA graph launch: the instrument frames of all
+// substeps are evaluated on the host (contactFrame, the same operations as on the device), uploaded
+// once, and the frame launches are replayed from a captured graph.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "frame_kernels.h"
+#include "mesh_build.h"
+#include "../../include/gbtissue.h"
+
+using namespace gbt;
+
+namespace {
+
+template <class T> struct Buf {
+    T* p = nullptr; size_t n = 0;
+    cudaError_t alloc(size_t count) { release(); n = count; return cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)); }
+    cudaError_t upload(const T* h, size_t count, cudaStream_t s) {
+        cudaError_t e = alloc(count);
+        if (e == cudaSuccess && count) e = cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
+        return e;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+};
+
+struct Batch {
+    cudaStream_t stream = nullptr;
+    int device = 0, smCount = 0, gridBlocks = 0, clockKHz = 2000000;
+    bool ready = false;
+    int count = 0, N = 0, E = 0, B = 0, T = 0;
+    int numSubsteps = 10;
+    float ks = 0, kb = 0, alpha = 0, betaS = 0, betaB = 0, youngE = 0, poisson = 0.45f, strainDamping = 0;
+    int nEdgeColors = 0, nBendColors = 0, nTetColors = 0;
+    std::vector<int> nodeBase, nodeCount, tetCount, edgeCount;
+    float typeB[6][9];
+    Buf<float4> pos, prev, vel, ext;
+    Buf<int> pinned, active, nbr, edgeOwner, edgeLive, bendSrc, bendLive, tetMeta, tetOwner, edgeSupport, nodeInstance;
+    Buf<int2> edgeEnds, unionEdge, unionBend, unionTet, instEdge, instBend, instTet;
+    Buf<float> edgeRest;
+    Buf<int4> bendIJK, tetIds;
+    Buf<BendRecord> bendPairs;
+    Buf<float2> tetStiff, tetAlpha;
+    Buf<int> nodeBaseD, nodeCountD, order, ctaStart;
+    Buf<unsigned> derived, state;
+    Buf<ContactFrame> frames;
+    unsigned* hostStatus = nullptr;
+    ContactFrame* framesHost = nullptr; size_t framesHostCap = 0;
+    // instruments
+    std::vector<ToolPose> toolFrom, tool;
+    bool armed = false;
+    ContactParams cp{0.02f, 1.0e-7f, 0.5f, 0.045f, 0.25f};
+    float lastH = -1.f;
+    // launch
+    int mode = 0, threads = 256, ctas = 0;            // mode 0 lockstep grid, 1 one CTA per instance
+    cudaGraphExec_t graph = nullptr; int graphSteps = 0; int graphMode = -1; float graphDt = 0.f;
+    bool profile = false; std::vector<cudaEvent_t> events;
+};
+Batch G;
+
+#define CK(call) do { cudaError_t _e = (call); if (_e != cudaSuccess) return -(int)_e; } while (0)
+
+void dropGraph() { if (G.graph) cudaGraphExecDestroy(G.graph); G.graph = nullptr; G.graphSteps = 0; }
+
+void releaseAll() {
+    dropGraph();
+    for (auto* b : {&G.pos, &G.prev, &G.vel, &G.ext}) b->release();
+    for (auto* b : {&G.pinned, &G.active, &G.nbr, &G.edgeOwner, &G.edgeLive, &G.bendSrc, &G.bendLive, &G.tetMeta, &G.tetOwner,
+                    &G.edgeSupport, &G.nodeInstance, &G.nodeBaseD, &G.nodeCountD, &G.order, &G.ctaStart}) b->release();
+    for (auto* b : {&G.edgeEnds, &G.unionEdge, &G.unionBend, &G.unionTet, &G.instEdge, &G.instBend, &G.instTet}) b->release();
+    G.edgeRest.release(); G.bendIJK.release(); G.tetIds.release(); G.bendPairs.release(); G.tetStiff.release(); G.tetAlpha.release();
+    G.derived.release(); G.state.release(); G.frames.release();
+    if (G.framesHost) cudaFreeHost(G.framesHost);
+    G.framesHost = nullptr; G.framesHostCap = 0;
+    for (cudaEvent_t e : G.events) cudaEventDestroy(e);
+    G.events.clear();
+    G.ready = false; G.armed = false; G.lastH = -1.f;
+}
+
+int ensureDevice() {
+    if (G.stream) return 0;
+    CK(cudaGetDevice(&G.device));
+    CK(cudaDeviceGetAttribute(&G.smCount, cudaDevAttrMultiProcessorCount, G.device));
+    int khz = 0;
+    if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, G.device) == cudaSuccess && khz > 0) G.clockKHz = khz;
+    CK(cudaStreamCreateWithFlags(&G.stream, cudaStreamNonBlocking));
+    CK(cudaMallocHost(&G.hostStatus, 4 * sizeof(unsigned)));
+    int perSm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, frameKernelGrid, kFrameThreads, 0));
+    G.gridBlocks = std::max(1, perSm) * G.smCount;
+    return 0;
+}
+
+// Longest-processing-time packing of instances (by tet count) over `ctas` CTAs.
+int packInstances(int ctas) {
+    ctas = std::max(1, std::min(ctas, G.count));
+    std::vector<int> byWork(G.count);
+    std::iota(byWork.begin(), byWork.end(), 0);
+    std::stable_sort(byWork.begin(), byWork.end(), [](int a, int b) { return G.tetCount[a] > G.tetCount[b]; });
+    std::vector<long long> load(ctas, 0);
+    std::vector<std::vector<int>> lists(ctas);
+    for (int i : byWork) {
+        int best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        lists[best].push_back(i);
+        load[best] += G.tetCount[i] + 1;
+    }
+    std::vector<int> order, start(1, 0);
+    for (auto& l : lists) { order.insert(order.end(), l.begin(), l.end()); start.push_back((int)order.size()); }
+    CK(G.order.upload(order.data(), order.size(), G.stream));
+    CK(G.ctaStart.upload(start.data(), start.size(), G.stream));
+    G.ctas = ctas;
+    return 0;
+}
+
+DeviceMesh batchMesh() {
+    DeviceMesh m{};
+    m.nNodes = G.N; m.nodeBase = 0; m.dx = m.dy = m.dz = 0;
+    m.pos = G.pos.p; m.prev = G.prev.p; m.vel = G.vel.p; m.ext = G.ext.p;
+    m.pinned = G.pinned.p; m.active = G.active.p; m.nbr = G.nbr.p;
+    m.nEdgeColors = G.nEdgeColors; m.edgeRange = G.unionEdge.p;
+    m.edgeEnds = G.edgeEnds.p; m.edgeRest = G.edgeRest.p; m.edgeOwner = G.edgeOwner.p; m.edgeLive = G.edgeLive.p;
+    m.nBendColors = G.nBendColors; m.bendRange = G.unionBend.p;
+    m.bendIJK = G.bendIJK.p; m.bendSrc = G.bendSrc.p; m.bendLive = G.bendLive.p; m.bendPairs = G.bendPairs.p; m.nBendPairs = (int)G.bendPairs.n;
+    m.nTetColors = G.nTetColors; m.tetRange = G.unionTet.p;
+    m.tetIds = G.tetIds.p; m.tetMeta = G.tetMeta.p; m.tetOwner = G.tetOwner.p; m.tetAlpha = G.tetAlpha.p; m.tetStiff = G.tetStiff.p;
+    m.edgeSupport = G.edgeSupport.p;
+    m.nodeInstance = G.nodeInstance.p; m.contactFrames = G.frames.p; m.nInstances = G.count;
+    std::memcpy(m.typeB, G.typeB, sizeof(G.typeB));
+    return m;
+}
+
+FrameCoeffs frameCoeffs(float h) {
+    FrameCoeffs fc{};
+    const int N = G.numSubsteps;
+    fc.numSubsteps = N; fc.substeps = N; fc.firstSubstep = 0;
+    float at = G.ks > 0.f ? 1.f / (G.ks * h * h) : 0.f;
+    fc.velScale = 1.f / (1.f + G.alpha * h);
+    fc.betaGammaHS = at * G.betaS * h;
+    fc.alphaTilde = at;
+    fc.doBend = (G.B > 0 && G.kb > 0.f) ? 1 : 0;
+    fc.alphaB = fc.doBend ? 1.f / (G.kb * h * h) : 0.f;
+    fc.betaGammaHB = fc.alphaB * G.betaB * h;
+    fc.h = h; fc.invH = 1.f / h; fc.invH2 = 1.f / (h * h);
+    fc.doStrain = (G.T > 0 && G.youngE > 0.f) ? 1 : 0;
+    fc.fallback = (fc.doStrain && G.ks <= 0.f) ? 1 : 0;
+    fc.doEdges = (G.ks > 0.f || fc.fallback) ? 1 : 0;
+    fc.fallbackInvEh2 = fc.fallback ? 1.f / (G.youngE * h * h) : 0.f;
+    fc.perpDamp = G.betaS > 0.f ? 1 : 0;
+    fc.betaS = G.betaS;
+    fc.omega = 1.f;
+    fc.dampingOverH = fmaxf(0.f, G.strainDamping) / h;
+    fc.contact = G.armed ? 1 : 0;
+    fc.contactAlphaH2 = G.cp.contactAlpha / (h * h);
+    fc.spinBudget = (long long)(2.0 * 1e3 * G.clockKHz);
+    return fc;
+}
+
+int ensureFramesHost(size_t records) {
+    if (records <= G.framesHostCap) return 0;
+    if (G.framesHost) cudaFreeHost(G.framesHost);
+    G.framesHost = nullptr;
+    CK(cudaMallocHost(&G.framesHost, records * sizeof(ContactFrame)));
+    G.framesHostCap = records;
+    return 0;
+}
+
+// Instrument frames of `steps` frames into the pinned staging area, with the single session's command
+// semantics (xpbd_set_tool, xpbd_solver.cu:2327-2334, 3467-3483): a new command for frame k makes the
+// previous command its starting pose (itself when no instrument was armed yet); the frame
+// interpolates from it; after the frame the starting pose is the command.
+void stageFrames(int steps, const ToolPose* tools, float h) {
+    const int NS = G.numSubsteps;
+    float alpha = G.cp.contactAlpha / (h * h);
+    std::vector<ToolPose> from = G.toolFrom, to = G.tool;
+    bool armed = G.armed;
+    for (int k = 0; k < steps; k++) {
+        if (tools) {
+            std::vector<ToolPose> next(tools + (size_t)k * G.count, tools + (size_t)(k + 1) * G.count);
+            from = armed ? to : next;
+            to = next;
+            armed = true;
+        }
+        for (int s = 0; s < NS; s++) {
+            float t = fminf(1.f, (float)(s + 1) / (float)NS);
+            for (int i = 0; i < G.count; i++)
+                G.framesHost[((size_t)k * NS + s) * G.count + i] = contactFrame(from[i], to[i], t, G.cp, alpha);
+        }
+        from = to;
+    }
+    G.tool = to;
+    G.toolFrom = to;
+    G.armed = armed;
+}
+
+int launchFrame(const FrameCoeffs& fc, const ContactFrame* frames) {
+    DeviceMesh m = batchMesh();
+    m.contactFrames = frames;
+    if (G.mode == 0) {
+        CutParams cu{};
+        ToolPose none{};
+        ContactParams cp = G.cp;
+        unsigned* state = G.state.p;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(G.gridBlocks); cfg.blockDim = dim3(kFrameThreads); cfg.stream = G.stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative; attr[0].val.cooperative = 1;
+        cfg.attrs = attr; cfg.numAttrs = 1;
+        CK(cudaMemsetAsync(state + 1, 0, sizeof(unsigned), G.stream));
+        CK(cudaLaunchKernelEx(&cfg, frameKernelGrid, m, fc, none, none, cp, cu, state));
+    } else {
+        InstanceTable it{G.nodeBaseD.p, G.nodeCountD.p, G.instEdge.p, G.instBend.p, G.instTet.p, G.order.p, G.ctaStart.p, G.derived.p};
+        if (G.threads == 512) frameKernelInstances512<<<G.ctas, 512, 0, G.stream>>>(m, fc, G.cp, it);
+        else frameKernelInstances256<<<G.ctas, 256, 0, G.stream>>>(m, fc, G.cp, it);
+        CK(cudaGetLastError());
+    }
+    return 0;
+}
+
+int prepareAlphas(float h) {
+    if (G.T > 0 && G.youngE > 0.f && h != G.lastH) {
+        tetAlphaKernel<<<(G.T + 255) / 256, 256, 0, G.stream>>>(G.T, 1.f / (h * h), G.tetStiff.p, G.tetAlpha.p);
+        CK(cudaGetLastError());
+        G.lastH = h;
+    }
+    return 0;
+}
+
+// Advance `steps` frames; `tools` is [steps][count] XpbdToolState or null (instruments unchanged).
+int stepFrames(float dt, int steps, const ToolPose* tools, bool useGraph) {
+    if (!G.ready) return XPBD_ERR_NOT_READY;
+    if (steps <= 0) return XPBD_ERR_BAD_ARG;
+    float h = dt / (float)G.numSubsteps;
+    if (!(h > 0.f) || !std::isfinite(h)) return XPBD_ERR_BAD_DT;
+    int rc = prepareAlphas(h);
+    if (rc) return rc;
+    const size_t per = (size_t)G.numSubsteps * G.count;
+    rc = ensureFramesHost(per * steps);
+    if (rc) return rc;
+    bool contact = G.armed || tools;
+    if (contact) stageFrames(steps, tools, h);
+    FrameCoeffs fc = frameCoeffs(h);
+    if (G.frames.n < per * steps) { CK(G.frames.alloc(per * steps)); dropGraph(); }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (G.profile) { CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1)); CK(cudaEventRecord(e0, G.stream)); }
+    CK(cudaMemsetAsync(G.state.p + 2, 0, sizeof(unsigned), G.stream));
+    if (useGraph) {
+        if (G.graph && (G.graphSteps != steps || G.graphMode != G.mode * 1000 + G.threads + (fc.contact ? 1 : 0) || G.graphDt != dt)) dropGraph();
+        if (!G.graph) {
+            CK(cudaStreamBeginCapture(G.stream, cudaStreamCaptureModeThreadLocal));
+            CK(cudaMemcpyAsync(G.frames.p, G.framesHost, per * steps * sizeof(ContactFrame), cudaMemcpyHostToDevice, G.stream));
+            for (int k = 0; k < steps && rc == 0; k++) rc = launchFrame(fc, G.frames.p + per * k);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(G.stream, &g);
+            if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+            if (e != cudaSuccess) return -(int)e;
+            e = cudaGraphInstantiate(&G.graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return -(int)e;
+            G.graphSteps = steps; G.graphMode = G.mode * 1000 + G.threads + (fc.contact ? 1 : 0); G.graphDt = dt;
+        }
+        CK(cudaGraphLaunch(G.graph, G.stream));
+    } else {
+        if (contact) CK(cudaMemcpyAsync(G.frames.p, G.framesHost, per * steps * sizeof(ContactFrame), cudaMemcpyHostToDevice, G.stream));
+        for (int k = 0; k < steps; k++) {
+            rc = launchFrame(fc, G.frames.p + per * k);
+            if (rc) return rc;
+        }
+    }
+    if (G.profile) { CK(cudaEventRecord(e1, G.stream)); G.events.push_back(e0); G.events.push_back(e1); }
+    CK(cudaMemcpyAsync(G.hostStatus, G.state.p + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, G.stream));
+    CK(cudaStreamSynchronize(G.stream));
+    return G.hostStatus[0] != 0u ? LCS_ERR_DEVICE_TIMEOUT : 0;
+}
+
+}  // namespace
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+LCS_API int GBT_BatchInit(int count, const GbtInstanceDesc* inst, const GbtBatchParams* params) {
+    releaseAll();
+    if (count <= 0 || !inst || !params) return XPBD_ERR_BAD_ARG;
+    if (!std::isfinite(params->youngE) || params->youngE < 0.f || !std::isfinite(params->poisson) || params->poisson < 0.f ||
+        params->poisson >= 0.5f || !std::isfinite(params->strainDamping) || params->strainDamping < 0.f) return -2004;
+    int rc = ensureDevice();
+    if (rc) return rc;
+    G.N = G.E = G.B = G.T = 0;
+    G.nEdgeColors = G.nBendColors = G.nTetColors = 0;
+    G.mode = 0; G.threads = 256;
+    G.count = count;
+    G.numSubsteps = params->substeps > 0 ? params->substeps : 20;
+    G.ks = params->ks; G.kb = params->kb; G.alpha = params->alpha; G.betaS = params->cs; G.betaB = params->cb;
+    G.youngE = params->youngE; G.poisson = params->poisson; G.strainDamping = params->strainDamping;
+    std::vector<HostMesh> meshes(count);
+    for (int i = 0; i < count; i++) {
+        const GbtInstanceDesc& d = inst[i];
+        if (d.dimsX <= 0 || d.dimsY <= 0 || d.dimsZ <= 0 || !d.cornerPos || !d.mass || !d.pinned || !d.active || !d.nbrIdx ||
+            !d.restNbr || d.bendPairCount < 0 || (d.bendPairCount > 0 && !d.bendPairs)) return XPBD_ERR_BAD_ARG;
+        int n = (d.dimsX + 1) * (d.dimsY + 1) * (d.dimsZ + 1);
+        std::vector<float> zeros(3 * (size_t)n, 0.f);
+        MeshInput in{d.dimsX, d.dimsY, d.dimsZ, d.cornerPos, d.mass, d.pinned, d.active, zeros.data(), d.nbrIdx, d.restNbr,
+                     d.bendPairs, d.bendPairCount, G.youngE, G.poisson};
+        rc = buildHostMesh(in, meshes[i]);
+        if (rc) return rc;
+        HostMesh& hm = meshes[i];
+        if (d.tetMuV && d.tetKappaV)   // per-tet material in storage order, placed through the colour order
+            for (int k = 0; k < hm.T; k++) {
+                int t = hm.tetColorOrder[k];
+                if (!(d.tetMuV[t] > 0.f) || !(d.tetKappaV[t] > 0.f)) return XPBD_ERR_BAD_ARG;
+                hm.tetStiff[k] = make_float2(d.tetMuV[t], d.tetKappaV[t]);
+            }
+        if (d.stiffnessScale > 0.f && d.stiffnessScale != 1.f) {
+            if (!std::isfinite(d.stiffnessScale)) return XPBD_ERR_BAD_ARG;
+            for (auto& s : hm.tetStiff) s = make_float2(s.x * d.stiffnessScale, s.y * d.stiffnessScale);
+        }
+        for (int a = 0; a < 54; a++)   // one rest shape per Kuhn type for the whole table
+            if (std::fabs((&hm.typeB[0][0])[a] - (&meshes[0].typeB[0][0])[a]) > 1e-6f * (1.f + std::fabs((&meshes[0].typeB[0][0])[a])))
+                return XPBD_ERR_IRREGULAR_REST;
+    }
+    std::memcpy(G.typeB, meshes[0].typeB, sizeof(G.typeB));
+    // instance offsets and colour counts
+    G.nodeBase.assign(count, 0); G.nodeCount.assign(count, 0); G.tetCount.assign(count, 0); G.edgeCount.assign(count, 0);
+    int bendPairBase = 0;
+    std::vector<int> bendBase(count);
+    for (int i = 0; i < count; i++) {
+        G.nodeBase[i] = G.N; G.nodeCount[i] = meshes[i].N; G.tetCount[i] = meshes[i].T; G.edgeCount[i] = meshes[i].E;
+        G.N += meshes[i].N; G.E += meshes[i].E; G.B += meshes[i].B; G.T += meshes[i].T;
+        bendBase[i] = bendPairBase; bendPairBase += inst[i].bendPairCount;
+        G.nEdgeColors = std::max(G.nEdgeColors, (int)meshes[i].edgeColorOff.size() - 1);
+        G.nBendColors = std::max(G.nBendColors, (int)meshes[i].bendColorOff.size() - 1);
+        G.nTetColors = std::max(G.nTetColors, (int)meshes[i].tetColorOff.size() - 1);
+    }
+    // node arrays and topology, instance after instance
+    std::vector<float4> pos, ext; std::vector<int> pinned, active, nbr, nodeInst;
+    std::vector<BendRecord> bends;
+    pos.reserve(G.N); ext.reserve(G.N);
+    for (int i = 0; i < count; i++) {
+        const HostMesh& hm = meshes[i];
+        const int base = G.nodeBase[i];
+        pos.insert(pos.end(), hm.pos.begin(), hm.pos.end());
+        ext.insert(ext.end(), hm.ext.begin(), hm.ext.end());
+        pinned.insert(pinned.end(), inst[i].pinned, inst[i].pinned + hm.N);
+        active.insert(active.end(), inst[i].active, inst[i].active + hm.N);
+        for (int k = 0; k < 6 * hm.N; k++) nbr.push_back(inst[i].nbrIdx[k] >= 0 ? inst[i].nbrIdx[k] + base : -1);
+        nodeInst.insert(nodeInst.end(), hm.N, i);
+        const BendRecord* bp = (const BendRecord*)inst[i].bendPairs;
+        for (int b = 0; b < inst[i].bendPairCount; b++) {
+            BendRecord r = bp[b];
+            r.i += base; r.j = r.j >= 0 ? r.j + base : r.j; r.k = r.k >= 0 ? r.k + base : r.k;
+            bends.push_back(r);
+        }
+    }
+    // colour-major element tables: colour c of instance 0, of instance 1, ...
+    std::vector<int2> eEnds, uEdge, uBend, uTet, iEdge((size_t)count * G.nEdgeColors), iBend((size_t)count * G.nBendColors),
+        iTet((size_t)count * G.nTetColors);
+    std::vector<float> eRest; std::vector<int> eOwner, bSrc, tMeta, tOwner; std::vector<int4> bIJK, tIds; std::vector<float2> tStiff;
+    auto colourSlice = [](const std::vector<int>& off, int c) {
+        return c + 1 < (int)off.size() ? std::make_pair(off[c], off[c + 1]) : std::make_pair(0, 0);
+    };
+    for (int c = 0; c < G.nEdgeColors; c++) {
+        int lo = (int)eEnds.size();
+        for (int i = 0; i < count; i++) {
+            const HostMesh& hm = meshes[i];
+            const int base = G.nodeBase[i];
+            auto sl = colourSlice(hm.edgeColorOff, c);
+            iEdge[(size_t)i * G.nEdgeColors + c] = make_int2((int)eEnds.size(), (int)eEnds.size() + sl.second - sl.first);
+            for (int k = sl.first; k < sl.second; k++) {
+                eEnds.push_back(make_int2(hm.edgeEnds[k].x + base, hm.edgeEnds[k].y + base));
+                eRest.push_back(hm.edgeRest[k]);
+                eOwner.push_back(hm.edgeOwner[k] + 6 * base);
+            }
+        }
+        uEdge.push_back(make_int2(lo, (int)eEnds.size()));
+    }
+    for (int c = 0; c < G.nBendColors; c++) {
+        int lo = (int)bIJK.size();
+        for (int i = 0; i < count; i++) {
+            const HostMesh& hm = meshes[i];
+            const int base = G.nodeBase[i];
+            auto sl = colourSlice(hm.bendColorOff, c);
+            iBend[(size_t)i * G.nBendColors + c] = make_int2((int)bIJK.size(), (int)bIJK.size() + sl.second - sl.first);
+            for (int k = sl.first; k < sl.second; k++) {
+                int4 r = hm.bendIJK[k];
+                bIJK.push_back(make_int4(r.x + base, r.y + base, r.z + base, r.w));
+                bSrc.push_back(hm.bendSrc[k] + bendBase[i]);
+            }
+        }
+        uBend.push_back(make_int2(lo, (int)bIJK.size()));
+    }
+    for (int c = 0; c < G.nTetColors; c++) {
+        int lo = (int)tIds.size();
+        for (int i = 0; i < count; i++) {
+            const HostMesh& hm = meshes[i];
+            const int base = G.nodeBase[i];
+            auto sl = colourSlice(hm.tetColorOff, c);
+            iTet[(size_t)i * G.nTetColors + c] = make_int2((int)tIds.size(), (int)tIds.size() + sl.second - sl.first);
+            for (int k = sl.first; k < sl.second; k++) {
+                int4 d = hm.tetIds[k];
+                tIds.push_back(make_int4(d.x + base, d.y + base, d.z + base, d.w + base));
+                tMeta.push_back(hm.tetMeta[k]);
+                for (int o = 0; o < 3; o++) tOwner.push_back(hm.tetOwner[3 * k + o] + 6 * base);
+                tStiff.push_back(hm.tetStiff[k]);
+            }
+        }
+        uTet.push_back(make_int2(lo, (int)tIds.size()));
+    }
+    std::vector<float4> zero4(G.N, make_float4(0, 0, 0, 0));
+    std::vector<int> ones(std::max(std::max(G.E, G.B), 1), 1), zeros6((size_t)6 * G.N, 0);
+    std::vector<unsigned> derived(count, ~0u), state(4, 0u);
+    state[0] = ~0u;
+    CK(G.pos.upload(pos.data(), G.N, G.stream)); CK(G.prev.upload(pos.data(), G.N, G.stream));
+    CK(G.vel.upload(zero4.data(), G.N, G.stream)); CK(G.ext.upload(ext.data(), G.N, G.stream));
+    CK(G.pinned.upload(pinned.data(), G.N, G.stream)); CK(G.active.upload(active.data(), G.N, G.stream));
+    CK(G.nbr.upload(nbr.data(), nbr.size(), G.stream)); CK(G.nodeInstance.upload(nodeInst.data(), G.N, G.stream));
+    CK(G.edgeEnds.upload(eEnds.data(), eEnds.size(), G.stream)); CK(G.edgeRest.upload(eRest.data(), eRest.size(), G.stream));
+    CK(G.edgeOwner.upload(eOwner.data(), eOwner.size(), G.stream)); CK(G.edgeLive.upload(ones.data(), G.E, G.stream));
+    CK(G.bendIJK.upload(bIJK.data(), bIJK.size(), G.stream)); CK(G.bendSrc.upload(bSrc.data(), bSrc.size(), G.stream));
+    CK(G.bendLive.upload(ones.data(), G.B, G.stream)); CK(G.bendPairs.upload(bends.data(), bends.size(), G.stream));
+    CK(G.tetIds.upload(tIds.data(), tIds.size(), G.stream)); CK(G.tetMeta.upload(tMeta.data(), tMeta.size(), G.stream));
+    CK(G.tetOwner.upload(tOwner.data(), tOwner.size(), G.stream)); CK(G.tetStiff.upload(tStiff.data(), tStiff.size(), G.stream));
+    CK(G.tetAlpha.alloc(G.T)); CK(G.edgeSupport.upload(zeros6.data(), zeros6.size(), G.stream));
+    CK(G.unionEdge.upload(uEdge.data(), uEdge.size(), G.stream)); CK(G.unionBend.upload(uBend.data(), uBend.size(), G.stream));
+    CK(G.unionTet.upload(uTet.data(), uTet.size(), G.stream));
+    CK(G.instEdge.upload(iEdge.data(), iEdge.size(), G.stream)); CK(G.instBend.upload(iBend.data(), iBend.size(), G.stream));
+    CK(G.instTet.upload(iTet.data(), iTet.size(), G.stream));
+    CK(G.nodeBaseD.upload(G.nodeBase.data(), count, G.stream)); CK(G.nodeCountD.upload(G.nodeCount.data(), count, G.stream));
+    CK(G.derived.upload(derived.data(), count, G.stream)); CK(G.state.upload(state.data(), 4, G.stream));
+    rc = packInstances(G.smCount * 2);
+    if (rc) return rc;
+    G.tool.assign(count, ToolPose{}); G.toolFrom = G.tool;
+    CK(cudaStreamSynchronize(G.stream));
+    G.ready = true;
+    return 0;
+}
+
+LCS_API int GBT_BatchSetGravity(float gx, float gy, float gz) {
+    if (!G.ready) return XPBD_ERR_NOT_READY;
+    if (!std::isfinite(gx) || !std::isfinite(gy) || !std::isfinite(gz)) return XPBD_ERR_BAD_ARG;
+    gravityKernel<<<(G.N + 255) / 256, 256, 0, G.stream>>>(G.N, gx, gy, gz, G.ext.p);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(G.stream));
+    return 0;
+}
+
+LCS_API void GBT_BatchSetGraspParams(const GraspParamsAbi* p) {
+    if (!p) return;
+    G.cp.jawGapClosed = p->jawGapClosed; G.cp.contactAlpha = p->contactAlpha; G.cp.ccdVelThresh = p->ccdVelThresh;
+    G.cp.ccdMaxDisp = p->ccdMaxDisp; G.cp.ccdOmega = p->ccdOmega;
+}
+
+LCS_API int GBT_BatchSetTools(const void* tools) {
+    if (!G.ready || !tools) return XPBD_ERR_BAD_ARG;
+    const ToolPose* t = (const ToolPose*)tools;
+    G.toolFrom = G.armed ? G.tool : std::vector<ToolPose>(t, t + G.count);
+    G.tool.assign(t, t + G.count);
+    G.armed = true;
+    return 0;
+}
+
+LCS_API int GBT_BatchStep(float dt) { return stepFrames(dt, 1, nullptr, false); }
+
+LCS_API int GBT_BatchStepMany(float dt, int steps, const void* tools, int useGraph) {
+    return stepFrames(dt, steps, (const ToolPose*)tools, useGraph != 0);
+}
+
+LCS_API int GBT_BatchGetPositions(float* out3N) {
+    if (!G.ready || !out3N) return XPBD_ERR_BAD_ARG;
+    std::vector<float4> p(G.N);
+    CK(cudaMemcpyAsync(p.data(), G.pos.p, G.N * sizeof(float4), cudaMemcpyDeviceToHost, G.stream));
+    CK(cudaStreamSynchronize(G.stream));
+    for (int i = 0; i < G.N; i++) { out3N[3 * i] = p[i].x; out3N[3 * i + 1] = p[i].y; out3N[3 * i + 2] = p[i].z; }
+    return 0;
+}
+
+LCS_API int GBT_BatchInfo(int* counts8) {
+    if (!G.ready || !counts8) return XPBD_ERR_BAD_ARG;
+    int v[8] = {G.count, G.N, G.E, G.T, G.nEdgeColors, G.nTetColors, G.mode, G.threads};
+    std::memcpy(counts8, v, sizeof(v));
+    return 0;
+}
+
+LCS_API int GBT_BatchNodeRange(int instance, int* base, int* count) {
+    if (!G.ready || instance < 0 || instance >= G.count || !base || !count) return XPBD_ERR_BAD_ARG;
+    *base = G.nodeBase[instance]; *count = G.nodeCount[instance];
+    return 0;
+}
+
+LCS_API int GBT_BatchSetLaunch(int mode, int threads) {
+    if (!G.ready || mode < 0 || mode > 1 || (threads != 256 && threads != 512)) return XPBD_ERR_BAD_ARG;
+    G.mode = mode; G.threads = threads;
+    int perSm = threads == 512 ? 1 : 2;
+    int rc = packInstances(G.smCount * perSm);
+    if (rc) return rc;
+    dropGraph();
+    return 0;
+}
+
+// Try every launch shape for `trialSteps` frames from the current state, keep the fastest, and put
+// the state back (all shapes give bit-identical results, so the trial frames leave no trace).
+// Out: mode, threads, and the ms per frame of each candidate (3 floats).
+LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threadsOut, float* msOut3) {
+    if (!G.ready || trialSteps <= 0) return XPBD_ERR_BAD_ARG;
+    Buf<float4> savePos, savePrev, saveVel;
+    CK(savePos.alloc(G.N)); CK(savePrev.alloc(G.N)); CK(saveVel.alloc(G.N));
+    CK(cudaMemcpyAsync(savePos.p, G.pos.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
+    CK(cudaMemcpyAsync(savePrev.p, G.prev.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
+    CK(cudaMemcpyAsync(saveVel.p, G.vel.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
+    std::vector<ToolPose> keepFrom = G.toolFrom, keepTool = G.tool;
+    const int modes[3][2] = {{0, 256}, {1, 256}, {1, 512}};
+    float best = 1e30f; int bestK = 0;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a)); CK(cudaEventCreate(&b));
+    for (int k = 0; k < 3; k++) {
+        int rc = GBT_BatchSetLaunch(modes[k][0], modes[k][1]);
+        if (rc) return rc;
+        rc = stepFrames(dt, 1, nullptr, false);   // warm-up
+        if (rc) return rc;
+        CK(cudaEventRecord(a, G.stream));
+        for (int s = 0; s < trialSteps; s++) { rc = stepFrames(dt, 1, nullptr, false); if (rc) return rc; }
+        CK(cudaEventRecord(b, G.stream));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        ms /= trialSteps;
+        if (msOut3) msOut3[k] = ms;
+        if (ms < best) { best = ms; bestK = k; }
+        CK(cudaMemcpyAsync(G.pos.p, savePos.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
+        CK(cudaMemcpyAsync(G.prev.p, savePrev.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
+        CK(cudaMemcpyAsync(G.vel.p, saveVel.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
+        G.toolFrom = keepFrom; G.tool = keepTool;
+    }
+    cudaEventDestroy(a); cudaEventDestroy(b);
+    savePos.release(); savePrev.release(); saveVel.release();
+    int rc = GBT_BatchSetLaunch(modes[bestK][0], modes[bestK][1]);
+    if (rc) return rc;
+    if (modeOut) *modeOut = modes[bestK][0];
+    if (threadsOut) *threadsOut = modes[bestK][1];
+    CK(cudaStreamSynchronize(G.stream));
+    return 0;
+}
+
+LCS_API void GBT_BatchProfileEnable(int enabled) {
+    for (cudaEvent_t e : G.events) cudaEventDestroy(e);
+    G.events.clear();
+    G.profile = enabled != 0;
+}
+LCS_API int GBT_BatchProfileRead(float* msTotal) {
+    if (!msTotal || G.events.empty()) return XPBD_ERR_BAD_ARG;
+    float total = 0.f;
+    for (size_t k = 0; k + 1 < G.events.size(); k += 2) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, G.events[k], G.events[k + 1]));
+        total += t;
+    }
+    *msTotal = total;
+    return 0;
+}
+
+LCS_API void GBT_BatchShutdown() {
+    if (G.stream) cudaStreamSynchronize(G.stream);
+    releaseAll();
+}

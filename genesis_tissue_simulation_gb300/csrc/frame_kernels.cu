@@ -29,6 +29,7 @@ struct GridSync {
     unsigned extra;       // arrivals awaited beyond the grid (non-zero only in the timeout test mode)
     __device__ int rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
     __device__ int size() const { return gridDim.x * blockDim.x; }
+    __device__ bool leader() const { return blockIdx.x == 0 && threadIdx.x == 0; }
     __device__ bool sync() {
         __shared__ unsigned ok;
         __syncthreads();
@@ -57,39 +58,14 @@ struct BlockSync {
     __device__ int rank() const { return threadIdx.x; }
     __device__ int size() const { return blockDim.x; }
     __device__ bool sync() { __syncthreads(); return true; }
+    __device__ bool leader() const { return threadIdx.x == 0; }
 };
 
 // ---------------------------------------------------------------------------------------------
 // contact model 0: shaft capsule + jaw slab CCD gate, k_SolveCCDContact (xpbd_solver.cu:1049-1123)
 // ---------------------------------------------------------------------------------------------
-struct ContactFrame { f3 sa, sb, hinge, axis, normal, w; float shaftR, jawLen, halfWidth, gapHalf, alpha; };
-
-__device__ __forceinline__ f3 lerpTool(float ax, float ay, float az, float bx, float by, float bz, float t) {
-    return mk(ax, ay, az) * (1.f - t) + mk(bx, by, bz) * t;
-}
-
-// Substep pose of the instrument: linear interpolation from the previous frame's command, then the
-// jaw frame orthonormalised (xpbd_solver.cu:3467-3483, 3573-3580).
-__device__ __forceinline__ ContactFrame contactFrame(const ToolPose& a, const ToolPose& b, float t, const ContactParams& cp, float alpha) {
-    ContactFrame f;
-    f.sa = lerpTool(a.sax, a.say, a.saz, b.sax, b.say, b.saz, t);
-    f.sb = lerpTool(a.sbx, a.sby, a.sbz, b.sbx, b.sby, b.sbz, t);
-    f.hinge = lerpTool(a.hx, a.hy, a.hz, b.hx, b.hy, b.hz, t);
-    f3 ax = lerpTool(a.ax, a.ay, a.az, b.ax, b.ay, b.az, t);
-    f3 nm = lerpTool(a.nx, a.ny, a.nz, b.nx, b.ny, b.nz, t);
-    float gap = a.gap * (1.f - t) + b.gap * t;
-    f.axis = len(ax) > 1e-9f ? ax * (1.f / len(ax)) : mk(0.f, 0.f, 1.f);
-    f3 n = len(nm) > 1e-9f ? nm * (1.f / len(nm)) : mk(0.f, 1.f, 0.f);
-    n = n - f.axis * dot(n, f.axis);
-    if (len(n) < 1e-7f) n = cross(f.axis, fabsf(f.axis.x) < 0.9f ? mk(1.f, 0.f, 0.f) : mk(0.f, 1.f, 0.f));
-    f.normal = n * (1.f / len(n));
-    f.w = cross(f.axis, f.normal);
-    f.shaftR = b.shaftR; f.jawLen = b.len; f.halfWidth = b.halfWidth;
-    f.gapHalf = 0.5f * fmaxf(gap, cp.jawGapClosed);
-    f.alpha = alpha;
-    return f;
-}
-
+// The substep's instrument frame (contactFrame) lives in tissue_device.cuh: batches evaluate it on
+// the host, single meshes on the device, with the same operations.
 __device__ __forceinline__ void contactNode(const DeviceMesh& m, int c, const ContactFrame& f, const ContactParams& cp) {
     float4 P = m.pos[c];
     float wc = P.w;
@@ -277,26 +253,42 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
     // state[0]: topology revision the liveness flags were derived at (~0u: never)
     unsigned derivedAt = *(volatile unsigned*)state;
     bool havePrev = cu.havePrev != 0;
+    // Section profiler: the first thread of CTA 0 stamps the global timer when each phase ends.
+    const bool stamp = fc.phaseClock != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
+    int slot = 0;
+    auto mark = [&](int s, unsigned tag) {
+        if (stamp && slot < kPhaseRecordsPerSubstep) {
+            unsigned long long ns;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(ns));
+            fc.phaseClock[(size_t)s * kPhaseRecordsPerSubstep + slot++] = ((unsigned long long)tag << 56) | (ns & 0x00FFFFFFFFFFFFFFull);
+        }
+    };
     for (int s = 0; s < fc.substeps; s++) {
+        slot = 0;
+        mark(s, kPhaseFrameStart);
         // -- liveness refresh when the topology moved (k_TopologyStale + k_RefreshLiveness) --
         unsigned revision = cu.counters ? *(volatile unsigned*)(cu.counters) : 0u;
         bool stale = derivedAt != revision || derivedAt == ~0u;
         if (stale) {
             if (fc.fallback) {
-                for (int i = r; i < 6 * m.nNodes; i += R) m.edgeSupport[i] = 0;
+                for (int i = 6 * m.nodeBase + r; i < 6 * (m.nodeBase + m.nNodes); i += R) m.edgeSupport[i] = 0;
                 if (!sync.sync()) return;
             }
-            for (int e = r; e < m.nEdges; e += R) refreshEdge(m, e);
-            for (int b = r; b < m.nBends; b += R) m.bendLive[b] = m.bendPairs[m.bendSrc[b]].alive != 0 ? 1 : 0;
-            for (int k = r; k < m.nTets; k += R) {
-                refreshTet(m, k);
-                if (fc.fallback && (m.tetMeta[k] & 8))
-                    for (int o = 0; o < 3; o++) m.edgeSupport[m.tetOwner[3 * k + o]] = 1;
-            }
+            for (int c = 0; c < m.nEdgeColors; c++)
+                for (int e = m.edgeRange[c].x + r; e < m.edgeRange[c].y; e += R) refreshEdge(m, e);
+            for (int c = 0; c < m.nBendColors; c++)
+                for (int b = m.bendRange[c].x + r; b < m.bendRange[c].y; b += R) m.bendLive[b] = m.bendPairs[m.bendSrc[b]].alive != 0 ? 1 : 0;
+            for (int c = 0; c < m.nTetColors; c++)
+                for (int k = m.tetRange[c].x + r; k < m.tetRange[c].y; k += R) {
+                    refreshTet(m, k);
+                    if (fc.fallback && (m.tetMeta[k] & 8))
+                        for (int o = 0; o < 3; o++) m.edgeSupport[m.tetOwner[3 * k + o]] = 1;
+                }
             derivedAt = revision;
         }
+        const int nodeEnd = m.nodeBase + m.nNodes;
         // -- predict (k_predict) --
-        for (int i = r; i < m.nNodes; i += R) {
+        for (int i = m.nodeBase + r; i < nodeEnd; i += R) {
             float4 P = m.pos[i];
             if (stale) P.w = nodeInvMass(m, i);
             m.prev[i] = make_float4(P.x, P.y, P.z, 0.f);
@@ -311,31 +303,57 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
             m.pos[i] = P;
         }
         if (!sync.sync()) return;
+        mark(s, kPhasePredict);
         // -- coloured Gauss-Seidel sweeps --
+        // Tets: a thread loads the record of its first tet of colour c+1 (indices, rest data and
+        // substep-start positions, none of which the sweep writes) before the barrier that closes
+        // colour c, so only the gathers of current positions follow the barrier.  (Loading further
+        // ahead inside a colour costs more in registers, hence occupancy, than it saves; measured.)
         if (fc.doEdges)
             for (int c = 0; c < m.nEdgeColors; c++) {
-                int lo = m.edgeColorOff[c], hi = m.edgeColorOff[c + 1];
-                for (int e = lo + r; e < hi; e += R) projectEdge(m, e, fc);
+                int2 rg = m.edgeRange[c];
+                for (int e = rg.x + r; e < rg.y; e += R) applyEdge(m, loadEdge(m, e, fc), fc);
                 if (!sync.sync()) return;
+                mark(s, kPhaseEdges);
             }
         if (fc.doBend)
             for (int c = 0; c < m.nBendColors; c++) {
-                int lo = m.bendColorOff[c], hi = m.bendColorOff[c + 1];
-                for (int e = lo + r; e < hi; e += R) projectBend(m, e, fc);
+                int2 rg = m.bendRange[c];
+                for (int e = rg.x + r; e < rg.y; e += R) projectBend(m, e, fc);
                 if (!sync.sync()) return;
+                mark(s, kPhaseBends);
             }
-        if (fc.doStrain)
+        if (fc.doStrain) {
+            TetRecord next;
+            int2 first = m.nTetColors > 0 ? m.tetRange[0] : make_int2(0, 0);
+            bool hasNext = first.x + r < first.y;
+            if (hasNext) next = loadTet(m, first.x + r);
             for (int c = 0; c < m.nTetColors; c++) {
-                int lo = m.tetColorOff[c], hi = m.tetColorOff[c + 1];
-                for (int k = lo + r; k < hi; k += R) projectTet(m, k, fc);
+                int2 rg = m.tetRange[c];
+                TetRecord cur = next;
+                bool hasCur = hasNext;
+                int2 nrg = c + 1 < m.nTetColors ? m.tetRange[c + 1] : make_int2(0, 0);
+                hasNext = nrg.x + r < nrg.y;
+                if (hasNext) next = loadTet(m, nrg.x + r);
+                if (hasCur) applyTet(m, cur, fc);
+                for (int k = rg.x + r + R; k < rg.y; k += R) projectTet(m, k, fc);
                 if (!sync.sync()) return;
+                mark(s, kPhaseTets);
             }
+        }
         // -- contact, velocity --
         float t = fminf(1.f, (float)(fc.firstSubstep + s + 1) / (float)fc.numSubsteps);
         ContactFrame cf;
-        if (fc.contact) cf = contactFrame(from, to, t, cp, fc.contactAlphaH2);
-        for (int i = r; i < m.nNodes; i += R) {
-            if (fc.contact) contactNode(m, i, cf, cp);
+        if (fc.contact && !m.nodeInstance) cf = contactFrame(from, to, t, cp, fc.contactAlphaH2);
+        for (int i = m.nodeBase + r; i < nodeEnd; i += R) {
+            if (fc.contact) {
+                if (m.nodeInstance) {   // batched instances: each node meets its own instance's tool
+                    const ContactFrame& own = m.contactFrames[(size_t)(fc.firstSubstep + s) * m.nInstances + m.nodeInstance[i]];
+                    contactNode(m, i, own, cp);
+                } else {
+                    contactNode(m, i, cf, cp);
+                }
+            }
             float4 P = m.pos[i], Q = m.prev[i];
             f3 v = P.w > 0.f ? (xyz(P) - xyz(Q)) * fc.invH : mk(0.f, 0.f, 0.f);
             if (!fc.perpDamp) v = P.w > 0.f ? v * fc.velScale : mk(0.f, 0.f, 0.f);
@@ -344,8 +362,8 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         if (fc.perpDamp) {   // k_perp_damp_edges between the raw velocity write and the Rayleigh scale
             if (!sync.sync()) return;
             for (int c = 0; c < m.nEdgeColors; c++) {
-                int lo = m.edgeColorOff[c], hi = m.edgeColorOff[c + 1];
-                for (int e = lo + r; e < hi; e += R) {
+                int2 rg = m.edgeRange[c];
+                for (int e = rg.x + r; e < rg.y; e += R) {
                     if (m.edgeLive[e] == 0) continue;
                     int2 ij = m.edgeEnds[e];
                     float4 Pi = m.pos[ij.x], Pj = m.pos[ij.y];
@@ -361,23 +379,52 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 }
                 if (!sync.sync()) return;
             }
-            for (int i = r; i < m.nNodes; i += R) {
+            for (int i = m.nodeBase + r; i < nodeEnd; i += R) {
                 float4 V = m.vel[i];
                 f3 v = m.pos[i].w > 0.f ? xyz(V) * fc.velScale : mk(0.f, 0.f, 0.f);
                 m.vel[i] = make_float4(v.x, v.y, v.z, 0.f);
             }
         }
+        mark(s, kPhaseVelocity);
         // -- blade ribbon tick between substeps --
         if (fc.cut) {   // the first tick after the blade is set only takes the position snapshot
             if (havePrev) {
                 if (!sync.sync()) return;
                 for (int e = r; e < cu.nGridEdges; e += R) tickEdge(m, cu, e, true);
                 if (!sync.sync()) return;
+                mark(s, kPhaseTick);
             }
             havePrev = true;
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *(volatile unsigned*)state = derivedAt;
+    if (sync.leader()) *(volatile unsigned*)state = derivedAt;
+}
+
+// Batched instances, one CTA per instance at a time: CTA b serves the instances
+// order[ctaStart[b]] .. order[ctaStart[b+1]-1] (a longest-processing-time packing by tet count),
+// each for the whole frame with __syncthreads between colours, on that instance's own colour
+// ranges and node range of the packed table.  No grid barrier at all.
+__device__ __forceinline__ void runInstances(const DeviceMesh& m, const FrameCoeffs& fc, const ContactParams& cp, const InstanceTable& it) {
+    BlockSync b{nullptr};
+    CutParams noCut{};
+    ToolPose none{};
+    for (int j = it.ctaStart[blockIdx.x]; j < it.ctaStart[blockIdx.x + 1]; j++) {
+        const int i = it.order[j];
+        DeviceMesh v = m;
+        v.nodeBase = it.nodeBase[i];
+        v.nNodes = it.nodeCount[i];
+        v.edgeRange = it.edgeRange + (size_t)i * m.nEdgeColors;
+        v.bendRange = it.bendRange + (size_t)i * m.nBendColors;
+        v.tetRange = it.tetRange + (size_t)i * m.nTetColors;
+        runFrame(v, fc, none, none, cp, noCut, it.derived + i, b);
+        __syncthreads();
+    }
+}
+__global__ void __launch_bounds__(256) frameKernelInstances256(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it) {
+    runInstances(m, fc, cp, it);
+}
+__global__ void __launch_bounds__(512) frameKernelInstances512(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it) {
+    runInstances(m, fc, cp, it);
 }
 
 __global__ void __launch_bounds__(kFrameThreads) frameKernelGrid(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
@@ -386,10 +433,28 @@ __global__ void __launch_bounds__(kFrameThreads) frameKernelGrid(DeviceMesh m, F
     runFrame(m, fc, from, to, cp, cu, state, g);
 }
 
-__global__ void __launch_bounds__(kFrameThreads) frameKernelBlock(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
+// One CTA per mesh.  When fc.stageNodes is set the whole node state (positions and substep-start
+// positions, 32 B per node) is copied into shared memory for the frame, so every gather of every
+// colour is a shared-memory access; it is written back when the frame ends.
+__global__ void __launch_bounds__(kBlockThreads) frameKernelBlock(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                    ContactParams cp, CutParams cu, unsigned* state) {
+    extern __shared__ float4 staged[];
     BlockSync b{state + 2};
+    if (!fc.stageNodes) {
+        runFrame(m, fc, from, to, cp, cu, state, b);
+        return;
+    }
+    float4* sPos = staged;
+    float4* sPrev = staged + m.nNodes;
+    for (int i = threadIdx.x; i < m.nNodes; i += blockDim.x) { sPos[i] = m.pos[i]; sPrev[i] = m.prev[i]; }
+    __syncthreads();
+    float4* gPos = m.pos;
+    float4* gPrev = m.prev;
+    m.pos = sPos;
+    m.prev = sPrev;
     runFrame(m, fc, from, to, cp, cu, state, b);
+    __syncthreads();
+    for (int i = threadIdx.x; i < m.nNodes; i += blockDim.x) { gPos[i] = sPos[i]; gPrev[i] = sPrev[i]; }
 }
 
 // Per-tet compliance of the frame, k_ComputeTetAlpha (xpbd_solver.cu:578-587).

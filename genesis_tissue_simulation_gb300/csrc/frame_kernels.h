@@ -4,12 +4,24 @@
 
 namespace gbt {
 
-constexpr int kFrameThreads = 256;     // threads per CTA of both frame kernels
+constexpr int kFrameThreads = 256;     // threads per CTA of the whole-GPU frame kernel
+constexpr int kBlockThreads = 512;     // threads of the one-CTA frame kernel
 
 __global__ void frameKernelGrid(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to, ContactParams cp, CutParams cu,
                                 unsigned* state);
 __global__ void frameKernelBlock(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to, ContactParams cp, CutParams cu,
                                  unsigned* state);
+// Per-instance view of a packed batch: node range and colour ranges of every instance, and the
+// work list of each CTA of frameKernelInstances.
+struct InstanceTable {
+    const int* nodeBase; const int* nodeCount;
+    const int2* edgeRange; const int2* bendRange; const int2* tetRange;   // [instances x colours]
+    const int* order; const int* ctaStart;                                 // CTA b: order[ctaStart[b] .. ctaStart[b+1])
+    unsigned* derived;                                                     // per instance: revision its liveness was derived at
+};
+__global__ void frameKernelInstances256(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it);
+__global__ void frameKernelInstances512(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it);
+
 __global__ void tetAlphaKernel(int n, float invH2, const float2* stiff, float2* alpha);
 __global__ void gravityKernel(int n, float gx, float gy, float gz, float4* ext);
 

@@ -12,9 +12,12 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <cstdio>
+#include <string>
 #include <vector>
 
 #include "frame_kernels.h"
+#include "mesh_build.h"
 #include "../../include/gbtissue.h"
 
 using namespace gbt;
@@ -82,8 +85,12 @@ struct Session {
     // launch choice and profiling
     int launchMode = 0;                     // 0 automatic, 1 whole-GPU grid, 2 single CTA
     int clockKHz = 2000000;                 // SM clock, for the barrier spin budget
+    int maxStageBytes = 0;                  // shared memory one CTA may stage the node state in
     int syncTestExtra = 0; float syncBudgetSeconds = 2.f;
     bool profile = false; std::vector<cudaEvent_t> events; int profiledSteps = 0;
+    // section profiler (xpbd_profile_sections, xpbd_solver.cu:30-60): device time per phase kind
+    bool sections = false; DBuf<unsigned long long> phaseClock; std::vector<unsigned long long> phaseHost;
+    double sectionMs[8] = {}; long long sectionCount[8] = {};
 };
 Session S;
 
@@ -118,6 +125,10 @@ int ensureStream() {
     CK(cudaMallocHost(&S.hostState, 8 * sizeof(unsigned)));
     int perSm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, frameKernelGrid, kFrameThreads, 0));
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, S.device));
+    S.maxStageBytes = optin;
+    CK(cudaFuncSetAttribute((const void*)frameKernelBlock, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     int khz = 0;
     if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, S.device) == cudaSuccess && khz > 0) S.clockKHz = khz;
     S.gridBlocks = std::max(1, perSm) * S.smCount;
@@ -131,115 +142,11 @@ int directedSlot(int a, int b) {
     return 6 * a + 2 * axis + (d > 0 ? 1 : 0);
 }
 
-// Greedy colouring: each element takes the lowest of 64 colours none of its nodes carries yet
-// (xpbd_solver.cu:1213-1230 edges, 1340-1352 bends, 1738-1751 tets).  Returns the colour count or
-// XPBD_ERR_COLOR_OVERFLOW.
-int colourGreedy(int count, int arity, const int* nodesOf, int nodeCount, std::vector<int>& colourOf) {
-    std::vector<uint64_t> taken(nodeCount, 0);
-    colourOf.resize(count);
-    int colours = 0;
-    for (int e = 0; e < count; e++) {
-        const int* nd = nodesOf + (size_t)arity * e;
-        uint64_t busy = 0;
-        for (int k = 0; k < arity; k++) busy |= taken[nd[k]];
-        if (busy == ~0ull) return XPBD_ERR_COLOR_OVERFLOW;
-        int c = __builtin_ctzll(~busy);
-        colourOf[e] = c;
-        for (int k = 0; k < arity; k++) taken[nd[k]] |= 1ull << c;
-        colours = std::max(colours, c + 1);
-    }
-    return colours;
-}
-// Colour-major order: offsets[c] .. offsets[c+1] hold colour c, members in element order.
-void colourOrder(const std::vector<int>& colourOf, int colours, std::vector<int>& offsets, std::vector<int>& order) {
-    offsets.assign(colours + 1, 0);
-    for (int c : colourOf) offsets[c + 1]++;
-    for (int c = 0; c < colours; c++) offsets[c + 1] += offsets[c];
-    std::vector<int> fill(offsets.begin(), offsets.end() - 1);
-    order.resize(colourOf.size());
-    for (size_t e = 0; e < colourOf.size(); e++) order[fill[colourOf[e]]++] = (int)e;
-}
-
-bool invert3(const double a[3][3], double o[3][3], double* detOut) {
-    double c00 = a[1][1] * a[2][2] - a[1][2] * a[2][1], c01 = a[1][0] * a[2][2] - a[1][2] * a[2][0], c02 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
-    double det = a[0][0] * c00 - a[0][1] * c01 + a[0][2] * c02;
-    if (detOut) *detOut = det;
-    if (std::fabs(det) < 1e-20) return false;
-    double r = 1.0 / det;
-    o[0][0] = c00 * r; o[0][1] = -(a[0][1] * a[2][2] - a[0][2] * a[2][1]) * r; o[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) * r;
-    o[1][0] = -c01 * r; o[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) * r; o[1][2] = -(a[0][0] * a[1][2] - a[0][2] * a[1][0]) * r;
-    o[2][0] = c02 * r; o[2][1] = -(a[0][0] * a[2][1] - a[0][1] * a[2][0]) * r; o[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) * r;
-    return true;
-}
-
-// Kuhn split of a cell along the diagonal from local corner 0 to 7; corner bit a = +axis a.
-const int kKuhn[6][4] = {{0, 1, 3, 7}, {0, 3, 2, 7}, {0, 2, 6, 7}, {0, 6, 4, 7}, {0, 4, 5, 7}, {0, 5, 1, 7}};
-
-// Tet mesh of every cell whose 8 corners are active (xpbd_build_tets, xpbd_solver.cu:1600-1848).
-int buildTets(const int* activeFlags, std::vector<int>& ids, std::vector<int>& owner, std::vector<int>& kind, std::vector<float2>& stiff) {
-    const float* P = S.hostRest.data();
-    double spacing[3] = {((double)P[3 * nodeIndex(S.dx, 0, 0)] - (double)P[0]) / S.dx,
-                         ((double)P[3 * nodeIndex(0, S.dy, 0) + 1] - (double)P[1]) / S.dy,
-                         ((double)P[3 * nodeIndex(0, 0, S.dz) + 2] - (double)P[2]) / S.dz};
-    double typeInv[6][3][3], typeVol[6];
-    for (int t = 0; t < 6; t++) {
-        double Dm[3][3];
-        for (int k = 1; k < 4; k++)
-            for (int a = 0; a < 3; a++) Dm[a][k - 1] = ((kKuhn[t][k] >> a) & 1) * spacing[a];
-        double det;
-        if (!invert3(Dm, typeInv[t], &det)) return XPBD_ERR_IRREGULAR_REST;
-        typeVol[t] = std::fabs(det) / 6.0;
-        for (int a = 0; a < 3; a++)
-            for (int b = 0; b < 3; b++) S.typeB[t][3 * a + b] = (float)typeInv[t][a][b];
-    }
-    float mu = 1.f, kappa = 1.f;
-    if (S.youngE > 0.f && S.poisson > -1.f && S.poisson < 0.5f) {
-        mu = S.youngE / (2.f * (1.f + S.poisson));
-        kappa = S.youngE / (3.f * (1.f - 2.f * S.poisson));
-    }
-    if (!(mu > 0.f)) mu = 1.f;
-    if (!(kappa > 0.f)) kappa = 1.f;
-    for (int z = 0; z < S.dz; z++)
-        for (int y = 0; y < S.dy; y++)
-            for (int x = 0; x < S.dx; x++) {
-                int corner[8];
-                bool full = true;
-                for (int l = 0; l < 8; l++) {
-                    corner[l] = nodeIndex(x + (l & 1), y + ((l >> 1) & 1), z + ((l >> 2) & 1));
-                    full = full && activeFlags[corner[l]] != 0;
-                }
-                if (!full) continue;
-                for (int t = 0; t < 6; t++) {
-                    const int* q = kKuhn[t];
-                    double Dm[3][3], inv[3][3], det;
-                    for (int c = 0; c < 3; c++)
-                        for (int a = 0; a < 3; a++) Dm[a][c] = (double)P[3 * corner[q[c + 1]] + a] - (double)P[3 * corner[q[0]] + a];
-                    if (!invert3(Dm, inv, &det)) continue;
-                    if (std::fabs(det) / 6.0 < 1e-12) continue;
-                    double scale = 0, dev = 0;
-                    for (int a = 0; a < 3; a++)
-                        for (int b = 0; b < 3; b++) {
-                            scale = std::max(scale, std::fabs(typeInv[t][a][b]));
-                            dev = std::max(dev, std::fabs(inv[a][b] - typeInv[t][a][b]));
-                        }
-                    if (dev > 1e-4 * scale) return XPBD_ERR_IRREGULAR_REST;
-                    // the three tet edges along lattice axes, owned by their lower node's +axis slot
-                    int found = 0;
-                    for (int a = 0; a < 4 && found < 3; a++)
-                        for (int b = a + 1; b < 4 && found < 3; b++) {
-                            int diff = q[a] ^ q[b];
-                            if (diff != 1 && diff != 2 && diff != 4) continue;
-                            int axis = diff == 1 ? 0 : (diff == 2 ? 1 : 2);
-                            int low = ((q[a] >> axis) & 1) ? q[b] : q[a];
-                            owner.push_back(6 * corner[low] + 2 * axis + 1);
-                            found++;
-                        }
-                    for (int k = 0; k < 4; k++) ids.push_back(corner[q[k]]);
-                    kind.push_back(t);
-                    stiff.push_back(make_float2(mu * (float)typeVol[t], kappa * (float)typeVol[t]));
-                }
-            }
-    return 0;
+// Colour offsets [c0, c1, ..., cn] as the (begin, end) pair of every colour, the kernels' range form.
+std::vector<int> colourRanges(const std::vector<int>& offsets) {
+    std::vector<int> out;
+    for (size_t c = 0; c + 1 < offsets.size(); c++) { out.push_back(offsets[c]); out.push_back(offsets[c + 1]); }
+    return out;
 }
 
 int uploadFrameState() {
@@ -250,15 +157,15 @@ int uploadFrameState() {
 
 DeviceMesh deviceMesh() {
     DeviceMesh m{};
-    m.nNodes = S.N; m.dx = S.dx; m.dy = S.dy; m.dz = S.dz;
+    m.nNodes = S.N; m.nodeBase = 0; m.dx = S.dx; m.dy = S.dy; m.dz = S.dz;
     m.pos = S.pos.p; m.prev = S.prev.p; m.vel = S.vel.p; m.ext = S.ext.p;
     m.pinned = S.pinned.p; m.active = S.active.p; m.nbr = S.nbr.p;
-    m.nEdges = S.E; m.nEdgeColors = (int)S.edgeColorOff.size() - 1; m.edgeColorOff = S.edgeColorOffD.p;
+    m.nEdgeColors = (int)S.edgeColorOff.size() - 1; m.edgeRange = (const int2*)S.edgeColorOffD.p;
     m.edgeEnds = S.edgeEnds.p; m.edgeRest = S.edgeRest.p; m.edgeOwner = S.edgeOwner.p; m.edgeLive = S.edgeLive.p;
-    m.nBends = S.B; m.nBendColors = (int)S.bendColorOff.size() - 1; m.bendColorOff = S.bendColorOffD.p;
+    m.nBendColors = (int)S.bendColorOff.size() - 1; m.bendRange = (const int2*)S.bendColorOffD.p;
     m.bendIJK = S.bendIJK.p; m.bendSrc = S.bendSrc.p; m.bendLive = S.bendLive.p; m.bendPairs = S.bendPairs.p;
     m.nBendPairs = (int)S.bendPairs.n;
-    m.nTets = S.T; m.nTetColors = (int)S.tetColorOff.size() - 1; m.tetColorOff = S.tetColorOffD.p;
+    m.nTetColors = (int)S.tetColorOff.size() - 1; m.tetRange = (const int2*)S.tetColorOffD.p;
     m.tetIds = S.tetIds.p; m.tetMeta = S.tetMeta.p; m.tetOwner = S.tetOwner.p; m.tetAlpha = S.tetAlpha.p; m.tetStiff = S.tetStiff.p;
     m.edgeSupport = S.edgeSupport.p;
     std::memcpy(m.typeB, S.typeB, sizeof(S.typeB));
@@ -281,9 +188,13 @@ int launchFrame(const FrameCoeffs& fc) {
     CutParams cu = cutParams();
     unsigned* state = S.state.p;
     CK(cudaMemsetAsync(state + 1, 0, 2 * sizeof(unsigned), S.stream));
-    bool single = S.launchMode == 2 || (S.launchMode == 0 && S.T < 65536 && S.N < 32768);
+    size_t stageBytes = (size_t)S.N * 2 * sizeof(float4);
+    bool stage = stageBytes <= (size_t)S.maxStageBytes;
+    bool single = S.launchMode == 2 || (S.launchMode == 0 && stage);
     if (single) {
-        frameKernelBlock<<<1, kFrameThreads, 0, S.stream>>>(m, fc, S.toolFrom, S.tool, S.cp, cu, state);
+        FrameCoeffs f = fc;
+        f.stageNodes = stage ? 1 : 0;
+        frameKernelBlock<<<1, kBlockThreads, stage ? stageBytes : 0, S.stream>>>(m, f, S.toolFrom, S.tool, S.cp, cu, state);
         CK(cudaGetLastError());
     } else {
         ToolPose from = S.toolFrom, to = S.tool;
@@ -344,110 +255,44 @@ LCS_API int LCS_InitPhysics(const PhysicsInitDesc* desc, const float* mass, cons
     S.omega = 1.f; S.damping = 0.f; S.ks = desc->ks; S.kb = desc->kb; S.alpha = desc->alpha; S.betaS = desc->cs; S.betaB = desc->cb;
     S.youngE = desc->youngE; S.poisson = desc->poisson; S.strainDamping = desc->strainDamping;
 
-    // lattice edges, each from its lower node's positive slot (xpbd_bind, xpbd_solver.cu:1445-1463)
-    std::vector<int> ends, owner;
-    std::vector<float> restLen;
-    for (int p = 0; p < cc; p++)
-        for (int a = 0; a < 3; a++) {
-            int slot = 6 * p + 2 * a + 1, n = nbrIdx[slot];
-            if (n < 0) continue;
-            if (n >= cc) return XPBD_ERR_BAD_ARG;
-            const float* r = restNbr + 3 * (size_t)slot;
-            ends.push_back(p); ends.push_back(n); owner.push_back(slot);
-            restLen.push_back(sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]));
-        }
-    const int E = (int)owner.size();
-    std::vector<int> colourOf, order;
-    int edgeColours = colourGreedy(E, 2, ends.data(), cc, colourOf);
-    if (edgeColours < 0) return edgeColours;
-    colourOrder(colourOf, edgeColours, S.edgeColorOff, order);
-    std::vector<int2> eEnds(E); std::vector<float> eRest(E); std::vector<int> eOwner(E);
-    for (int k = 0; k < E; k++) {
-        int e = order[k];
-        eEnds[k] = make_int2(ends[2 * e], ends[2 * e + 1]); eRest[k] = restLen[e]; eOwner[k] = owner[e];
-    }
-    S.edgeOwnerColor = eOwner;
-    // bend elements alive at bind time, coloured over their three nodes (xpbd_solver.cu:1465-1479)
-    const BendRecord* bp = (const BendRecord*)bendPairs;
-    std::vector<int> bNodes, bSrc; std::vector<float> bTheta;
-    for (int b = 0; b < bpc; b++) {
-        if (bp[b].alive == 0) continue;
-        if (bp[b].i < 0 || bp[b].i >= cc || bp[b].j < 0 || bp[b].j >= cc || bp[b].k < 0 || bp[b].k >= cc) return XPBD_ERR_BAD_ARG;
-        bNodes.push_back(bp[b].i); bNodes.push_back(bp[b].j); bNodes.push_back(bp[b].k);
-        bTheta.push_back(bp[b].theta0); bSrc.push_back(b);
-    }
-    const int B = (int)bSrc.size();
-    int bendColours = colourGreedy(B, 3, bNodes.data(), cc, colourOf);
-    if (bendColours < 0) return bendColours;
-    colourOrder(colourOf, bendColours, S.bendColorOff, order);
-    std::vector<int4> bIJK(B); std::vector<int> bSrcOrd(B);
-    for (int k = 0; k < B; k++) {
-        int e = order[k];
-        float th = bTheta[e];
-        int thBits; std::memcpy(&thBits, &th, 4);
-        bIJK[k] = make_int4(bNodes[3 * e], bNodes[3 * e + 1], bNodes[3 * e + 2], thBits);
-        bSrcOrd[k] = bSrc[e];
-    }
-    // tets
-    std::vector<int> tIds, tOwner, tKind; std::vector<float2> tStiff;
-    int rc = buildTets(active, tIds, tOwner, tKind, tStiff);
+    MeshInput in{S.dx, S.dy, S.dz, S.hostRest.data(), mass, pinned, active, extForce, nbrIdx, restNbr, bendPairs, bpc,
+                 S.youngE, S.poisson};
+    HostMesh hm;
+    int rc = buildHostMesh(in, hm);
     if (rc) return rc;
-    const int T = (int)tKind.size();
-    if (T % 6) return XPBD_ERR_IRREGULAR_REST;
-    int tetColours = colourGreedy(T, 4, tIds.data(), cc, colourOf);
-    if (tetColours < 0) return tetColours;
-    colourOrder(colourOf, tetColours, S.tetColorOff, order);
-    // storage index: Kuhn type major, cell order minor (xpbd_solver.cu:1757-1780)
-    std::vector<int> place(T), perType(7, 0);
-    for (int e = 0; e < T; e++) perType[tKind[e] + 1]++;
-    for (int k = 0; k < 6; k++) perType[k + 1] += perType[k];
-    for (int e = 0; e < T; e++) place[e] = perType[tKind[e]]++;
-    S.tetIdsStorage.assign((size_t)4 * T, 0); S.tetStiffStorage.assign(T, make_float2(0, 0)); S.tetColorOrder.assign(T, 0);
-    std::vector<int4> cIds(T); std::vector<int> cMeta(T), cOwner((size_t)3 * T); std::vector<float2> cStiff(T);
-    for (int e = 0; e < T; e++) {
-        for (int k = 0; k < 4; k++) S.tetIdsStorage[4 * place[e] + k] = tIds[4 * e + k];
-        S.tetStiffStorage[place[e]] = tStiff[e];
-    }
-    for (int k = 0; k < T; k++) {
-        int e = order[k];
-        S.tetColorOrder[k] = place[e];
-        cIds[k] = make_int4(tIds[4 * e], tIds[4 * e + 1], tIds[4 * e + 2], tIds[4 * e + 3]);
-        cMeta[k] = tKind[e] | 8;
-        for (int o = 0; o < 3; o++) cOwner[3 * k + o] = tOwner[3 * e + o];
-        cStiff[k] = tStiff[e];
-    }
+    const int E = hm.E, B = hm.B, T = hm.T;
+    S.edgeColorOff = hm.edgeColorOff; S.bendColorOff = hm.bendColorOff; S.tetColorOff = hm.tetColorOff;
+    S.edgeOwnerColor = hm.edgeOwner; S.tetColorOrder = hm.tetColorOrder;
+    S.tetIdsStorage = hm.tetIdsStorage; S.tetStiffStorage = hm.tetStiffStorage;
+    std::memcpy(S.typeB, hm.typeB, sizeof(S.typeB));
     S.E = E; S.B = B; S.T = T;
-
-    // node state: pos.w = inverse mass, ext.w = mass
-    std::vector<float4> ext4(cc), zero4(cc, make_float4(0, 0, 0, 0)), pos4(cc);
-    for (int i = 0; i < cc; i++) {
-        ext4[i] = make_float4(extForce[3 * i], extForce[3 * i + 1], extForce[3 * i + 2], mass[i]);
-        float w = (pinned[i] != 0 || active[i] == 0) ? 0.f : 1.f / mass[i];
-        pos4[i] = make_float4(S.hostRest[3 * i], S.hostRest[3 * i + 1], S.hostRest[3 * i + 2], w);
-    }
-    CK(S.pos.upload(pos4.data(), cc, S.stream));
-    CK(S.prev.upload(pos4.data(), cc, S.stream));
+    const BendRecord* bp = (const BendRecord*)bendPairs;
+    std::vector<float4> zero4(cc, make_float4(0, 0, 0, 0));
+    CK(S.pos.upload(hm.pos.data(), cc, S.stream));
+    CK(S.prev.upload(hm.pos.data(), cc, S.stream));
     CK(S.vel.upload(zero4.data(), cc, S.stream));
-    CK(S.ext.upload(ext4.data(), cc, S.stream));
+    CK(S.ext.upload(hm.ext.data(), cc, S.stream));
     CK(S.pinned.upload(pinned, cc, S.stream));
     CK(S.active.upload(active, cc, S.stream));
     CK(S.nbr.upload(nbrIdx, (size_t)6 * cc, S.stream));
-    CK(S.edgeColorOffD.upload(S.edgeColorOff.data(), S.edgeColorOff.size(), S.stream));
-    CK(S.edgeEnds.upload(eEnds.data(), E, S.stream));
-    CK(S.edgeRest.upload(eRest.data(), E, S.stream));
-    CK(S.edgeOwner.upload(eOwner.data(), E, S.stream));
+    std::vector<int> edgeRanges = colourRanges(S.edgeColorOff), bendRanges = colourRanges(S.bendColorOff),
+                     tetRanges = colourRanges(S.tetColorOff);
+    CK(S.edgeColorOffD.upload(edgeRanges.data(), edgeRanges.size(), S.stream));
+    CK(S.edgeEnds.upload(hm.edgeEnds.data(), E, S.stream));
+    CK(S.edgeRest.upload(hm.edgeRest.data(), E, S.stream));
+    CK(S.edgeOwner.upload(hm.edgeOwner.data(), E, S.stream));
     std::vector<int> ones(std::max(std::max(E, B), 1), 1);
     CK(S.edgeLive.upload(ones.data(), E, S.stream));
-    CK(S.bendColorOffD.upload(S.bendColorOff.data(), S.bendColorOff.size(), S.stream));
-    CK(S.bendIJK.upload(bIJK.data(), B, S.stream));
-    CK(S.bendSrc.upload(bSrcOrd.data(), B, S.stream));
+    CK(S.bendColorOffD.upload(bendRanges.data(), bendRanges.size(), S.stream));
+    CK(S.bendIJK.upload(hm.bendIJK.data(), B, S.stream));
+    CK(S.bendSrc.upload(hm.bendSrc.data(), B, S.stream));
     CK(S.bendLive.upload(ones.data(), B, S.stream));
     CK(S.bendPairs.upload(bp, bpc, S.stream));
-    CK(S.tetColorOffD.upload(S.tetColorOff.data(), S.tetColorOff.size(), S.stream));
-    CK(S.tetIds.upload(cIds.data(), T, S.stream));
-    CK(S.tetMeta.upload(cMeta.data(), T, S.stream));
-    CK(S.tetOwner.upload(cOwner.data(), (size_t)3 * T, S.stream));
-    CK(S.tetStiff.upload(cStiff.data(), T, S.stream));
+    CK(S.tetColorOffD.upload(tetRanges.data(), tetRanges.size(), S.stream));
+    CK(S.tetIds.upload(hm.tetIds.data(), T, S.stream));
+    CK(S.tetMeta.upload(hm.tetMeta.data(), T, S.stream));
+    CK(S.tetOwner.upload(hm.tetOwner.data(), (size_t)3 * T, S.stream));
+    CK(S.tetStiff.upload(hm.tetStiff.data(), T, S.stream));
     CK(S.tetAlpha.alloc(T));
     std::vector<int> zeros((size_t)6 * cc, 0);
     CK(S.edgeSupport.upload(zeros.data(), (size_t)6 * cc, S.stream));
@@ -646,11 +491,36 @@ LCS_API int LCS_Step(float dt) {
         CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
         CK(cudaEventRecord(e0, S.stream));
     }
+    size_t records = (size_t)N * kPhaseRecordsPerSubstep;
+    if (S.sections) {
+        if (S.phaseClock.n < records) CK(S.phaseClock.alloc(records));
+        CK(cudaMemsetAsync(S.phaseClock.p, 0, records * sizeof(unsigned long long), S.stream));
+        fc.phaseClock = S.phaseClock.p;
+    }
     int rc = launchFrame(fc);
     if (rc) return rc;
     if (S.profile) { CK(cudaEventRecord(e1, S.stream)); S.events.push_back(e0); S.events.push_back(e1); }
     CK(cudaMemcpyAsync(S.hostState, S.state.p, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    if (S.sections) {
+        S.phaseHost.resize(records);
+        CK(cudaMemcpyAsync(S.phaseHost.data(), S.phaseClock.p, records * sizeof(unsigned long long), cudaMemcpyDeviceToHost, S.stream));
+    }
     CK(cudaStreamSynchronize(S.stream));
+    if (S.sections) {   // each record's time since the previous record belongs to the phase it closes
+        const unsigned long long mask = 0x00FFFFFFFFFFFFFFull;
+        unsigned long long last = 0;
+        for (size_t i = 0; i < records; i++) {
+            unsigned long long r = S.phaseHost[i];
+            if (r == 0) continue;
+            unsigned tag = (unsigned)(r >> 56);
+            unsigned long long ns = r & mask;
+            if (last != 0 && tag != kPhaseFrameStart && tag < 8) {
+                S.sectionMs[tag] += (double)(ns - last) * 1e-6;
+                S.sectionCount[tag]++;
+            }
+            last = ns;
+        }
+    }
     if (fc.cut) S.havePrev = true;
     if (S.toolArmed) S.toolFrom = S.tool;
     if (S.hostState[2] != 0u) return LCS_ERR_DEVICE_TIMEOUT;
@@ -737,6 +607,28 @@ LCS_API int LCS_ProfileRead(int steps, float* ms) {
     ms[0] = total; ms[1] = 0.f; ms[2] = 0.f;
     return 0;
 }
+// Section timing (xpbd_profile_sections / _read, xpbd_solver.cu:30-60): while enabled, the first
+// CTA stamps the GPU's global timer at the end of every phase of every substep, and the host adds
+// each interval to its phase kind.  Read returns "name=ms count=n" lines, or the capacity needed.
+LCS_API void LCS_ProfileSections(int enabled) {
+    S.sections = enabled != 0;
+    for (int k = 0; k < 8; k++) { S.sectionMs[k] = 0.0; S.sectionCount[k] = 0; }
+}
+LCS_API int LCS_ProfileSectionsRead(char* text, int capacity) {
+    static const char* names[8] = {"frame start", "liveness and predict", "edge colours", "bend colours", "tet colours",
+                                   "contact and velocity", "ribbon tick", ""};
+    std::string out;
+    for (int k = 1; k < 7; k++) {
+        if (!S.sectionCount[k]) continue;
+        char line[160];
+        snprintf(line, sizeof line, "%s=%.4f count=%lld\n", names[k], S.sectionMs[k], S.sectionCount[k]);
+        out += line;
+    }
+    if (!text || capacity <= (int)out.size()) return (int)out.size() + 1;
+    std::memcpy(text, out.c_str(), out.size() + 1);
+    return 0;
+}
+
 LCS_API int LCS_SetLaunchMode(int mode) {
     if (mode < 0 || mode > 2) return XPBD_ERR_BAD_ARG;
     S.launchMode = mode;

@@ -21,6 +21,7 @@ reference's numpy promotion rules exactly (they are pinned by golden hashes in `
 """
 from __future__ import annotations
 
+import functools
 from dataclasses import dataclass
 
 import numpy as np
@@ -98,6 +99,12 @@ coordinates = lattice_coordinates
 
 
 def connectivity_table():
+    """Component labels of the 8 voxel corners for each of the 2^12 edge-cut masks (a fresh copy)."""
+    return _connectivity_table().copy()
+
+
+@functools.lru_cache(maxsize=1)
+def _connectivity_table():
     """Component labels of the 8 voxel corners for each of the 2^12 edge-cut masks (grid.py:69-82).
 
     Row ``m`` holds ``(count, label_0 .. label_7)``: bit ``b`` of ``m`` set means voxel edge ``b``

@@ -82,6 +82,8 @@ LCS_API int LCS_GetCutDebug(unsigned* out18, float* alphaOut);      /* slots 15 
 /* ---- profiling and shutdown (plugin_api.cpp:21-22, 236-242) ------------------------------------ */
 LCS_API void LCS_ProfileEnable(int enabled);
 LCS_API int LCS_ProfileRead(int steps, float* ms3);                  /* ms3[0] = device ms of the first `steps` frames */
+LCS_API void LCS_ProfileSections(int enabled);                       /* plugin_api.cpp:25 */
+LCS_API int LCS_ProfileSectionsRead(char* text, int capacity);       /* plugin_api.cpp:26: "name=ms count=n" lines */
 LCS_API void LCS_Shutdown(void);
 
 /* ---- module diagnostics without an LCS_ export in the reference -------------------------------- */
@@ -106,6 +108,35 @@ LCS_API int LCS_SetLaunchMode(int mode);         /* 0 automatic, 1 whole-GPU coo
  * never come and gives up after `budgetSeconds` (normal budget 2 s); LCS_Step then returns -4002 and
  * the context stays usable.  (0, 2.0) restores normal operation. */
 LCS_API int LCS_SetBarrierTest(int extraArrivals, float budgetSeconds);
+
+/* ---- batched instances (no counterpart in the reference, which has one session per process) ----
+ * Many independent tissue meshes, each with the topology its own plain session would build, are
+ * packed into one table and advanced together, one persistent launch per frame.  Instance inputs are
+ * the LCS_InitPhysics arrays of one lattice; tetMuV/tetKappaV (storage order, may be null) replace the
+ * (E, nu) bake like LCS_SetTetStiffness.  Instruments: contact model 0 capsules, one XpbdToolState
+ * (92 B) per instance per frame.  Every instance shares the lattice spacing and parameters below. */
+typedef struct { int dimsX, dimsY, dimsZ; const float* cornerPos; const float* mass; const int* pinned; const int* active;
+                 const int* nbrIdx; const float* restNbr; const void* bendPairs; int bendPairCount;
+                 const float* tetMuV; const float* tetKappaV; float stiffnessScale; } GbtInstanceDesc;
+/* stiffnessScale > 0 multiplies both per-tet stiffnesses (after any override), in FP32: an instance of
+ * Young's modulus E' is stiffnessScale = E'/E of the bake. */
+typedef struct { int substeps; float ks, cs, kb, cb, alpha, youngE, poisson, strainDamping; } GbtBatchParams;
+LCS_API int GBT_BatchInit(int count, const GbtInstanceDesc* instances, const GbtBatchParams* params);
+LCS_API int GBT_BatchSetGravity(float gx, float gy, float gz);
+LCS_API void GBT_BatchSetGraspParams(const GraspParamsAbi* params);
+LCS_API int GBT_BatchSetTools(const void* xpbdToolStates);            /* count x 92 B: the next frame's instruments */
+LCS_API int GBT_BatchStep(float dt);                                   /* one frame of every instance */
+/* `steps` frames; tools = [steps][count] XpbdToolState or null; useGraph: replay the launches from a
+ * CUDA graph captured on first use (recaptured when steps, launch shape or dt change). */
+LCS_API int GBT_BatchStepMany(float dt, int steps, const void* tools, int useGraph);
+LCS_API int GBT_BatchGetPositions(float* out3N);                      /* all nodes, instance after instance */
+LCS_API int GBT_BatchNodeRange(int instance, int* base, int* count);
+LCS_API int GBT_BatchInfo(int* counts8);                               /* instances, nodes, edges, tets, edge colours, tet colours, mode, threads */
+LCS_API int GBT_BatchSetLaunch(int mode, int threads);                 /* 0 lockstep grid | 1 one CTA per instance; 256 | 512 */
+LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threadsOut, float* msPerFrame3);
+LCS_API void GBT_BatchProfileEnable(int enabled);
+LCS_API int GBT_BatchProfileRead(float* msTotal);                      /* device ms of the profiled step calls */
+LCS_API void GBT_BatchShutdown(void);
 
 /* LCS_StepNoAlloc has no counterpart in the reference.  It advances the session by one frame
  * exactly as LCS_Step does, for hosts that cannot let a plugin allocate GPU memory while they run

@@ -1043,6 +1043,12 @@ API int LCS_GetCutDebug(unsigned* out18, float* alpha) {
     return 0;
 }
 API void LCS_ProfileEnable(int enabled) { S.profile = enabled != 0; S.stepMs.clear(); }
+API void LCS_ProfileSections(int enabled) { (void)enabled; }
+API int LCS_ProfileSectionsRead(char* text, int capacity) {   // the oracle times whole steps only
+    if (!text || capacity < 1) return 1;
+    text[0] = 0;
+    return 0;
+}
 API int LCS_ProfileRead(int steps, float* ms) {
     if (!ms || steps <= 0 || (int)S.stepMs.size() < steps) return -1;
     double total = 0;
