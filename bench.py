@@ -165,6 +165,98 @@ def cpu_baseline_sample(workload_name, budget_s=15.0, max_steps=40):
             "sample": f"steps 2..{n + 1} of {w.name} (one warm-up step), CPU restatement FP32, OpenMP {threads} threads, {elapsed:.1f} s"}
 
 
+def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6):
+    """Batched uneven instances: 256 grids with dims U{8..32} x U{4..16}(up) x U{8..32} cells from one
+    seed, per-instance log-uniform compliance and capsule path, 10 substeps per frame.
+
+    Device rate: CUDA events around each graph-replayed frame launch (autotuned launch shape).  The
+    packed state (~0.5 GB of node and element tables) exceeds L2, so no flush is added.  End to end:
+    the public batch call with the frame's capsule poses from host memory and every instance's node
+    positions copied back to host memory.  Plain rate: the single-instance LCS path stepping a
+    sample of the same instances, one session each, device time per frame from its own events.
+    """
+    import ctypes
+
+    import torch
+
+    from genesis_tissue_simulation_gb300 import batch as BT
+    from genesis_tissue_simulation_gb300 import workloads as W
+    from genesis_tissue_simulation_gb300.native_backend import GraspParams, PlainTissue
+
+    w = BT.make_c4(steps=warmup + 2 * frames + 1)
+    grasp = dict(W.DEFAULT_GRASP, ccd_velocity=0.0)
+    scale = w.stiffness_scale()
+    count = len(w.grids)
+    n_active = int(sum(int((g.active != 0).sum()) for g in w.grids))
+    with BT.TissueBatch(w.grids, dt=1 / 60, substeps=w.substeps, ks=1e6, stiffness_scale=scale,
+                        grasp_params=GraspParams(**grasp), dll_path=lib) as b:
+        info = b.info()
+        b.set_gravity(0.0, -981.0, 0.0)
+        b.set_capsules(w.capsules_at(0))
+        tune = b.autotune(trial_steps=2)
+        for k in range(warmup):
+            b.step_many([w.capsules_at(k + 1)], use_graph=True)
+        torch.cuda.synchronize()
+        b.profile(1)
+        for k in range(warmup, warmup + frames):
+            b.step_many([w.capsules_at(k + 1)], use_graph=True)
+        torch.cuda.synchronize()
+        device_s = b.profile_read() / 1e3
+        b.profile(0)
+        e0 = time.perf_counter()
+        for k in range(warmup + frames, warmup + 2 * frames):
+            b.step_many([w.capsules_at(k + 1)], use_graph=True)
+            positions = b.positions()
+        e2e_s = time.perf_counter() - e0
+        assert np.isfinite(positions).all(), "non-finite batched state"
+
+    # plain path on a size-spread sample of the same instances
+    order = np.argsort([g.positions.shape[0] for g in w.grids])
+    picks = order[np.linspace(0, count - 1, plain_sample).round().astype(int)]
+    plain_ms = []
+    for i in picks:
+        g = w.grids[i]
+        s = PlainTissue(g, dt=1 / 60, substeps=w.substeps, ks=1e6, grasp_params=GraspParams(**grasp), dll_path=lib)
+        try:
+            mu, kappa = s.tet_stiffness()
+            s.set_tet_stiffness(mu * scale[i], kappa * scale[i])
+            s.set_gravity(0.0, -981.0, 0.0)
+            s.set_capsule(w.capsule_paths[i][0])
+            for k in range(2):
+                s.set_capsule(w.capsule_paths[i][k + 1])
+                s.step()
+            s.functions["LCS_ProfileEnable"](1)
+            for k in range(2, 2 + plain_frames):
+                s.set_capsule(w.capsule_paths[i][k + 1])
+                s.step()
+            ms = np.zeros(3, dtype=np.float32)
+            s.check("LCS_ProfileRead", plain_frames, ms.ctypes.data_as(ctypes.c_void_p))
+            plain_ms.append(float(ms[0]) / plain_frames)
+            s.functions["LCS_ProfileEnable"](0)
+        finally:
+            s.close()
+    # the sample is spread evenly over the size order, so its mean stands for the mean instance
+    plain_rate = 1e3 / float(np.mean(plain_ms))
+    value = count * frames / device_s
+    bytes_per_substep = 64 * n_active + 4 * info["tets"]
+    achieved = w.substeps * bytes_per_substep / (device_s / frames) / 1e9
+    return {
+        "workload": "c4: 256 uneven instances, one launch per frame, CUDA graph",
+        "value": value, "unit": "instance-steps/s", "ms_per_frame": 1e3 * device_s / frames, "frames": frames,
+        "proj_per_s": value * w.substeps * (info["edges"] + info["tets"]) / count,
+        "instances": count, "lattice_nodes": info["nodes"], "active_nodes": n_active, "tets": info["tets"],
+        "edges": info["edges"], "substeps": w.substeps, "launch": {"mode": tune["mode"], "threads": tune["threads"],
+                                                                    "autotune_ms_per_frame": tune["ms_per_frame"]},
+        "plain_instance_steps_per_s": plain_rate, "plain_sample": f"{len(picks)} instances spread over the size order, "
+                                                                  f"{plain_frames} frames each after 2 warm-up frames",
+        "batched_over_plain": value / plain_rate,
+        "e2e": {"value": count * frames / e2e_s, "unit": "instance-steps/s", "h2d_bytes_per_step": 92 * count,
+                "d2h_bytes_per_step": 16 * info["nodes"]},
+        "l2": "state larger than L2 (no flush)",
+        "roofline": {"bound": "hbm", "achieved": achieved, "unit": "GB/s", "algorithmic_bytes_per_launch": w.substeps * bytes_per_substep},
+    }
+
+
 def main():
     parser = argparse.ArgumentParser()
     parser.add_argument("--gpus", type=int, default=1)
@@ -173,6 +265,8 @@ def main():
     parser.add_argument("--impl", default="ours", choices=("ours", "reference"))
     parser.add_argument("--workload", default="c2")
     parser.add_argument("--no-cpu-baseline", action="store_true")
+    parser.add_argument("--no-batched", action="store_true")
+    parser.add_argument("--batched-frames", type=int, default=20)
     args = parser.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -274,6 +368,10 @@ def main():
                      "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": substeps * bytes_per_substep},
         "clocks": clocks.summary(),
     }
+    if not args.no_batched:
+        batched = batched_measurement(lib, args.batched_frames, max(args.warmup, 3))
+        batched["roofline"].update(peak=peak, frac=batched["roofline"]["achieved"] / peak, peak_kind=peak_kind)
+        line["batched"] = batched
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(args.workload)
     print(json.dumps(line), flush=True)

@@ -59,6 +59,7 @@ struct Batch {
     Buf<ContactFrame> frames;
     unsigned* hostStatus = nullptr;
     ContactFrame* framesHost = nullptr; size_t framesHostCap = 0;
+    float4* posHost = nullptr; size_t posHostCap = 0;   // pinned staging for GBT_BatchGetPositions
     // instruments
     std::vector<ToolPose> toolFrom, tool;
     bool armed = false;
@@ -85,6 +86,8 @@ void releaseAll() {
     G.derived.release(); G.state.release(); G.frames.release();
     if (G.framesHost) cudaFreeHost(G.framesHost);
     G.framesHost = nullptr; G.framesHostCap = 0;
+    if (G.posHost) cudaFreeHost(G.posHost);
+    G.posHost = nullptr; G.posHostCap = 0;
     for (cudaEvent_t e : G.events) cudaEventDestroy(e);
     G.events.clear();
     G.ready = false; G.armed = false; G.lastH = -1.f;
@@ -478,8 +481,14 @@ LCS_API int GBT_BatchStepMany(float dt, int steps, const void* tools, int useGra
 
 LCS_API int GBT_BatchGetPositions(float* out3N) {
     if (!G.ready || !out3N) return XPBD_ERR_BAD_ARG;
-    std::vector<float4> p(G.N);
-    CK(cudaMemcpyAsync(p.data(), G.pos.p, G.N * sizeof(float4), cudaMemcpyDeviceToHost, G.stream));
+    if (G.posHostCap < (size_t)G.N) {
+        if (G.posHost) cudaFreeHost(G.posHost);
+        G.posHost = nullptr; G.posHostCap = 0;
+        CK(cudaMallocHost(&G.posHost, G.N * sizeof(float4)));
+        G.posHostCap = G.N;
+    }
+    const float4* p = G.posHost;
+    CK(cudaMemcpyAsync(G.posHost, G.pos.p, G.N * sizeof(float4), cudaMemcpyDeviceToHost, G.stream));
     CK(cudaStreamSynchronize(G.stream));
     for (int i = 0; i < G.N; i++) { out3N[3 * i] = p[i].x; out3N[3 * i + 1] = p[i].y; out3N[3 * i + 2] = p[i].z; }
     return 0;
