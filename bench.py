@@ -188,7 +188,7 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6):
     scale = w.stiffness_scale()
     count = len(w.grids)
     n_active = int(sum(int((g.active != 0).sum()) for g in w.grids))
-    with BT.TissueBatch(w.grids, dt=1 / 60, substeps=w.substeps, ks=1e6, stiffness_scale=scale,
+    with BT.TissueBatch(w.grids, dt=1 / 60, substeps=w.substeps, ks=1e6, strain_damping_s=w.strain_damping_s, stiffness_scale=scale,
                         grasp_params=GraspParams(**grasp), dll_path=lib) as b:
         info = b.info()
         b.set_gravity(0.0, -981.0, 0.0)
@@ -216,7 +216,7 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6):
     plain_ms = []
     for i in picks:
         g = w.grids[i]
-        s = PlainTissue(g, dt=1 / 60, substeps=w.substeps, ks=1e6, grasp_params=GraspParams(**grasp), dll_path=lib)
+        s = PlainTissue(g, dt=1 / 60, substeps=w.substeps, ks=1e6, strain_damping_s=w.strain_damping_s, grasp_params=GraspParams(**grasp), dll_path=lib)
         try:
             mu, kappa = s.tet_stiffness()
             s.set_tet_stiffness(mu * scale[i], kappa * scale[i])
@@ -257,6 +257,61 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6):
     }
 
 
+def adjoint_measurement(lib, reps=3):
+    """C5 differentiable identification: 32 x 16(up) x 32 cells (98,304 tets), 10 substeps, 50 frames,
+    checkpoints every 5 substeps.  Times (wall clock around the synchronous C-ABI calls, after one
+    warm-up) the checkpointing forward rollout, the adjoint (recompute + reverse sweep), and the
+    plain forward (50 LCS_Step frames) on the same mesh; reports backward / forward."""
+    import torch
+
+    from genesis_tissue_simulation_gb300 import diff as D
+    from genesis_tissue_simulation_gb300.native_backend import Capsule
+
+    c5 = D.make_c5()
+    with c5.open(lib) as t:
+        theta = torch.tensor(c5.theta_initial, device="cuda")
+        path = torch.tensor(c5.path, device="cuda")
+        target = t.forward(torch.tensor(c5.theta_hidden, device="cuda"), path).clone()
+        top = torch.tensor(c5.top, device="cuda")
+        fwd, bwd = [], []
+        for k in range(reps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            x = t.forward(theta, path)
+            t1 = time.perf_counter()
+            g = torch.zeros_like(x)
+            g[top] = 2.0 * (x[top] - target[top]) / (3 * len(c5.top))
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            grads = t.backward(g)
+            t3 = time.perf_counter()
+            if k:
+                fwd.append(t1 - t0)
+                bwd.append(t3 - t2)
+        loss = float(((x[top] - target[top]) ** 2).mean())
+        info = t.info()
+        assert torch.isfinite(grads["theta"]).all() and torch.isfinite(grads["path"]).all()
+        # plain forward: the same frames through LCS_Step
+        sess = t.session   # its per-tet stiffness is the bake, i.e. the uniform initial estimate's material
+        caps = [Capsule(tuple(c5.path[k, :3]), tuple(c5.path[k, 3:]), c5.radius) for k in range(c5.frames + 1)]
+        sess.set_capsule(caps[0])
+        torch.cuda.synchronize()
+        p0 = time.perf_counter()
+        for k in range(c5.frames):
+            sess.set_capsule(caps[k + 1])
+            sess.step()
+        torch.cuda.synchronize()
+        plain = time.perf_counter() - p0
+    f, b = float(np.median(fwd)), float(np.median(bwd))
+    frames, substeps = c5.frames, c5.params["substeps"]
+    return {"workload": "c5: 32x16x32 cells, 98,304 tets, 10 substeps, 50 frames, checkpoints every 5 substeps",
+            "forward_ms": 1e3 * f, "backward_ms": 1e3 * b, "plain_forward_ms": 1e3 * plain, "backward_over_forward": b / f,
+            "backward_over_plain_forward": b / plain, "frames_per_s_forward": frames / f, "loss": loss,
+            "launch": "grid" if info["grid_launch"] else "one CTA", "ctas": info["ctas"],
+            "timing": f"wall clock around each synchronous call, median of {reps} after one warm-up",
+            "gradients": "theta [98,304] and capsule path [51, 6]", "substeps": frames * substeps}
+
+
 def main():
     parser = argparse.ArgumentParser()
     parser.add_argument("--gpus", type=int, default=1)
@@ -266,6 +321,7 @@ def main():
     parser.add_argument("--workload", default="c2")
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--no-batched", action="store_true")
+    parser.add_argument("--no-adjoint", action="store_true")
     parser.add_argument("--batched-frames", type=int, default=20)
     args = parser.parse_args()
     world, rank, local = dist_setup()
@@ -368,6 +424,8 @@ def main():
                      "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": substeps * bytes_per_substep},
         "clocks": clocks.summary(),
     }
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_measurement(lib)
     if not args.no_batched:
         batched = batched_measurement(lib, args.batched_frames, max(args.warmup, 3))
         batched["roofline"].update(peak=peak, frac=batched["roofline"]["achieved"] / peak, peak_kind=peak_kind)

@@ -10,56 +10,10 @@
 // node-to-thread map in every phase, so a node's contact, velocity update and next predict need
 // no barrier between them.
 #include "tissue_device.cuh"
+#include "grid_sync.cuh"
 #include "frame_kernels.h"
 
 namespace gbt {
-
-// ---------------------------------------------------------------------------------------------
-// barriers
-// ---------------------------------------------------------------------------------------------
-// Grid barrier on a monotonically increasing arrival counter (reset by the host before launch).
-// The arriving thread releases its block's writes with a gpu-scope fence, spins with a clock
-// budget, and acquires.  A barrier that times out records kSyncTimeout in the status word; every
-// block leaves at its next barrier, so the launch ends and the host reports the error.
-constexpr unsigned kSyncTimeout = 1u;
-
-struct GridSync {
-    unsigned* counter; unsigned* status; unsigned nblocks; unsigned target;
-    long long budget;     // spin budget in SM clock cycles
-    unsigned extra;       // arrivals awaited beyond the grid (non-zero only in the timeout test mode)
-    __device__ int rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
-    __device__ int size() const { return gridDim.x * blockDim.x; }
-    __device__ bool leader() const { return blockIdx.x == 0 && threadIdx.x == 0; }
-    __device__ bool sync() {
-        __shared__ unsigned ok;
-        __syncthreads();
-        target += nblocks;
-        if (threadIdx.x == 0) {
-            __threadfence();
-            atomicAdd(counter, 1u);
-            long long start = clock64();
-            while (true) {
-                unsigned now;
-                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(now) : "l"(counter) : "memory");
-                if ((int)(now - (target + extra)) >= 0) break;
-                if (*(volatile unsigned*)status != 0u) break;
-                if (clock64() - start > budget) { atomicOr(status, kSyncTimeout); break; }
-            }
-            __threadfence();
-            ok = *(volatile unsigned*)status == 0u;
-        }
-        __syncthreads();
-        return ok != 0u;
-    }
-};
-
-struct BlockSync {
-    unsigned* status;
-    __device__ int rank() const { return threadIdx.x; }
-    __device__ int size() const { return blockDim.x; }
-    __device__ bool sync() { __syncthreads(); return true; }
-    __device__ bool leader() const { return threadIdx.x == 0; }
-};
 
 // ---------------------------------------------------------------------------------------------
 // contact model 0: shaft capsule + jaw slab CCD gate, k_SolveCCDContact (xpbd_solver.cu:1049-1123)

@@ -18,6 +18,7 @@
 
 #include "frame_kernels.h"
 #include "mesh_build.h"
+#include "session_view.h"
 #include "../../include/gbtissue.h"
 
 using namespace gbt;
@@ -737,4 +738,22 @@ LCS_API void LCS_Shutdown() {
     if (S.stream) cudaStreamSynchronize(S.stream);
     LCS_ProfileEnable(0);
     freeAll();
+}
+
+// ---------------------------------------------------------------------------------------------
+// session view for the differentiable rollout (adjoint_api.cu)
+// ---------------------------------------------------------------------------------------------
+int gbt::sessionView(SessionView* v) {
+    if (!S.physReady || !v) return XPBD_ERR_NOT_READY;
+    v->mesh = deviceMesh();
+    v->stream = S.stream; v->device = S.device; v->smCount = S.smCount; v->clockKHz = S.clockKHz; v->launchMode = S.launchMode;
+    v->N = S.N; v->E = S.E; v->T = S.T; v->numSubsteps = S.numSubsteps > 0 ? S.numSubsteps : 1;
+    v->ks = S.ks; v->betaS = S.betaS; v->kb = (S.B > 0) ? S.kb : 0.f; v->strainDamping = S.strainDamping; v->omega = S.omega;
+    v->damping = S.damping; v->alpha = S.alpha; v->youngE = S.youngE; v->syncBudgetSeconds = S.syncBudgetSeconds;
+    v->cutActive = S.cutReady && S.toolSet && !S.pressure;
+    v->contactModel = S.contactModel;
+    v->cp = S.cp;
+    v->tetColorOrder = S.tetColorOrder.data();
+    v->state = S.state.p;
+    return 0;
 }

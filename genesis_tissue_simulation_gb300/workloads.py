@@ -60,9 +60,17 @@ def tet_stiffness(params: dict, baked_mu_v: np.ndarray, baked_kappa_v: np.ndarra
         kappa_v = np.full(len(baked_mu_v), 1.0 / m["volume_compliance"], dtype=np.float32)
         return baked_mu_v.astype(np.float32), kappa_v
     if m["mode"] == "per_tet_compliance":
-        scale = young_scale(per_tet_compliance(len(baked_mu_v), m["low"], m["high"], m["seed"]), m["young_pa"])
+        scale = young_scale(per_tet_compliance(len(baked_mu_v), m["low"], m["high"], m["seed"]), scale_modulus(m))
         return (baked_mu_v * scale).astype(np.float32), (baked_kappa_v * scale).astype(np.float32)
     raise ValueError(f"unknown material mode {m['mode']}")
+
+
+def scale_modulus(material: dict) -> float:
+    """The modulus M of the compliance map scale = 1 / (c M).  Without a ``compliance_reference``,
+    c is the tet's Young's compliance (1/Pa) and M the bake's Young's modulus; with one, c is
+    relative to it (c = compliance_reference leaves the bake unscaled) and M = 1 / reference."""
+    ref = material.get("compliance_reference")
+    return float(material["young_pa"]) if ref is None else 1.0 / float(ref)
 
 
 def young_scale(compliance, young_pa):

@@ -138,6 +138,32 @@ LCS_API void GBT_BatchProfileEnable(int enabled);
 LCS_API int GBT_BatchProfileRead(float* msTotal);                      /* device ms of the profiled step calls */
 LCS_API void GBT_BatchShutdown(void);
 
+/* ---- differentiable rollout (no counterpart in the reference, whose solver is not differentiable)
+ * Runs the plain substep (predict, lattice edges, unguarded Neo-Hookean tets, capsule contact of
+ * the shaft, velocity update) on the LCS session's mesh and returns adjoints of the final node
+ * positions' loss.  Every array argument of GBT_DiffForward / GBT_DiffBackward is DEVICE memory on
+ * the session's device (a torch CUDA tensor's data pointer); sizes: N nodes, T tets (storage order,
+ * as LCS_SetTetStiffness), F frames.  Sessions with bending, perpendicular damping, edge-only
+ * fallback, an active blade or contact model != 0 return LCS_ERR_UNSUPPORTED.                    */
+/* Take the session's current state as the rollout origin and its per-tet stiffness as the bake
+ * that log-compliances scale: (mu V, kappa V) * 1 / (exp(theta) * youngPa).  Checkpoints are kept
+ * every checkpointEvery substeps; buffers are sized for up to maxFrames frames. */
+LCS_API int GBT_DiffBegin(float youngPa, int checkpointEvery, int maxFrames);
+/* F frames from the origin.  logCompliance float[T]; capsulePath float[(F + 1) * 6] = end points
+ * (a, b) of the capsule per command, frame f moving from command f to f + 1 (NULL: no instrument);
+ * finalPos float[3N] or NULL.  The session is left at the final state. */
+LCS_API int GBT_DiffForward(float dt, int frames, const float* logCompliance, const float* capsulePath, float capsuleRadius,
+                            float* finalPos);
+/* Adjoint of the last forward.  gradPos float[3N] in; out: gradLogCompliance float[T];
+ * gradCapsulePath float[(F + 1) * 6] or NULL; gradRestLength float[6N] by directed slot 6p + s of
+ * the edge's owner (rest length of each lattice edge) or NULL; gradRestInverse float[9T] (each
+ * tet's rest inverse Dm^-1, row major, storage order) or NULL; gradOrigin float[6N] (3N position
+ * then 3N velocity adjoints of the origin state) or NULL. */
+LCS_API int GBT_DiffBackward(const float* gradPos, float* gradLogCompliance, float* gradCapsulePath, float* gradRestLength,
+                             float* gradRestInverse, float* gradOrigin);
+LCS_API int GBT_DiffInfo(int* out4);   /* grid launch (1) or one CTA (0), CTAs, checkpoint interval, max frames */
+LCS_API void GBT_DiffEnd(void);
+
 /* LCS_StepNoAlloc has no counterpart in the reference.  It advances the session by one frame
  * exactly as LCS_Step does, for hosts that cannot let a plugin allocate GPU memory while they run
  * (engines that own every device allocation through their own pool or budget, and real-time

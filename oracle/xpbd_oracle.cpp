@@ -1064,3 +1064,6 @@ API int ORC_Threads() {
     return 1;
 #endif
 }
+
+// differentiable rollout and its adjoint
+#include "diff_oracle.inc"

@@ -15,8 +15,9 @@ ROOT = Path(__file__).resolve().parents[1]
 HEADER = ROOT / "include" / "gbtissue.h"
 
 
-def declared_symbols():
-    return sorted(set(re.findall(r"LCS_API\s+[\w\s\*]+?\b(LCS_\w+)\s*\(", HEADER.read_text())))
+def declared_symbols(prefixes=("LCS_",)):
+    names = re.findall(r"LCS_API\s+[\w\s\*]+?\b((?:LCS|GBT)_\w+)\s*\(", HEADER.read_text())
+    return sorted(n for n in set(names) if n.startswith(prefixes))
 
 
 def test_abi_layout():
@@ -39,7 +40,9 @@ def test_header_declares_plain_path():
 def test_cuda_library_exports_declared_symbols():
     lib = native_build.build()
     dll = ctypes.CDLL(str(lib))
-    missing = [n for n in declared_symbols() if not hasattr(dll, n)]
+    names = declared_symbols(("LCS_", "GBT_"))
+    assert any(n.startswith("GBT_Diff") for n in names) and any(n.startswith("GBT_Batch") for n in names)
+    missing = [n for n in names if not hasattr(dll, n)]
     assert not missing, missing
 
 
