@@ -253,7 +253,8 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6):
         "e2e": {"value": count * frames / e2e_s, "unit": "instance-steps/s", "h2d_bytes_per_step": 92 * count,
                 "d2h_bytes_per_step": 16 * info["nodes"]},
         "l2": "state larger than L2 (no flush)",
-        "roofline": {"bound": "hbm", "achieved": achieved, "unit": "GB/s", "algorithmic_bytes_per_launch": w.substeps * bytes_per_substep},
+        "roofline": {"bound": "hbm", "achieved": achieved, "unit": "GB/s", "algorithmic_bytes_per_launch": w.substeps * bytes_per_substep,
+                     "traffic": ncu_traffic_per_launch("ncu_batch_frame_c4")},
     }
 
 
@@ -322,6 +323,8 @@ def main():
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--no-batched", action="store_true")
     parser.add_argument("--no-adjoint", action="store_true")
+    parser.add_argument("--only", default="all", choices=("all", "batched", "adjoint"),
+                        help="run one section alone and print its JSON object (for profiling)")
     parser.add_argument("--batched-frames", type=int, default=20)
     args = parser.parse_args()
     world, rank, local = dist_setup()
@@ -343,6 +346,11 @@ def main():
     if world > 1:
         dist.barrier()
     lib = native_build.build()
+    if args.only != "all":   # one section alone (profiling runs): its JSON object, no bench line
+        section = (batched_measurement(lib, args.batched_frames, max(args.warmup, 3)) if args.only == "batched"
+                   else adjoint_measurement(lib, reps=max(args.steps, 1)))
+        print(json.dumps({"only": args.only, **section}), flush=True)
+        return
 
     w = W.make(args.workload, steps=args.warmup + args.steps)
     session = w.open(lib)

@@ -111,16 +111,16 @@ int launch(const SessionView& v, bool backward, DeviceMesh m, const DiffBuffers&
 
 }  // namespace
 
-LCS_API int GBT_DiffBegin(float youngPa, int checkpointEvery, int maxFrames) {
+LCS_API int GBT_DiffBegin(float scaleModulus, int checkpointEvery, int maxFrames) {
     releaseAll();
     SessionView v{};
     int rc = sessionView(&v);
     if (rc) return rc;
-    if (!(youngPa > 0.f) || !std::isfinite(youngPa) || checkpointEvery < 1 || maxFrames < 1) return XPBD_ERR_BAD_ARG;
+    if (!(scaleModulus > 0.f) || !std::isfinite(scaleModulus) || checkpointEvery < 1 || maxFrames < 1) return XPBD_ERR_BAD_ARG;
     // the differentiable substep: predict, lattice edges, unguarded tets, capsule contact, velocity
     if (v.kb > 0.f || v.betaS > 0.f || v.ks <= 0.f || v.cutActive || v.contactModel != 0) return LCS_ERR_UNSUPPORTED;
     D.N = v.N; D.E = v.E; D.T = v.T; D.every = checkpointEvery; D.maxFrames = maxFrames; D.substeps = v.numSubsteps;
-    D.young = youngPa;
+    D.young = scaleModulus;
     const size_t N = v.N, E = v.E, T = v.T, K = checkpointEvery;
     const size_t total = (size_t)maxFrames * v.numSubsteps, segments = (total + K - 1) / K;
     CK(D.originPos.ensure(N)); CK(D.originVel.ensure(N)); CK(D.finalPos.ensure(N)); CK(D.finalVel.ensure(N));

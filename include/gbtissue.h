@@ -146,9 +146,10 @@ LCS_API void GBT_BatchShutdown(void);
  * as LCS_SetTetStiffness), F frames.  Sessions with bending, perpendicular damping, edge-only
  * fallback, an active blade or contact model != 0 return LCS_ERR_UNSUPPORTED.                    */
 /* Take the session's current state as the rollout origin and its per-tet stiffness as the bake
- * that log-compliances scale: (mu V, kappa V) * 1 / (exp(theta) * youngPa).  Checkpoints are kept
- * every checkpointEvery substeps; buffers are sized for up to maxFrames frames. */
-LCS_API int GBT_DiffBegin(float youngPa, int checkpointEvery, int maxFrames);
+ * that log-compliances scale: (mu V, kappa V) * 1 / (exp(theta) * scaleModulus) (scaleModulus =
+ * the bake's Young's modulus in Pa makes exp(theta) a Young's compliance in 1/Pa).  Checkpoints
+ * are kept every checkpointEvery substeps; buffers are sized for up to maxFrames frames. */
+LCS_API int GBT_DiffBegin(float scaleModulus, int checkpointEvery, int maxFrames);
 /* F frames from the origin.  logCompliance float[T]; capsulePath float[(F + 1) * 6] = end points
  * (a, b) of the capsule per command, frame f moving from command f to f + 1 (NULL: no instrument);
  * finalPos float[3N] or NULL.  The session is left at the final state. */

@@ -44,3 +44,12 @@ def reference_lib():
             pytest.skip("reference sources not staged (oracle/build_ref.sh stage)")
         subprocess.run(["bash", str(ROOT / "oracle" / "build_ref.sh"), "build"], check=True)
     return REFERENCE_LIB
+
+
+def results_dir():
+    """Where GPU tests append the figures they measure (JSON lines): $GBT_RESULTS_DIR, else
+    test_results/ at the repository root (git-ignored)."""
+    import os
+    path = Path(os.environ.get("GBT_RESULTS_DIR", ROOT / "test_results"))
+    path.mkdir(parents=True, exist_ok=True)
+    return path

@@ -3,10 +3,13 @@ the CPU oracle: forward positions and adjoints against the FP32 oracle, which ev
 operations in the same order, in both launch shapes; the torch.autograd.Function; and the C5
 identification workload's gradient against the FP64 reference gradient and FP64 central
 finite differences on 64 random directions (relative error <= 1e-3)."""
+import json
+
 import numpy as np
 import pytest
 import torch
 
+from conftest import results_dir
 from diff_cases import YOUNG, C5Oracle, Case, bind_oracle, oracle_adjoint, oracle_rollout
 
 pytestmark = pytest.mark.gpu
@@ -15,6 +18,11 @@ pytestmark = pytest.mark.gpu
 def rel(a, b):
     a, b = np.ravel(np.asarray(a, np.float64)), np.ravel(np.asarray(b, np.float64))
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def record(name, **values):
+    with open(results_dir() / "adjoint.jsonl", "a") as f:
+        f.write(json.dumps({"case": name, **values}) + "\n")
 
 
 def gpu_tissue(case, lib, mode, modulus=YOUNG):
@@ -130,6 +138,8 @@ def test_c5_gradient_matches_fp64_reference(c5_fp64, c5_gpu):
     c5 = c5_fp64.c5
     loss64 = c5_fp64.loss(c5.theta_initial, c5.path)
     gt, gp = c5_fp64.gradient(c5.theta_initial, c5.path)
+    record("c5_fp64_reference", loss_fp32=c5_gpu["loss"], loss_fp64=loss64, rel_theta=rel(c5_gpu["theta"], gt),
+           rel_path=rel(c5_gpu["path"], gp))
     assert abs(c5_gpu["loss"] - loss64) <= 1e-3 * loss64
     assert rel(c5_gpu["theta"], gt) <= 1e-3, rel(c5_gpu["theta"], gt)
     assert rel(c5_gpu["path"], gp) <= 1e-3, rel(c5_gpu["path"], gp)
@@ -149,4 +159,5 @@ def test_c5_gradient_matches_fp64_central_differences(c5_fp64, c5_gpu):
         dn = c5_fp64.loss(theta - eps * dth, path - eps * dpa)
         fd.append((up - dn) / (2 * eps))
         an.append(float((c5_gpu["theta"] * dth).sum() + (c5_gpu["path"] * dpa).sum()))
+    record("c5_fp64_central_differences", directions=64, step=eps, rel=rel(an, fd))
     assert rel(an, fd) <= 1e-3, (rel(an, fd), an[:4], fd[:4])

@@ -18,7 +18,9 @@ from genesis_tissue_simulation_gb300.grid import build_grid
 from genesis_tissue_simulation_gb300.native_backend import PlainTissue, GraspParams
 
 pytestmark = pytest.mark.gpu
-OUT = Path(__file__).resolve().parents[1] / "gpurun_out"
+from conftest import results_dir
+
+OUT = results_dir()
 SMALL = (4.78, 2.38, 3.98)
 
 
