@@ -117,8 +117,8 @@ LCS_API int GBT_DiffBegin(float scaleModulus, int checkpointEvery, int maxFrames
     int rc = sessionView(&v);
     if (rc) return rc;
     if (!(scaleModulus > 0.f) || !std::isfinite(scaleModulus) || checkpointEvery < 1 || maxFrames < 1) return XPBD_ERR_BAD_ARG;
-    // the differentiable substep: predict, lattice edges, unguarded tets, capsule contact, velocity
-    if (v.kb > 0.f || v.betaS > 0.f || v.ks <= 0.f || v.cutActive || v.contactModel != 0) return LCS_ERR_UNSUPPORTED;
+    // the differentiable substep: predict, lattice edges, unguarded tets, capsule contact, velocity (no guard)
+    if (v.kb > 0.f || v.betaS > 0.f || v.ks <= 0.f || v.cutActive || v.contactModel != 0 || v.volumePasses > 0) return LCS_ERR_UNSUPPORTED;
     D.N = v.N; D.E = v.E; D.T = v.T; D.every = checkpointEvery; D.maxFrames = maxFrames; D.substeps = v.numSubsteps;
     D.young = scaleModulus;
     const size_t N = v.N, E = v.E, T = v.T, K = checkpointEvery;

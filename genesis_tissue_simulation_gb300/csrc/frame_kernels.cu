@@ -198,6 +198,68 @@ __device__ void tickEdge(const DeviceMesh& m, const CutParams& cu, int e, bool c
 }
 
 // ---------------------------------------------------------------------------------------------
+// tissue guard: the feasibility chain after contact (finishFeasible, xpbd_solver.cu:628-741)
+// ---------------------------------------------------------------------------------------------
+// If a live tet is below the minimum relative volume: two colour sweeps of a linearised repair; if
+// one still is: every vertex of a tet whose substep motion may pass below the minimum restarts from
+// its substep-start position and advances as far as its incident live tets allow, in eight
+// lattice-parity colours whose order rotates with the substep index.  The flags are written by any
+// thread and read by all after a barrier, so every branch below is uniform.
+template <class Sync>
+__device__ bool guardFeasible(const DeviceMesh& m, const FrameCoeffs& fc, int substepIndex, Sync& sync) {
+    const int r = sync.rank(), R = sync.size();
+    const int T = m.nTetColors > 0 ? m.tetRange[m.nTetColors - 1].y : 0;
+    const int nodeEnd = m.nodeBase + m.nNodes;
+    const float minimum = fc.minVolume;
+    if (sync.leader()) { m.guardFlags[0] = 0u; m.guardFlags[1] = 0u; }
+    for (int i = m.nodeBase + r; i < nodeEnd; i += R) m.needed[i] = 0;
+    if (!sync.sync()) return false;
+    for (int k = r; k < T; k += R) {
+        int meta = m.tetMeta[k];
+        if ((meta & 8) == 0) continue;
+        float J = tetVolume(m, k, meta);
+        if (!isfinite(J) || J < minimum) m.guardFlags[0] = 1u;
+    }
+    if (!sync.sync()) return false;
+    if (*(volatile unsigned*)&m.guardFlags[0] == 0u) return true;
+    for (int pass = 0; pass < 2; pass++)
+        for (int c = 0; c < m.nTetColors; c++) {
+            int2 rg = m.tetRange[c];
+            for (int k = rg.x + r; k < rg.y; k += R) repairTet(m, k, minimum);
+            if (!sync.sync()) return false;
+        }
+    for (int k = r; k < T; k += R) {
+        int meta = m.tetMeta[k];
+        if ((meta & 8) == 0) continue;
+        float J = tetVolume(m, k, meta);
+        if (!isfinite(J) || J < minimum) m.guardFlags[1] = 1u;
+    }
+    if (!sync.sync()) return false;
+    if (*(volatile unsigned*)&m.guardFlags[1] == 0u) return true;
+    for (int k = r; k < T; k += R) needFeasible(m, k, minimum);
+    if (!sync.sync()) return false;
+    for (int i = m.nodeBase + r; i < nodeEnd; i += R)
+        if (m.needed[i]) {
+            float4 P = m.pos[i], Q = m.prev[i];
+            m.feasTarget[i] = P;
+            m.pos[i] = make_float4(Q.x, Q.y, Q.z, P.w);
+        }
+    if (!sync.sync()) return false;
+    const int nx = m.dx + 1, ny = m.dy + 1, nz = m.dz + 1;
+    const int cx = (nx + 1) / 2, cy = (ny + 1) / 2, cz = (nz + 1) / 2, sites = cx * cy * cz;
+    for (int k = 0; k < 8; k++) {
+        int color = (k + substepIndex) & 7;
+        for (int lane = r; lane < sites; lane += R) {
+            int x = 2 * (lane % cx) + (color & 1), y = 2 * ((lane / cx) % cy) + ((color >> 1) & 1), z = 2 * (lane / (cx * cy)) + ((color >> 2) & 1);
+            if (x >= nx || y >= ny || z >= nz) continue;
+            feasibleVertex(m, x + nx * (y + ny * z), minimum);
+        }
+        if (!sync.sync()) return false;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------------------------
 // frame driver
 // ---------------------------------------------------------------------------------------------
 template <class Sync>
@@ -294,13 +356,26 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 if (!sync.sync()) return;
                 mark(s, kPhaseTets);
             }
+            if (fc.guarded)   // tensile reinforcement after the tet colours (xpbd_solver.cu:2531-2533)
+                for (int pass = 0; pass < fc.volumePasses; pass++)
+                    for (int c = 0; c < m.nTetColors; c++) {
+                        int2 rg = m.tetRange[c];
+                        for (int k = rg.x + r; k < rg.y; k += R) projectTensile(m, k, fc, pass);
+                        if (!sync.sync()) return;
+                        mark(s, kPhaseTets);
+                    }
         }
         // -- contact, velocity --
         float t = fminf(1.f, (float)(fc.firstSubstep + s + 1) / (float)fc.numSubsteps);
         ContactFrame cf;
         if (fc.contact && !m.nodeInstance) cf = contactFrame(from, to, t, cp, fc.contactAlphaH2);
+        if (fc.guarded) {   // contact, then the feasibility chain, then the velocity update
+            if (fc.contact)
+                for (int i = m.nodeBase + r; i < nodeEnd; i += R) contactNode(m, i, cf, cp);
+            if (!guardFeasible(m, fc, fc.firstSubstep + s + 1, sync)) return;
+        }
         for (int i = m.nodeBase + r; i < nodeEnd; i += R) {
-            if (fc.contact) {
+            if (fc.contact && !fc.guarded) {
                 if (m.nodeInstance) {   // batched instances: each node meets its own instance's tool
                     const ContactFrame& own = m.contactFrames[(size_t)(fc.firstSubstep + s) * m.nInstances + m.nodeInstance[i]];
                     contactNode(m, i, own, cp);

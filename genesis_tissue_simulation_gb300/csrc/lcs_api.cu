@@ -55,7 +55,10 @@ struct Session {
     int numSubsteps = 20;
     float ks = 0, kb = 0, alpha = 0, betaS = 0, betaB = 0, youngE = 0, poisson = 0.45f, strainDamping = 0, omega = 1, damping = 0;
     float bulkDampingSeconds = 0.003125f, tissueHardening = 80.f;
-    int volumePasses = 0;
+    int volumePasses = 0; float minVolume = 0.f;
+    // tissue guard buffers (LCS_SetTissueGuard): fibre multipliers, feasibility candidates and marks,
+    // incident colour slots per node (CSR), two flags
+    DBuf<float> fiberLambda; DBuf<float4> feasTarget; DBuf<int> needed, incOff, incTet; DBuf<unsigned> guardFlags;
     float lastH = -1.f;
     // topology sizes (host copies for diagnostics)
     int E = 0, B = 0, T = 0;
@@ -110,6 +113,8 @@ void freePhysics() {
                     &S.bendSrc, &S.bendLive, &S.tetMeta, &S.tetOwner, &S.edgeSupport}) b->release();
     S.edgeEnds.release(); S.edgeRest.release(); S.bendIJK.release(); S.bendPairs.release(); S.tetIds.release();
     S.tetAlpha.release(); S.tetStiff.release(); S.state.release();
+    S.fiberLambda.release(); S.feasTarget.release(); S.needed.release(); S.incOff.release(); S.incTet.release(); S.guardFlags.release();
+    S.volumePasses = 0; S.minVolume = 0.f;
     S.physReady = false; S.toolArmed = false; S.E = S.B = S.T = 0; S.lastH = -1.f;
 }
 void freeAll() {
@@ -170,6 +175,8 @@ DeviceMesh deviceMesh() {
     m.tetIds = S.tetIds.p; m.tetMeta = S.tetMeta.p; m.tetOwner = S.tetOwner.p; m.tetAlpha = S.tetAlpha.p; m.tetStiff = S.tetStiff.p;
     m.edgeSupport = S.edgeSupport.p;
     std::memcpy(m.typeB, S.typeB, sizeof(S.typeB));
+    m.fiberLambda = S.fiberLambda.p; m.feasTarget = S.feasTarget.p; m.needed = S.needed.p;
+    m.incOff = S.incOff.p; m.incTet = S.incTet.p; m.guardFlags = S.guardFlags.p;
     return m;
 }
 
@@ -374,8 +381,25 @@ LCS_API int LCS_SetTissueGuard(float minimum, int passes, int count, const int* 
     (void)capture;
     if (!S.physReady || S.lastH > 0 || !std::isfinite(minimum) || minimum < 0 || minimum > .95f || passes < 0 || passes > 4 ||
         count != S.N || !inside) return XPBD_ERR_BAD_ARG;
-    if (passes > 0) return LCS_ERR_UNSUPPORTED;
-    S.volumePasses = 0;
+    // incident colour slots of every node (the feasibility line search reads each vertex's tets)
+    std::vector<int> off(S.N + 1, 0), inc((size_t)4 * S.T);
+    for (int k = 0; k < S.T; k++)
+        for (int c = 0; c < 4; c++) off[S.tetIdsStorage[4 * (size_t)S.tetColorOrder[k] + c] + 1]++;
+    for (int i = 0; i < S.N; i++) off[i + 1] += off[i];
+    std::vector<int> cursor(off.begin(), off.end() - 1);
+    for (int k = 0; k < S.T; k++)
+        for (int c = 0; c < 4; c++) inc[cursor[S.tetIdsStorage[4 * (size_t)S.tetColorOrder[k] + c]]++] = k;
+    CK(S.incOff.upload(off.data(), off.size(), S.stream));
+    CK(S.incTet.upload(inc.data(), inc.size(), S.stream));
+    CK(S.fiberLambda.alloc((size_t)6 * std::max(S.T, 1)));
+    CK(S.feasTarget.alloc(S.N));
+    CK(S.needed.alloc(S.N));
+    CK(S.guardFlags.alloc(2));
+    CK(cudaMemsetAsync(S.needed.p, 0, S.N * sizeof(int), S.stream));
+    CK(cudaMemsetAsync(S.guardFlags.p, 0, 2 * sizeof(unsigned), S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    S.volumePasses = passes;
+    S.minVolume = minimum;
     return 0;
 }
 LCS_API int LCS_SetTissueMaterial(float strength, float bulkDamping) {
@@ -477,6 +501,11 @@ LCS_API int LCS_Step(float dt) {
     fc.betaS = S.betaS;
     fc.omega = S.omega;
     fc.dampingOverH = fmaxf(0.f, S.strainDamping) / h;
+    fc.guarded = (S.volumePasses > 0 && S.T > 0) ? 1 : 0;
+    fc.volumePasses = S.volumePasses;
+    fc.tensileStrength = S.tissueHardening;
+    fc.bulkDampingOverH = S.bulkDampingSeconds / h;
+    fc.minVolume = S.minVolume;
     fc.contact = (S.toolArmed && S.contactModel == 0) ? 1 : 0;
     fc.contactAlphaH2 = S.cp.contactAlpha / (h * h);
     fc.cut = (S.cutReady && S.toolSet && !S.pressure) ? 1 : 0;
@@ -692,6 +721,11 @@ LCS_API int LCS_StepNoAlloc(float dt) {
     fc.betaS = S.betaS;
     fc.omega = S.omega;
     fc.dampingOverH = fmaxf(0.f, S.strainDamping) / h;
+    fc.guarded = (S.volumePasses > 0 && S.T > 0) ? 1 : 0;
+    fc.volumePasses = S.volumePasses;
+    fc.tensileStrength = S.tissueHardening;
+    fc.bulkDampingOverH = S.bulkDampingSeconds / h;
+    fc.minVolume = S.minVolume;
     fc.contact = (S.toolArmed && S.contactModel == 0) ? 1 : 0;
     fc.contactAlphaH2 = S.cp.contactAlpha / (h * h);
     fc.cut = (S.cutReady && S.toolSet && !S.pressure) ? 1 : 0;
@@ -751,6 +785,7 @@ int gbt::sessionView(SessionView* v) {
     v->ks = S.ks; v->betaS = S.betaS; v->kb = (S.B > 0) ? S.kb : 0.f; v->strainDamping = S.strainDamping; v->omega = S.omega;
     v->damping = S.damping; v->alpha = S.alpha; v->youngE = S.youngE; v->syncBudgetSeconds = S.syncBudgetSeconds;
     v->cutActive = S.cutReady && S.toolSet && !S.pressure;
+    v->volumePasses = S.volumePasses;
     v->contactModel = S.contactModel;
     v->cp = S.cp;
     v->tetColorOrder = S.tetColorOrder.data();

@@ -11,6 +11,7 @@ struct SessionView {
     int N, E, T, numSubsteps;
     float ks, betaS, kb, strainDamping, omega, damping, alpha, youngE, syncBudgetSeconds;
     bool cutActive;                    // a blade is set on an initialised cut: the topology may change
+    int volumePasses;                  // tissue guard armed (> 0)
     int contactModel;
     ContactParams cp;
     const int* tetColorOrder;          // host [T]: colour slot -> storage index

@@ -47,6 +47,10 @@ struct DeviceMesh {
     // (contactFrames: [substep][instance] instrument frames of the frame, evaluated on the host)
     const int* nodeInstance; const ContactFrame* contactFrames; int nInstances;
     float typeB[6][9];                                    // rest Dm^-1 of each Kuhn type, row major
+    // tissue guard (armed by LCS_SetTissueGuard): per-tet fibre multipliers [6T], the feasibility
+    // chain's candidate positions and marks [N], incident live-tet lists (CSR over colour slots),
+    // and two flags (candidate below the minimum volume; still below after the repair)
+    float* fiberLambda; float4* feasTarget; int* needed; const int* incOff; const int* incTet; unsigned* guardFlags;
 };
 
 // Per-frame coefficients, computed on the host in FP32 exactly as xpbd_begin_frame does
@@ -57,6 +61,8 @@ struct FrameCoeffs {
     int doEdges, fallback, doBend, doStrain, perpDamp, contact, cut;
     float h, invH, invH2, alphaTilde, betaGammaHS, alphaB, betaGammaHB, velScale, betaS;
     float omega, dampingOverH, fallbackInvEh2, contactAlphaH2;
+    int guarded, volumePasses;       // tissue guard: guarded tet form, tensile passes, feasibility chain
+    float tensileStrength, bulkDampingOverH, minVolume;
     long long spinBudget;            // grid-barrier spin budget, SM clock cycles
     int syncTestExtra;               // > 0: barriers await arrivals that never come (timeout test)
     int stageNodes;                  // one-CTA kernel: node state staged in shared memory
@@ -144,6 +150,26 @@ __device__ __forceinline__ float powMinusTwoThirds(float J) {
     return y * y;
 }
 
+// log x for the guarded bulk strain (x >= 0.05, a positive normal float): x = m 2^e with m in
+// (sqrt(1/2), sqrt(2)], log m = 2 atanh(s), s = (m - 1)/(m + 1), by its odd series to s^11 (the
+// truncation is below 3e-9 relative), e ln 2 with ln 2 split into an exactly representable head
+// and a tail.  The CPU restatement evaluates the same sequence.
+__device__ __forceinline__ float logPositive(float x) {
+    unsigned bits = __float_as_uint(x);
+    int e = (int)(bits >> 23) - 127;
+    float m = __uint_as_float((bits & 0x007FFFFFu) | 0x3F800000u);
+    if (m > 1.41421356f) { m = m * 0.5f; e += 1; }
+    float f = m - 1.f;                                  // exact on (sqrt(1/2), sqrt(2)]
+    float s = f / (2.f + f), z = s * s;
+    float t = z * (2.f / 11.f) + 2.f / 9.f;
+    t = t * z + 2.f / 7.f;
+    t = t * z + 2.f / 5.f;
+    t = t * z + 2.f / 3.f;
+    float r = s * (z * t) + s * 2.f;                    // 2s + s^3 (2/3 + 2 s^2 / 5 + ...)
+    float fe = (float)e;
+    return (r + fe * -2.12194440e-4f) + fe * 0.693359375f;
+}
+
 // ---------------------------------------------------------------------------------------------
 // constraint projections (one colour member each; members of a colour touch disjoint nodes)
 // ---------------------------------------------------------------------------------------------
@@ -227,8 +253,10 @@ __device__ __forceinline__ TetRecord loadTet(const DeviceMesh& m, int k) {
     return t;
 }
 
-// Coupled deviatoric/hydrostatic Neo-Hookean block of one tet, k_solve_tet (xpbd_solver.cu:749-829),
-// unguarded form (hydrostatic row J - 1, no trust region).
+// Coupled deviatoric/hydrostatic Neo-Hookean block of one tet, k_solve_tet (xpbd_solver.cu:749-829).
+// Unguarded: hydrostatic row J - 1.  Guarded (tissue guard armed): row log J with a linear floor
+// below J = 0.05, its own bulk damping, and a trust region capping every corner's move at 0.15 over
+// the longest row of Dm^-1.
 __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t, const FrameCoeffs& fc) {
     int meta = t.meta;
     if ((meta & 8) == 0) return;
@@ -250,13 +278,15 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
     float CD = sqrtf(fmaxf(q, 1e-12f));
     float devScale = 1.f / CD;
     float volGrad = J > .05f ? iso * I1 / (3.f * pJ) : 0.f;
-    float CH = J - 1.f;
+    const bool guarded = fc.guarded != 0;
+    float CH = guarded ? logPositive(pJ) + fminf(0.f, (J - .05f) / .05f) : J - 1.f;
     f3 gd[4], gh[4];
 #pragma unroll
     for (int c = 1; c < 4; c++) {
         f3 b = br[c - 1];
         gh[c] = cof[0] * b.x + cof[1] * b.y + cof[2] * b.z;
         gd[c] = ((F[0] * b.x + F[1] * b.y + F[2] * b.z) * iso - gh[c] * volGrad) * devScale;
+        if (guarded) gh[c] = gh[c] * (1.f / pJ);
     }
     gd[0] = (gd[1] + gd[2] + gd[3]) * -1.f;
     gh[0] = (gh[1] + gh[2] + gh[3]) * -1.f;
@@ -270,7 +300,7 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
         vd += dot(gd[c], dx);
         vh += dot(gh[c], dx);
     }
-    float scale = 1.f + fc.dampingOverH, bulkScale = scale;
+    float scale = 1.f + fc.dampingOverH, bulkScale = guarded ? 1.f + fc.bulkDampingOverH : scale;
     float eAd = ad / scale, eAh = ah / bulkScale;
     float A = dd + eAd, Bc = dh, gamma = Bc / A;
     float schur = eAh + eAd * gamma * gamma;
@@ -281,6 +311,14 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
     if (!(A > 0.f) || !(schur > 0.f)) return;
     float dlH = fc.omega * (rh - gamma * rd) / schur, dlD = (fc.omega * rd - Bc * dlH) / A;
     if (!isfinite(dlD) || !isfinite(dlH)) return;
+    if (guarded) {
+        float largest = 0.f;
+#pragma unroll
+        for (int c = 0; c < 4; c++) largest = fmaxf(largest, len((gd[c] * dlD + gh[c] * dlH) * w[c]));
+        float limit = .15f / fmaxf(len(br[0]), fmaxf(len(br[1]), len(br[2])));
+        float accepted = largest > limit ? limit / largest : 1.f;
+        dlD *= accepted; dlH *= accepted;
+    }
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         f3 o = p[c] + (gd[c] * dlD + gh[c] * dlH) * w[c];
@@ -305,6 +343,154 @@ __device__ __forceinline__ void refreshTet(const DeviceMesh& m, int k) {
 }
 __device__ __forceinline__ float nodeInvMass(const DeviceMesh& m, int i) {
     return (m.pinned[i] != 0 || m.active[i] == 0) ? 0.f : 1.f / m.ext[i].w;
+}
+
+// ---------------------------------------------------------------------------------------------
+// tissue guard (xpbd_solver.cu:588-741), armed by LCS_SetTissueGuard with passes > 0
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void typeRows(const DeviceMesh& m, int type, f3 b[3]) {
+    const float* B = m.typeB[type];
+    b[0] = mk(B[0], B[1], B[2]); b[1] = mk(B[3], B[4], B[5]); b[2] = mk(B[6], B[7], B[8]);
+}
+
+// Tensile reinforcement of one live tet (projectTensile, xpbd_solver.cu:592-620): each of the six
+// corner-to-corner fibres carries mu V strength / 2 s^6, s = max(length / rest - 1, 0), projected
+// with finite compliance alphaDev / strength; the rest corners are the columns of (Dm^-1)^-1.
+// `pass` > 0 continues the fibres' multipliers of this substep.
+__device__ __forceinline__ void projectTensile(const DeviceMesh& m, int k, const FrameCoeffs& fc, int pass) {
+    int meta = m.tetMeta[k];
+    if ((meta & 8) == 0 || !(fc.tensileStrength > 0.f)) return;
+    int4 ids = m.tetIds[k];
+    int id[4] = {ids.x, ids.y, ids.z, ids.w};
+    float4 P[4] = {m.pos[id[0]], m.pos[id[1]], m.pos[id[2]], m.pos[id[3]]};
+    f3 p[4] = {xyz(P[0]), xyz(P[1]), xyz(P[2]), xyz(P[3])};
+    f3 b[3];
+    typeRows(m, meta & 7, b);
+    float detB = dot(b[0], cross(b[1], b[2]));
+    f3 rest[4] = {mk(0.f, 0.f, 0.f), cross(b[1], b[2]) * (1.f / detB), cross(b[2], b[0]) * (1.f / detB), cross(b[0], b[1]) * (1.f / detB)};
+    float alpha = m.tetAlpha[k].x / fmaxf(fc.tensileStrength, 1e-10f);
+    int fiber = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = i + 1; j < 4; j++, fiber++) {
+            f3 edge = p[j] - p[i];
+            float length = len(edge), restLength = len(rest[j] - rest[i]);
+            float strain = fmaxf(length / restLength - 1.f, 0.f), gradient = 3.f * strain * strain / restLength;
+            float wi = P[i].w, wj = P[j].w;
+            float lambda = pass == 0 ? 0.f : m.fiberLambda[6 * (size_t)k + fiber];
+            if (strain > 0.f && length > 0.f) {
+                float dl = (-strain * strain * strain - alpha * lambda) / ((wi + wj) * gradient * gradient + alpha);
+                f3 g = edge * (gradient / length);
+                lambda += dl;
+                p[i] = p[i] - g * (wi * dl);
+                p[j] = p[j] + g * (wj * dl);
+            }
+            if (fc.volumePasses > 1) m.fiberLambda[6 * (size_t)k + fiber] = lambda;
+        }
+#pragma unroll
+    for (int c = 0; c < 4; c++) m.pos[id[c]] = make_float4(p[c].x, p[c].y, p[c].z, P[c].w);
+}
+
+// Relative volume det(Ds) det(Dm^-1) of colour slot k at the current positions.
+__device__ __forceinline__ float tetVolume(const DeviceMesh& m, int k, int meta) {
+    int4 ids = m.tetIds[k];
+    f3 b[3];
+    typeRows(m, meta & 7, b);
+    f3 a = xyz(m.pos[ids.x]), u = xyz(m.pos[ids.y]) - a, v = xyz(m.pos[ids.z]) - a, w = xyz(m.pos[ids.w]) - a;
+    return dot(u, cross(v, w)) * dot(b[0], cross(b[1], b[2]));
+}
+
+// Linearised volume repair of one live tet below minimum + 1e-4 (k_RepairMinimumVolume).
+__device__ __forceinline__ void repairTet(const DeviceMesh& m, int k, float minimum) {
+    int meta = m.tetMeta[k];
+    if ((meta & 8) == 0) return;
+    int4 ids = m.tetIds[k];
+    int id[4] = {ids.x, ids.y, ids.z, ids.w};
+    float4 P[4] = {m.pos[id[0]], m.pos[id[1]], m.pos[id[2]], m.pos[id[3]]};
+    f3 p[4] = {xyz(P[0]), xyz(P[1]), xyz(P[2]), xyz(P[3])};
+    f3 b[3];
+    typeRows(m, meta & 7, b);
+    f3 u = p[1] - p[0], v = p[2] - p[0], w = p[3] - p[0];
+    float detB = dot(b[0], cross(b[1], b[2]));
+    float J = dot(u, cross(v, w)) * detB;
+    if (!isfinite(J) || J >= minimum + 1e-4f) return;
+    f3 g[4];
+    g[1] = cross(v, w) * detB; g[2] = cross(w, u) * detB; g[3] = cross(u, v) * detB;
+    g[0] = (g[1] + g[2] + g[3]) * -1.f;
+    float den = 0.f;
+#pragma unroll
+    for (int c = 0; c < 4; c++) den += P[c].w * dot(g[c], g[c]);
+    if (den < 1e-20f) return;
+    float dl = (minimum + 2e-4f - J) / den;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        f3 o = p[c] + g[c] * (P[c].w * dl);
+        m.pos[id[c]] = make_float4(o.x, o.y, o.z, P[c].w);
+    }
+}
+
+// Whether a live tet's motion over the substep (substep-start positions `prev` to the candidate)
+// may pass below minimum + 1e-5 (k_NeedFeasible): a conservative bound first, then the 16 corners
+// of the multi-affine volume; if so its four corners are marked.
+__device__ __forceinline__ void needFeasible(const DeviceMesh& m, int k, float minimum) {
+    int meta = m.tetMeta[k];
+    if ((meta & 8) == 0) return;
+    int4 ids = m.tetIds[k];
+    int id[4] = {ids.x, ids.y, ids.z, ids.w};
+    f3 x[4], d[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) { x[c] = xyz(m.prev[id[c]]); d[c] = xyz(m.pos[id[c]]) - x[c]; }
+    f3 b[3];
+    typeRows(m, meta & 7, b);
+    float detB = dot(b[0], cross(b[1], b[2]));
+    f3 u = x[1] - x[0], vv = x[2] - x[0], w = x[3] - x[0];
+    float r0 = len(d[0]), r1 = r0 + len(d[1]), r2 = r0 + len(d[2]), r3 = r0 + len(d[3]);
+    float bound = r1 * len(cross(vv, w)) + r2 * len(cross(w, u)) + r3 * len(cross(u, vv)) + r1 * r2 * len(w) + r1 * r3 * len(vv) +
+                  r2 * r3 * len(u) + r1 * r2 * r3;
+    if (dot(u, cross(vv, w)) * detB - bound * fabsf(detB) >= minimum + 1e-5f) return;
+    bool bad = false;
+    for (int mask = 0; mask < 16 && !bad; mask++) {
+        f3 p[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) p[c] = x[c] + d[c] * (float)((mask >> c) & 1);
+        float j = dot(p[1] - p[0], cross(p[2] - p[0], p[3] - p[0])) * detB;
+        if (!isfinite(j) || j < minimum + 1e-5f) bad = true;
+    }
+    if (bad)
+#pragma unroll
+        for (int c = 0; c < 4; c++) m.needed[id[c]] = 1;
+}
+
+// One marked vertex advances from its substep-start position towards its candidate as far as every
+// incident live tet keeps its volume above min(minimum, current) (k_FeasibleVertex); the volume is
+// linear in this vertex's displacement with the other three fixed.
+__device__ __forceinline__ void feasibleVertex(const DeviceMesh& m, int i, float minimum) {
+    if (!m.needed[i]) return;
+    float4 Pi = m.pos[i];
+    f3 delta = xyz(m.feasTarget[i]) - xyz(Pi);
+    float accepted = 1.f;
+    if (!isfinite(delta.x + delta.y + delta.z)) return;
+    for (int q = m.incOff[i]; q < m.incOff[i + 1]; q++) {
+        int k = m.incTet[q];
+        int meta = m.tetMeta[k];
+        if ((meta & 8) == 0) continue;
+        int4 ids = m.tetIds[k];
+        f3 b[3];
+        typeRows(m, meta & 7, b);
+        f3 a = xyz(m.pos[ids.x]), u = xyz(m.pos[ids.y]) - a, v = xyz(m.pos[ids.z]) - a, w = xyz(m.pos[ids.w]) - a;
+        float detB = dot(b[0], cross(b[1], b[2]));
+        float j = dot(u, cross(v, w)) * detB;
+        f3 grad[3] = {cross(v, w), cross(w, u), cross(u, v)};
+        f3 g = i == ids.x ? (grad[0] + grad[1] + grad[2]) * -1.f : i == ids.y ? grad[0] : i == ids.z ? grad[1] : grad[2];
+        float dj = dot(g, delta) * detB;
+        if (dj < 0.f) {
+            float floorV = fminf(minimum, fmaxf(0.f, j));
+            if (j + dj < floorV) accepted = fminf(accepted, fmaxf(0.f, .95f * (j - floorV) / (-dj)));
+        }
+    }
+    f3 o = xyz(Pi) + delta * accepted;
+    m.pos[i] = make_float4(o.x, o.y, o.z, Pi.w);
 }
 
 }  // namespace gbt

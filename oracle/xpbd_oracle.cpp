@@ -104,6 +104,30 @@ static inline float powMinusTwoThirds(float J) {
 }
 static inline double powMinusTwoThirds(double J) { return std::pow(J, -2.0 / 3.0); }
 
+// log x for the guarded bulk strain (x >= 0.05, a positive normal float).  FP32: x = m 2^e with
+// m in (sqrt(1/2), sqrt(2)], log m = 2 atanh(s), s = (m - 1)/(m + 1), by its odd series to s^11,
+// e ln 2 with ln 2 split into an exact head and a tail; the CUDA kernels evaluate the same sequence.
+// FP64: the library logarithm.
+static inline float logPositive(float x) {
+    uint32_t bits;
+    std::memcpy(&bits, &x, 4);
+    int e = (int)(bits >> 23) - 127;
+    bits = (bits & 0x007FFFFFu) | 0x3F800000u;
+    float m;
+    std::memcpy(&m, &bits, 4);
+    if (m > 1.41421356f) { m = m * 0.5f; e += 1; }
+    float f = m - 1.f;                                  // exact on (sqrt(1/2), sqrt(2)]
+    float s = f / (2.f + f), z = s * s;
+    float t = z * (2.f / 11.f) + 2.f / 9.f;
+    t = t * z + 2.f / 7.f;
+    t = t * z + 2.f / 5.f;
+    t = t * z + 2.f / 3.f;
+    float r = s * (z * t) + s * 2.f;                    // 2s + s^3 (2/3 + 2 s^2 / 5 + ...)
+    float fe = (float)e;
+    return (r + fe * -2.12194440e-4f) + fe * 0.693359375f;
+}
+static inline double logPositive(double x) { return std::log(x); }
+
 // ---------------------------------------------------------------------------------------------
 // session state (one process-global session, as in the reference plugin)
 // ---------------------------------------------------------------------------------------------
@@ -137,6 +161,9 @@ struct Session {
     bool frameReady = false; Real h = 0, alphaTilde = 0, velScale = 1, betaGammaHS = 0, alphaB = 0, betaGammaHB = 0;
     bool doBend = false, doStrain = false; int substepIndex = 0;
     float bulkDampingSeconds = 0.003125f, tissueHardening = 80.f; int volumePasses = 0;
+    // tissue guard (LCS_SetTissueGuard): minimum relative volume, per-node incident tets, feasibility state
+    Real minVolume = 0; std::vector<int> incOff, incTet, needed; std::vector<V3> feasTarget; std::vector<Real> fiberLambda;
+    long long guardStats[3] = {0, 0, 0};   // substeps with a candidate below the minimum; still below after repair; marked vertices
     // tool / contact (contact model 0: capsule + jaw slab CCD gate)
     bool toolArmed = false, grasping = false; XpbdToolState tool = {}, toolFrom = {};
     XpbdGraspParams gp = {0.5f, 0.3f, 0.02f, 0.55f, 0.3f, 1.0e-7f, 0.02f, 0.5f, 0.045f, 0.25f, 0.25f, 1.0e-7f, 150.f, 0.045f, 1};
@@ -188,6 +215,7 @@ static void bucket(const std::vector<int>& colour, int numColours, std::vector<i
 static void resetPhysics() {
     S.physReady = false; S.frameReady = false; S.E = S.B = S.T = 0; S.toolArmed = false; S.grasping = false;
     S.livenessStale = true; S.livenessRevision = 0xffffffffu;
+    S.volumePasses = 0; S.minVolume = 0; S.incOff.clear(); S.incTet.clear(); S.h = 0;
 }
 static void resetCut() { S.cutReady = false; S.toolSet = false; S.havePrev = false; S.cutPoints = S.revision = S.tearMarks = 0; }
 
@@ -470,12 +498,29 @@ API int LCS_SetContactModel(int enabled, float muS, float muD, float thickness, 
     S.contactModel = 0; S.grasping = false;
     return 0;
 }
+// Tissue guard (xpbd_set_tissue_guard, xpbd_solver.cu:1892-1916): minimum relative volume and the
+// number of tensile passes; passes > 0 also switches the tet projection to its guarded form and
+// arms the feasibility chain.  `inside`/`capture` select grasp-capture wedges, which the plain
+// branch never uses.
 API int LCS_SetTissueGuard(float minimum, int passes, int count, const int* inside, int capture) {
     (void)capture;
     if (!S.physReady || S.h > 0 || !std::isfinite(minimum) || minimum < 0 || minimum > .95f || passes < 0 || passes > 4 || count != S.N || !inside)
         return ERR_BAD_ARG;
-    if (passes > 0) return ERR_UNSUPPORTED;
-    S.volumePasses = 0;
+    // incident tets of every node, ascending tet index (storage order)
+    S.incOff.assign(S.N + 1, 0);
+    for (int t = 0; t < S.T; t++)
+        for (int k = 0; k < 4; k++) S.incOff[S.tIds[4 * t + k] + 1]++;
+    for (int i = 0; i < S.N; i++) S.incOff[i + 1] += S.incOff[i];
+    S.incTet.assign((size_t)4 * S.T, 0);
+    std::vector<int> cursor(S.incOff.begin(), S.incOff.end() - 1);
+    for (int t = 0; t < S.T; t++)
+        for (int k = 0; k < 4; k++) S.incTet[cursor[S.tIds[4 * t + k]]++] = t;
+    S.needed.assign(S.N, 0);
+    S.feasTarget.assign(S.N, v3(0, 0, 0));
+    S.fiberLambda.assign((size_t)6 * S.T, Real(0));
+    S.minVolume = (Real)minimum;
+    S.volumePasses = passes;
+    for (int k = 0; k < 3; k++) S.guardStats[k] = 0;
     return 0;
 }
 API int LCS_SetTissueMaterial(float strength, float bulkDamping) {
@@ -600,12 +645,15 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
     Real CD = std::sqrt(std::fmax(q, Real(1e-12)));
     Real devScale = Real(1) / CD;
     Real volGrad = J > Real(0.05) ? iso * I1 / (Real(3) * pJ) : Real(0);
-    Real CH = J - Real(1);
+    // guarded (tissue guard armed): logarithmic bulk strain with a linear floor below J = 0.05
+    const bool guarded = S.volumePasses > 0;
+    Real CH = guarded ? logPositive(pJ) + std::fmin(Real(0), (J - Real(0.05)) / Real(0.05)) : J - Real(1);
     V3 gd[4], gh[4];
     for (int k = 1; k < 4; k++) {
         V3 b = br[k - 1];
         gh[k] = cof[0] * b.x + cof[1] * b.y + cof[2] * b.z;
         gd[k] = ((F[0] * b.x + F[1] * b.y + F[2] * b.z) * iso - gh[k] * volGrad) * devScale;
+        if (guarded) gh[k] = gh[k] * (Real(1) / pJ);
     }
     gd[0] = (gd[1] + gd[2] + gd[3]) * Real(-1);
     gh[0] = (gh[1] + gh[2] + gh[3]) * Real(-1);
@@ -616,8 +664,8 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
         V3 dx = p[k] - S.prev[id[k]];
         vd += dot(gd[k], dx); vh += dot(gh[k], dx);
     }
-    (void)hh; (void)bulkDampingOverH;
-    Real scale = Real(1) + dampingOverH, bulkScale = scale;
+    (void)hh;
+    Real scale = Real(1) + dampingOverH, bulkScale = guarded ? Real(1) + bulkDampingOverH : scale;
     Real eAd = ad / scale, eAh = ah / bulkScale;
     Real A = dd + eAd, Bc = dh, gamma = Bc / A;
     Real schur = eAh + eAd * gamma * gamma;
@@ -627,7 +675,166 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
     if (!(A > 0) || !(schur > 0)) return;
     Real dlH = S.omega * (rh - gamma * rd) / schur, dlD = (S.omega * rd - Bc * dlH) / A;
     if (!isFin(dlD) || !isFin(dlH)) return;
+    if (guarded) {   // trust region on the update: no corner moves more than 0.15 of the shortest rest edge scale
+        Real largest = 0;
+        for (int k = 0; k < 4; k++) largest = std::fmax(largest, len((gd[k] * dlD + gh[k] * dlH) * w[k]));
+        Real limit = Real(0.15) / std::fmax(len(br[0]), std::fmax(len(br[1]), len(br[2])));
+        Real accepted = largest > limit ? limit / largest : Real(1);
+        dlD *= accepted; dlH *= accepted;
+    }
     for (int k = 0; k < 4; k++) S.pos[id[k]] = p[k] + (gd[k] * dlD + gh[k] * dlH) * w[k];
+}
+
+// Tensile reinforcement of one live tet (projectTensile, xpbd_solver.cu:592-620): each of the six
+// corner-to-corner fibres carries the energy mu V strength / 2 s^6, s = max(length / rest - 1, 0),
+// projected with finite compliance alphaDev / strength; the rest corners are the columns of the
+// inverse of the rest matrix Dm^-1.  `pass` > 0 continues the fibres' multipliers of this substep.
+static void projectTensile(int e, int pass) {
+    if (!S.tActive[e]) return;
+    const Real strength = (Real)S.tissueHardening;
+    if (!(strength > 0)) return;
+    const int* id = &S.tIds[4 * e];
+    V3 p[4] = {S.pos[id[0]], S.pos[id[1]], S.pos[id[2]], S.pos[id[3]]};
+    const Real(*Bm)[3] = S.typeB[S.tType[e]];
+    V3 b[3] = {v3(Bm[0][0], Bm[0][1], Bm[0][2]), v3(Bm[1][0], Bm[1][1], Bm[1][2]), v3(Bm[2][0], Bm[2][1], Bm[2][2])};
+    Real detB = dot(b[0], cross(b[1], b[2]));
+    V3 rest[4] = {v3(0, 0, 0), cross(b[1], b[2]) * (Real(1) / detB), cross(b[2], b[0]) * (Real(1) / detB), cross(b[0], b[1]) * (Real(1) / detB)};
+    int fiber = 0;
+    for (int i = 0; i < 4; i++)
+        for (int k = i + 1; k < 4; k++, fiber++) {
+            V3 edge = p[k] - p[i];
+            Real length = len(edge), restLength = len(rest[k] - rest[i]);
+            Real strain = std::fmax(length / restLength - Real(1), Real(0)), gradient = Real(3) * strain * strain / restLength;
+            Real wi = S.invMass[id[i]], wk = S.invMass[id[k]], alpha = S.aDev[e] / std::fmax(strength, Real(1e-10));
+            Real& lambda = S.fiberLambda[6 * (size_t)e + fiber];
+            if (pass == 0) lambda = 0;
+            if (strain > 0 && length > 0) {
+                Real dl = (-strain * strain * strain - alpha * lambda) / ((wi + wk) * gradient * gradient + alpha);
+                V3 g = edge * (gradient / length);
+                lambda += dl;
+                p[i] = p[i] - g * (wi * dl);
+                p[k] = p[k] + g * (wk * dl);
+            }
+        }
+    for (int k = 0; k < 4; k++) S.pos[id[k]] = p[k];
+}
+
+// Relative volume det(Ds) det(Dm^-1) of a tet from the given positions (storage order).
+static Real tetVolume(int t, const std::vector<V3>& x) {
+    const int* id = &S.tIds[4 * t];
+    const Real(*Bm)[3] = S.typeB[S.tType[t]];
+    V3 b0 = v3(Bm[0][0], Bm[0][1], Bm[0][2]), b1 = v3(Bm[1][0], Bm[1][1], Bm[1][2]), b2 = v3(Bm[2][0], Bm[2][1], Bm[2][2]);
+    V3 a = x[id[0]], u = x[id[1]] - a, v = x[id[2]] - a, w = x[id[3]] - a;
+    return dot(u, cross(v, w)) * dot(b0, cross(b1, b2));
+}
+
+// The feasibility chain of a guarded substep (finishFeasible, xpbd_solver.cu:628-741), after contact:
+// if a live tet is below the minimum relative volume, two colour sweeps of a linearised volume repair;
+// if one still is, every vertex of a tet whose motion over the substep may pass below the minimum
+// (a conservative bound, then the 16 corners of the multi-affine volume) restarts from its
+// substep-start position and advances along its candidate displacement as far as every incident
+// live tet allows, in eight lattice-parity colours whose order rotates with the substep.
+static void finishFeasible(int substepIndex) {
+    const Real minimum = S.minVolume;
+    bool unsafe = false;
+    for (int t = 0; t < S.T && !unsafe; t++) {
+        if (!S.tActive[t]) continue;
+        Real J = tetVolume(t, S.pos);
+        if (!isFin(J) || J < minimum) unsafe = true;
+    }
+    if (!unsafe) return;
+    S.guardStats[0]++;
+    for (int pass = 0; pass < 2; pass++)
+        for (size_t c = 0; c < S.tColCnt.size(); c++) {
+            int off = S.tColOff[c], cnt = S.tColCnt[c];
+#pragma omp parallel for schedule(static)
+            for (int k = 0; k < cnt; k++) {
+                int t = S.tColorOrder[off + k];
+                if (!S.tActive[t]) continue;
+                const int* id = &S.tIds[4 * t];
+                const Real(*Bm)[3] = S.typeB[S.tType[t]];
+                V3 b0 = v3(Bm[0][0], Bm[0][1], Bm[0][2]), b1 = v3(Bm[1][0], Bm[1][1], Bm[1][2]), b2 = v3(Bm[2][0], Bm[2][1], Bm[2][2]);
+                V3 p[4] = {S.pos[id[0]], S.pos[id[1]], S.pos[id[2]], S.pos[id[3]]};
+                V3 u = p[1] - p[0], v = p[2] - p[0], w = p[3] - p[0];
+                Real detB = dot(b0, cross(b1, b2));
+                Real J = dot(u, cross(v, w)) * detB;
+                if (!isFin(J) || J >= minimum + Real(1e-4)) continue;
+                V3 g[4];
+                g[1] = cross(v, w) * detB; g[2] = cross(w, u) * detB; g[3] = cross(u, v) * detB;
+                g[0] = (g[1] + g[2] + g[3]) * Real(-1);
+                Real den = 0;
+                for (int n = 0; n < 4; n++) den += S.invMass[id[n]] * dot(g[n], g[n]);
+                if (den < Real(1e-20)) continue;
+                Real dl = (minimum + Real(2e-4) - J) / den;
+                for (int n = 0; n < 4; n++) S.pos[id[n]] = p[n] + g[n] * (S.invMass[id[n]] * dl);
+            }
+        }
+    unsafe = false;
+    for (int t = 0; t < S.T && !unsafe; t++) {
+        if (!S.tActive[t]) continue;
+        Real J = tetVolume(t, S.pos);
+        if (!isFin(J) || J < minimum) unsafe = true;
+    }
+    if (!unsafe) return;
+    S.guardStats[1]++;
+    std::fill(S.needed.begin(), S.needed.end(), 0);
+    for (int t = 0; t < S.T; t++) {
+        if (!S.tActive[t]) continue;
+        const int* id = &S.tIds[4 * t];
+        const Real(*Bm)[3] = S.typeB[S.tType[t]];
+        V3 b0 = v3(Bm[0][0], Bm[0][1], Bm[0][2]), b1 = v3(Bm[1][0], Bm[1][1], Bm[1][2]), b2 = v3(Bm[2][0], Bm[2][1], Bm[2][2]);
+        V3 x[4], d[4];
+        for (int k = 0; k < 4; k++) { x[k] = S.prev[id[k]]; d[k] = S.pos[id[k]] - x[k]; }
+        Real detB = dot(b0, cross(b1, b2));
+        V3 u = x[1] - x[0], vv = x[2] - x[0], w = x[3] - x[0];
+        Real r0 = len(d[0]), r1 = r0 + len(d[1]), r2 = r0 + len(d[2]), r3 = r0 + len(d[3]);
+        Real bound = r1 * len(cross(vv, w)) + r2 * len(cross(w, u)) + r3 * len(cross(u, vv)) + r1 * r2 * len(w) + r1 * r3 * len(vv) +
+                     r2 * r3 * len(u) + r1 * r2 * r3;
+        if (dot(u, cross(vv, w)) * detB - bound * std::fabs(detB) >= minimum + Real(1e-5)) continue;
+        bool bad = false;
+        for (int mask = 0; mask < 16 && !bad; mask++) {
+            V3 p[4];
+            for (int k = 0; k < 4; k++) p[k] = x[k] + d[k] * (Real)((mask >> k) & 1);
+            Real j = dot(p[1] - p[0], cross(p[2] - p[0], p[3] - p[0])) * detB;
+            if (!isFin(j) || j < minimum + Real(1e-5)) bad = true;
+        }
+        if (bad)
+            for (int k = 0; k < 4; k++) S.needed[id[k]] = 1;
+    }
+    for (int i = 0; i < S.N; i++)
+        if (S.needed[i]) { S.feasTarget[i] = S.pos[i]; S.pos[i] = S.prev[i]; S.guardStats[2]++; }
+    const int nx = S.dx + 1, ny = S.dy + 1, nz = S.dz + 1, phase = substepIndex & 7;
+    for (int k = 0; k < 8; k++) {
+        int color = (k + phase) & 7;
+#pragma omp parallel for schedule(static)
+        for (int z = (color >> 2) & 1; z < nz; z += 2)
+            for (int y = (color >> 1) & 1; y < ny; y += 2)
+                for (int x0 = color & 1; x0 < nx; x0 += 2) {
+                    int i = x0 + nx * (y + ny * z);
+                    if (!S.needed[i]) continue;
+                    V3 delta = S.feasTarget[i] - S.pos[i];
+                    Real accepted = 1;
+                    if (!isFin(delta.x + delta.y + delta.z)) continue;
+                    for (int q = S.incOff[i]; q < S.incOff[i + 1]; q++) {
+                        int t = S.incTet[q];
+                        if (!S.tActive[t]) continue;
+                        const int* id = &S.tIds[4 * t];
+                        const Real(*Bm)[3] = S.typeB[S.tType[t]];
+                        V3 b0 = v3(Bm[0][0], Bm[0][1], Bm[0][2]), b1 = v3(Bm[1][0], Bm[1][1], Bm[1][2]), b2 = v3(Bm[2][0], Bm[2][1], Bm[2][2]);
+                        V3 a = S.pos[id[0]], u = S.pos[id[1]] - a, v = S.pos[id[2]] - a, w = S.pos[id[3]] - a;
+                        Real detB = dot(b0, cross(b1, b2));
+                        Real j = dot(u, cross(v, w)) * detB;
+                        V3 grad[3] = {cross(v, w), cross(w, u), cross(u, v)};
+                        V3 g = i == id[0] ? (grad[0] + grad[1] + grad[2]) * Real(-1) : i == id[1] ? grad[0] : i == id[2] ? grad[1] : grad[2];
+                        Real dj = dot(g, delta) * detB;
+                        if (dj < 0) {
+                            Real floor = std::fmin(minimum, std::fmax(Real(0), j));
+                            if (j + dj < floor) accepted = std::fmin(accepted, std::fmax(Real(0), Real(0.95) * (j - floor) / (-dj)));
+                        }
+                    }
+                    S.pos[i] = S.pos[i] + delta * accepted;
+                }
+    }
 }
 
 static V3 lerpF(const F3& a, const F3& b, Real t) { return fromF(a) * (Real(1) - t) + fromF(b) * t; }
@@ -721,6 +928,12 @@ static int substep() {
 #pragma omp parallel for schedule(static)
             for (int k = 0; k < cnt; k++) projectTet(S.tColorOrder[off + k], dOH, bOH);
         }
+        for (int pass = 0; pass < S.volumePasses; pass++)   // tensile reinforcement (solveTetGraph, xpbd_solver.cu:2531-2533)
+            for (size_t c = 0; c < S.tColCnt.size(); c++) {
+                int off = S.tColOff[c], cnt = S.tColCnt[c];
+#pragma omp parallel for schedule(static)
+                for (int k = 0; k < cnt; k++) projectTensile(S.tColorOrder[off + k], pass);
+            }
     }
     if (S.toolArmed && S.contactModel == 0) {
         std::fill(S.jawLambda.begin(), S.jawLambda.end(), Real(0));
@@ -740,6 +953,7 @@ static int substep() {
         Real gapHalf = Real(0.5) * std::fmax(gap, (Real)S.gp.jawGapClosed);
         solveContact(sa, sb, st.shaftR, hinge, axis, normal, w, st.jawLen, st.jawHalfWidth, gapHalf, (Real)S.gp.contactAlpha / (h * h));
     }
+    if (S.volumePasses > 0 && S.T > 0) finishFeasible(S.substepIndex);
     Real invH = Real(1) / h;
 #pragma omp parallel for schedule(static)
     for (int p = 0; p < S.N; p++) S.vel[p] = S.invMass[p] > 0 ? (S.pos[p] - S.prev[p]) * invH : v3(0, 0, 0);
@@ -1057,6 +1271,13 @@ API int LCS_ProfileRead(int steps, float* ms) {
     return 0;
 }
 API void LCS_Shutdown() { resetCut(); resetPhysics(); S.reconReady = false; }
+API double ORC_LogPositive(double x) { return (double)logPositive((Real)x); }   // the guarded bulk strain's log
+API double ORC_PowMinusTwoThirds(double x) { return (double)powMinusTwoThirds((Real)x); }
+API int ORC_GuardStats(long long* out3) {   // feasibility chain activity since the guard was armed
+    if (!out3) return ERR_BAD_ARG;
+    for (int k = 0; k < 3; k++) out3[k] = S.guardStats[k];
+    return 0;
+}
 API int ORC_Threads() {
 #ifdef _OPENMP
     return omp_get_max_threads();

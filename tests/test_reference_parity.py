@@ -15,7 +15,7 @@ import pytest
 
 from genesis_tissue_simulation_gb300 import workloads as W
 from genesis_tissue_simulation_gb300.grid import build_grid
-from genesis_tissue_simulation_gb300.native_backend import PlainTissue, GraspParams
+from genesis_tissue_simulation_gb300.native_backend import Capsule, PlainTissue, GraspParams
 
 pytestmark = pytest.mark.gpu
 from conftest import results_dir
@@ -24,13 +24,18 @@ OUT = results_dir()
 SMALL = (4.78, 2.38, 3.98)
 
 
-def run(lib, grid, steps, reference, ks=1e6, substeps=10, capsule=None, blades=None, record=(1, 2, 5, 10, 20)):
+def run(lib, grid, steps, reference, ks=1e6, substeps=10, capsule=None, blades=None, record=(1, 2, 5, 10, 20), guard=None):
     s = PlainTissue(grid, dt=1 / 60, substeps=substeps, ks=ks, young_pa=6000.0, poisson=0.25, strain_damping_s=0.04,
                     dll_path=lib, reference=reference,
                     grasp_params=GraspParams(**dict(W.DEFAULT_GRASP, ccd_velocity=0.0)) if capsule else None)
     out = {}
     try:
         s.set_gravity(0.0, -981.0, 0.0)
+        if guard:   # the reference adapter's guard: minimum relative volume, passes; strength 80, bulk damping 0.01 s
+            import ctypes
+            from genesis_tissue_simulation_gb300.native_backend import pointer
+            s.check("LCS_SetTissueGuard", ctypes.c_float(guard[0]), guard[1], len(grid.positions), pointer(grid.inside), 1)
+            s.check("LCS_SetTissueMaterial", ctypes.c_float(80.0), ctypes.c_float(0.01))
         if capsule:
             s.set_capsule(capsule[0])
         for k in range(steps):
@@ -113,3 +118,18 @@ def test_tall_block_sag_matches_reference(reference_lib, oracle_libs):
     with open(OUT / "reference_parity.jsonl", "a") as f:
         f.write(json.dumps({"case": "tall_block_sag", "reference": sag[0], "oracle": sag[1]}) + "\n")
     assert abs(sag[0] - sag[1]) <= 0.05 * abs(sag[0]) + 1e-3
+
+
+@pytest.mark.parametrize("minimum,passes", [(0.15, 1), (0.9, 1)])
+def test_guarded_step_matches_reference(reference_lib, oracle_libs, minimum, passes):
+    """The tissue guard chain (guarded tet form, tensile passes, feasibility chain) against the
+    reference's own: a capsule pressed into the C1 block; at minimum 0.9 the repair and the vertex
+    line search run in most substeps."""
+    grid = build_grid(0.2, size=(3.18, 1.58, 3.18), density=1000.0)
+    top = float(grid.positions[grid.active != 0, 1].max())
+    caps = [Capsule((-1.0, top + 0.25 - 0.6 * k / 10, 0.0), (1.0, top + 0.25 - 0.6 * k / 10, 0.2), 0.25) for k in range(11)]
+    cap = (caps[0], caps[1:])
+    ref = run(reference_lib, grid, 10, True, capsule=cap, record=(1, 2, 5, 10), guard=(minimum, passes))
+    orc = run(oracle_libs[0], grid, 10, False, capsule=cap, record=(1, 2, 5, 10), guard=(minimum, passes))
+    rows = report(f"c1_guard_min{minimum:g}_passes{passes}", grid, ref, orc)
+    assert rows[1] <= 1e-4
