@@ -11,6 +11,7 @@
 // no barrier between them.
 #include "tissue_device.cuh"
 #include "grid_sync.cuh"
+#include "friction_contact.cuh"
 #include "frame_kernels.h"
 
 namespace gbt {
@@ -259,6 +260,15 @@ __device__ bool guardFeasible(const DeviceMesh& m, const FrameCoeffs& fc, int su
     return true;
 }
 
+// Contact model 1 over this thread's nodes: every node against the shaft capsule and both jaw
+// boxes (kept out of line so its shapes do not enlarge the frame kernel's register allocation).
+__device__ __noinline__ void frictionPhase(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
+                                           const ContactParams& cp, float t, int r, int R) {
+    const float previousT = fmaxf(0.f, t - 1.f / (float)fc.numSubsteps);
+    const FrictionShapes fs = frictionShapes(from, to, t, previousT, fc.jawThickness, cp.jawGapClosed);
+    for (int i = m.nodeBase + r; i < m.nodeBase + m.nNodes; i += R) frictionNode(m, i, fs, fc.contactRadius, fc.contactAlphaH2, fc.muS, fc.muD);
+}
+
 // ---------------------------------------------------------------------------------------------
 // frame driver
 // ---------------------------------------------------------------------------------------------
@@ -369,6 +379,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         float t = fminf(1.f, (float)(fc.firstSubstep + s + 1) / (float)fc.numSubsteps);
         ContactFrame cf;
         if (fc.contact && !m.nodeInstance) cf = contactFrame(from, to, t, cp, fc.contactAlphaH2);
+        if (fc.friction) frictionPhase(m, fc, from, to, cp, t, r, R);   // contact model 1
         if (fc.guarded) {   // contact, then the feasibility chain, then the velocity update
             if (fc.contact)
                 for (int i = m.nodeBase + r; i < nodeEnd; i += R) contactNode(m, i, cf, cp);

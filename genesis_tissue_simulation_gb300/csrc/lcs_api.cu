@@ -81,6 +81,7 @@ struct Session {
     ContactParams cp{0.02f, 1.0e-7f, 0.5f, 0.045f, 0.25f};
     GraspParamsAbi gp{0.5f, 0.3f, 0.02f, 0.55f, 0.3f, 1.0e-7f, 0.02f, 0.5f, 0.045f, 0.25f, 0.25f, 1.0e-7f, 150.f, 0.045f, 1};
     int contactModel = 0;
+    float muStatic = 0.f, muDynamic = 0.f, jawThickness = 0.f, contactRadius = 0.f;   // contact model 1
     // cut
     CutInitDesc cd{};
     DBuf<int4> gridEdges; DBuf<unsigned> occupied, cutMask, counters; DBuf<int> inside; DBuf<float> skinTD, edgeCutT;
@@ -373,8 +374,9 @@ LCS_API int LCS_SetContactModel(int enabled, float muS, float muD, float thickne
     if (!S.physReady) return XPBD_ERR_NOT_READY;
     if (enabled < 0 || enabled > 2 || !std::isfinite(muS) || !std::isfinite(muD) || !std::isfinite(thickness) || !std::isfinite(radius) ||
         muS < 0 || muD < 0 || muD > muS || thickness <= 0 || radius < 0) return XPBD_ERR_BAD_ARG;
-    if (enabled != 0) return LCS_ERR_UNSUPPORTED;
-    S.contactModel = 0;
+    if (enabled == 2) return LCS_ERR_UNSUPPORTED;   // anchor assist belongs to the unified grasp solver
+    S.contactModel = enabled;
+    S.muStatic = muS; S.muDynamic = muD; S.jawThickness = thickness; S.contactRadius = radius;
     return 0;
 }
 LCS_API int LCS_SetTissueGuard(float minimum, int passes, int count, const int* inside, int capture) {
@@ -507,6 +509,8 @@ LCS_API int LCS_Step(float dt) {
     fc.bulkDampingOverH = S.bulkDampingSeconds / h;
     fc.minVolume = S.minVolume;
     fc.contact = (S.toolArmed && S.contactModel == 0) ? 1 : 0;
+    fc.friction = (S.toolArmed && S.contactModel == 1) ? 1 : 0;
+    fc.muS = S.muStatic; fc.muD = S.muDynamic; fc.jawThickness = S.jawThickness; fc.contactRadius = S.contactRadius;
     fc.contactAlphaH2 = S.cp.contactAlpha / (h * h);
     fc.cut = (S.cutReady && S.toolSet && !S.pressure) ? 1 : 0;
     fc.spinBudget = (long long)((double)S.syncBudgetSeconds * 1e3 * S.clockKHz);
@@ -727,6 +731,8 @@ LCS_API int LCS_StepNoAlloc(float dt) {
     fc.bulkDampingOverH = S.bulkDampingSeconds / h;
     fc.minVolume = S.minVolume;
     fc.contact = (S.toolArmed && S.contactModel == 0) ? 1 : 0;
+    fc.friction = (S.toolArmed && S.contactModel == 1) ? 1 : 0;
+    fc.muS = S.muStatic; fc.muD = S.muDynamic; fc.jawThickness = S.jawThickness; fc.contactRadius = S.contactRadius;
     fc.contactAlphaH2 = S.cp.contactAlpha / (h * h);
     fc.cut = (S.cutReady && S.toolSet && !S.pressure) ? 1 : 0;
     fc.spinBudget = (long long)((double)S.syncBudgetSeconds * 1e3 * S.clockKHz);

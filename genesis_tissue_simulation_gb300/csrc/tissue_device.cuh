@@ -63,6 +63,8 @@ struct FrameCoeffs {
     float omega, dampingOverH, fallbackInvEh2, contactAlphaH2;
     int guarded, volumePasses;       // tissue guard: guarded tet form, tensile passes, feasibility chain
     float tensileStrength, bulkDampingOverH, minVolume;
+    int friction;                    // contact model 1: tool SDFs, swept contact, Coulomb friction
+    float muS, muD, jawThickness, contactRadius;
     long long spinBudget;            // grid-barrier spin budget, SM clock cycles
     int syncTestExtra;               // > 0: barriers await arrivals that never come (timeout test)
     int stageNodes;                  // one-CTA kernel: node state staged in shared memory

@@ -168,6 +168,7 @@ struct Session {
     bool toolArmed = false, grasping = false; XpbdToolState tool = {}, toolFrom = {};
     XpbdGraspParams gp = {0.5f, 0.3f, 0.02f, 0.55f, 0.3f, 1.0e-7f, 0.02f, 0.5f, 0.045f, 0.25f, 0.25f, 1.0e-7f, 150.f, 0.045f, 1};
     int contactModel = 0;
+    Real muStatic = 0, muDynamic = 0, jawThickness = 0, contactRadius = 0;   // contact model 1 (LCS_SetContactModel)
     std::vector<Real> jawLambda, shaftLambda;
     // cut
     bool cutReady = false; CutInitDesc cd = {}; std::vector<GridEdge2> gridEdges; std::vector<unsigned> occupied, cutMask;
@@ -494,8 +495,9 @@ API int LCS_SetContactModel(int enabled, float muS, float muD, float thickness, 
     if (!S.physReady) return ERR_NOT_READY;
     if (enabled < 0 || enabled > 2 || !std::isfinite(muS) || !std::isfinite(muD) || !std::isfinite(thickness) || !std::isfinite(radius) ||
         muS < 0 || muD < 0 || muD > muS || thickness <= 0 || radius < 0) return ERR_BAD_ARG;
-    if (enabled != 0) return ERR_UNSUPPORTED;     // friction/surface contact needs the reconstructed surface
-    S.contactModel = 0; S.grasping = false;
+    if (enabled == 2) return ERR_UNSUPPORTED;     // anchor assist belongs to the unified grasp solver
+    S.contactModel = enabled; S.grasping = false;
+    S.muStatic = muS; S.muDynamic = muD; S.jawThickness = thickness; S.contactRadius = radius;
     return 0;
 }
 // Tissue guard (xpbd_set_tissue_guard, xpbd_solver.cu:1892-1916): minimum relative volume and the
@@ -887,6 +889,8 @@ static void solveContact(const V3& shaftA, const V3& shaftB, Real shaftR, const 
     }
 }
 
+#include "friction_oracle.inc"
+
 static int substep() {
     if (!S.physReady) return ERR_NOT_READY;
     if (!S.frameReady) return ERR_NO_FRAME;
@@ -953,6 +957,7 @@ static int substep() {
         Real gapHalf = Real(0.5) * std::fmax(gap, (Real)S.gp.jawGapClosed);
         solveContact(sa, sb, st.shaftR, hinge, axis, normal, w, st.jawLen, st.jawHalfWidth, gapHalf, (Real)S.gp.contactAlpha / (h * h));
     }
+    if (S.toolArmed && S.contactModel == 1) frictionContact(t);   // contact model 1, no surface (xpbd_solver.cu:3655-3665)
     if (S.volumePasses > 0 && S.T > 0) finishFeasible(S.substepIndex);
     Real invH = Real(1) / h;
 #pragma omp parallel for schedule(static)

@@ -133,3 +133,18 @@ def test_guarded_step_matches_reference(reference_lib, oracle_libs, minimum, pas
     orc = run(oracle_libs[0], grid, 10, False, capsule=cap, record=(1, 2, 5, 10), guard=(minimum, passes))
     rows = report(f"c1_guard_min{minimum:g}_passes{passes}", grid, ref, orc)
     assert rows[1] <= 1e-4
+
+
+@pytest.mark.parametrize("closing", [False, True])
+def test_friction_contact_matches_reference(reference_lib, oracle_libs, closing):
+    """Contact model 1 without a surface (shaft capsule + jaw boxes, swept contact, Coulomb
+    friction) against the reference's own kernels."""
+    from test_friction_contact import friction_run
+    grid, ref = friction_run(reference_lib, closing=closing, reference=True)
+    _, orc = friction_run(oracle_libs[0], closing=closing)
+    active = grid.active != 0
+    diag = W.bbox_diagonal(grid)
+    rows = {k + 1: float(np.abs(ref[k] - orc[k])[active].max()) / diag for k in (0, 1, 4, 9)}
+    with open(OUT / "reference_parity.jsonl", "a") as f:
+        f.write(json.dumps({"case": f"c1_friction_contact_closing{int(closing)}", "err_over_diag": rows}) + "\n")
+    assert rows[1] <= 1e-4
