@@ -272,10 +272,13 @@ __device__ __noinline__ void frictionPhase(const DeviceMesh& m, const FrameCoeff
 // ---------------------------------------------------------------------------------------------
 // frame driver
 // ---------------------------------------------------------------------------------------------
-template <class Sync>
+// Extended: the tissue guard and contact model 1 are compiled in.  Kernels without them keep the
+// plain path's register allocation (the extended kernel launches only when either is armed).
+template <class Sync, bool Extended>
 __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
                          const ContactParams& cp, const CutParams& cu, unsigned* state, Sync& sync) {
     const int r = sync.rank(), R = sync.size();
+    const bool guarded = Extended && fc.guarded != 0;
     // state[0]: topology revision the liveness flags were derived at (~0u: never)
     unsigned derivedAt = *(volatile unsigned*)state;
     bool havePrev = cu.havePrev != 0;
@@ -361,12 +364,12 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 int2 nrg = c + 1 < m.nTetColors ? m.tetRange[c + 1] : make_int2(0, 0);
                 hasNext = nrg.x + r < nrg.y;
                 if (hasNext) next = loadTet(m, nrg.x + r);
-                if (hasCur) applyTet(m, cur, fc);
-                for (int k = rg.x + r + R; k < rg.y; k += R) projectTet(m, k, fc);
+                if (hasCur) applyTet(m, cur, fc, guarded);
+                for (int k = rg.x + r + R; k < rg.y; k += R) projectTet(m, k, fc, guarded);
                 if (!sync.sync()) return;
                 mark(s, kPhaseTets);
             }
-            if (fc.guarded)   // tensile reinforcement after the tet colours (xpbd_solver.cu:2531-2533)
+            if (guarded)   // tensile reinforcement after the tet colours (xpbd_solver.cu:2531-2533)
                 for (int pass = 0; pass < fc.volumePasses; pass++)
                     for (int c = 0; c < m.nTetColors; c++) {
                         int2 rg = m.tetRange[c];
@@ -379,14 +382,14 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         float t = fminf(1.f, (float)(fc.firstSubstep + s + 1) / (float)fc.numSubsteps);
         ContactFrame cf;
         if (fc.contact && !m.nodeInstance) cf = contactFrame(from, to, t, cp, fc.contactAlphaH2);
-        if (fc.friction) frictionPhase(m, fc, from, to, cp, t, r, R);   // contact model 1
-        if (fc.guarded) {   // contact, then the feasibility chain, then the velocity update
+        if (Extended && fc.friction) frictionPhase(m, fc, from, to, cp, t, r, R);   // contact model 1
+        if (guarded) {   // contact, then the feasibility chain, then the velocity update
             if (fc.contact)
                 for (int i = m.nodeBase + r; i < nodeEnd; i += R) contactNode(m, i, cf, cp);
             if (!guardFeasible(m, fc, fc.firstSubstep + s + 1, sync)) return;
         }
         for (int i = m.nodeBase + r; i < nodeEnd; i += R) {
-            if (fc.contact && !fc.guarded) {
+            if (fc.contact && !guarded) {
                 if (m.nodeInstance) {   // batched instances: each node meets its own instance's tool
                     const ContactFrame& own = m.contactFrames[(size_t)(fc.firstSubstep + s) * m.nInstances + m.nodeInstance[i]];
                     contactNode(m, i, own, cp);
@@ -456,7 +459,7 @@ __device__ __forceinline__ void runInstances(const DeviceMesh& m, const FrameCoe
         v.edgeRange = it.edgeRange + (size_t)i * m.nEdgeColors;
         v.bendRange = it.bendRange + (size_t)i * m.nBendColors;
         v.tetRange = it.tetRange + (size_t)i * m.nTetColors;
-        runFrame(v, fc, none, none, cp, noCut, it.derived + i, b);
+        runFrame<BlockSync, false>(v, fc, none, none, cp, noCut, it.derived + i, b);
         __syncthreads();
     }
 }
@@ -467,21 +470,31 @@ __global__ void __launch_bounds__(512) frameKernelInstances512(DeviceMesh m, Fra
     runInstances(m, fc, cp, it);
 }
 
+template <bool Extended>
+__device__ __forceinline__ void gridFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
+                                          const ContactParams& cp, const CutParams& cu, unsigned* state) {
+    GridSync g{state + 1, state + 2, gridDim.x, 0u, fc.spinBudget, (unsigned)fc.syncTestExtra};
+    runFrame<GridSync, Extended>(m, fc, from, to, cp, cu, state, g);
+}
 __global__ void __launch_bounds__(kFrameThreads) frameKernelGrid(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                   ContactParams cp, CutParams cu, unsigned* state) {
-    GridSync g{state + 1, state + 2, gridDim.x, 0u, fc.spinBudget, (unsigned)fc.syncTestExtra};
-    runFrame(m, fc, from, to, cp, cu, state, g);
+    gridFrame<false>(m, fc, from, to, cp, cu, state);
+}
+__global__ void __launch_bounds__(kFrameThreads) frameKernelGridExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
+                                                                     ContactParams cp, CutParams cu, unsigned* state) {
+    gridFrame<true>(m, fc, from, to, cp, cu, state);
 }
 
 // One CTA per mesh.  When fc.stageNodes is set the whole node state (positions and substep-start
 // positions, 32 B per node) is copied into shared memory for the frame, so every gather of every
 // colour is a shared-memory access; it is written back when the frame ends.
-__global__ void __launch_bounds__(kBlockThreads) frameKernelBlock(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
-                                                                   ContactParams cp, CutParams cu, unsigned* state) {
+template <bool Extended>
+__device__ __forceinline__ void blockFrame(DeviceMesh m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
+                                           const ContactParams& cp, const CutParams& cu, unsigned* state) {
     extern __shared__ float4 staged[];
     BlockSync b{state + 2};
     if (!fc.stageNodes) {
-        runFrame(m, fc, from, to, cp, cu, state, b);
+        runFrame<BlockSync, Extended>(m, fc, from, to, cp, cu, state, b);
         return;
     }
     float4* sPos = staged;
@@ -492,9 +505,17 @@ __global__ void __launch_bounds__(kBlockThreads) frameKernelBlock(DeviceMesh m, 
     float4* gPrev = m.prev;
     m.pos = sPos;
     m.prev = sPrev;
-    runFrame(m, fc, from, to, cp, cu, state, b);
+    runFrame<BlockSync, Extended>(m, fc, from, to, cp, cu, state, b);
     __syncthreads();
     for (int i = threadIdx.x; i < m.nNodes; i += blockDim.x) { gPos[i] = sPos[i]; gPrev[i] = sPrev[i]; }
+}
+__global__ void __launch_bounds__(kBlockThreads) frameKernelBlock(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
+                                                                   ContactParams cp, CutParams cu, unsigned* state) {
+    blockFrame<false>(m, fc, from, to, cp, cu, state);
+}
+__global__ void __launch_bounds__(kBlockThreads) frameKernelBlockExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
+                                                                      ContactParams cp, CutParams cu, unsigned* state) {
+    blockFrame<true>(m, fc, from, to, cp, cu, state);
 }
 
 // Per-tet compliance of the frame, k_ComputeTetAlpha (xpbd_solver.cu:578-587).

@@ -11,6 +11,11 @@ __global__ void frameKernelGrid(DeviceMesh m, FrameCoeffs fc, ToolPose from, Too
                                 unsigned* state);
 __global__ void frameKernelBlock(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to, ContactParams cp, CutParams cu,
                                  unsigned* state);
+// the same frames with the tissue guard and contact model 1 compiled in
+__global__ void frameKernelGridExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to, ContactParams cp, CutParams cu,
+                                unsigned* state);
+__global__ void frameKernelBlockExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to, ContactParams cp, CutParams cu,
+                                 unsigned* state);
 // Per-instance view of a packed batch: node range and colour ranges of every instance, and the
 // work list of each CTA of frameKernelInstances.
 struct InstanceTable {

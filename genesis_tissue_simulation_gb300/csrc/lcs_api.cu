@@ -45,7 +45,7 @@ template <class T> struct DBuf {
 
 struct Session {
     cudaStream_t stream = nullptr;
-    int device = 0, smCount = 0, gridBlocks = 0;
+    int device = 0, smCount = 0, gridBlocks = 0, gridBlocksExt = 0;   // cooperative CTAs: plain / extended frame kernel
     bool reconReady = false, physReady = false, cutReady = false;
     int N = 0, dx = 0, dy = 0, dz = 0;
     std::vector<float> hostRest;            // rest lattice (3N), the first corner positions uploaded
@@ -130,15 +130,18 @@ int ensureStream() {
     CK(cudaDeviceGetAttribute(&S.smCount, cudaDevAttrMultiProcessorCount, S.device));
     CK(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
     CK(cudaMallocHost(&S.hostState, 8 * sizeof(unsigned)));
-    int perSm = 0;
+    int perSm = 0, perSmExt = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, frameKernelGrid, kFrameThreads, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSmExt, frameKernelGridExt, kFrameThreads, 0));
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, S.device));
     S.maxStageBytes = optin;
     CK(cudaFuncSetAttribute((const void*)frameKernelBlock, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    CK(cudaFuncSetAttribute((const void*)frameKernelBlockExt, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     int khz = 0;
     if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, S.device) == cudaSuccess && khz > 0) S.clockKHz = khz;
     S.gridBlocks = std::max(1, perSm) * S.smCount;
+    S.gridBlocksExt = std::max(1, perSmExt) * S.smCount;
     return 0;
 }
 
@@ -203,13 +206,16 @@ int launchFrame(const FrameCoeffs& fc) {
     if (single) {
         FrameCoeffs f = fc;
         f.stageNodes = stage ? 1 : 0;
-        frameKernelBlock<<<1, kBlockThreads, stage ? stageBytes : 0, S.stream>>>(m, f, S.toolFrom, S.tool, S.cp, cu, state);
+        const bool ext = fc.guarded || fc.friction;
+        (ext ? frameKernelBlockExt : frameKernelBlock)<<<1, kBlockThreads, stage ? stageBytes : 0, S.stream>>>(m, f, S.toolFrom, S.tool, S.cp, cu, state);
         CK(cudaGetLastError());
     } else {
         ToolPose from = S.toolFrom, to = S.tool;
         ContactParams cp = S.cp;
         void* args[] = {&m, (void*)&fc, &from, &to, &cp, &cu, &state};
-        CK(cudaLaunchCooperativeKernel((const void*)frameKernelGrid, dim3(S.gridBlocks), dim3(kFrameThreads), args, 0, S.stream));
+        const bool ext = fc.guarded || fc.friction;
+        CK(cudaLaunchCooperativeKernel(ext ? (const void*)frameKernelGridExt : (const void*)frameKernelGrid, dim3(ext ? S.gridBlocksExt : S.gridBlocks),
+                                       dim3(kFrameThreads), args, 0, S.stream));
     }
     return 0;
 }
@@ -754,11 +760,13 @@ LCS_API int LCS_StepNoAlloc(float dt) {
     ContactParams cp = S.cp;
     bool single = S.launchMode == 2 || (S.launchMode == 0 && S.T < 65536 && S.N < 32768);
     if (single) {
-        frameKernelBlock<<<1, kFrameThreads, 0, S.stream>>>(m, fc, from, to, cp, cu, state);
+        (fc.guarded || fc.friction ? frameKernelBlockExt : frameKernelBlock)<<<1, kFrameThreads, 0, S.stream>>>(m, fc, from, to, cp, cu, state);
         CK(cudaGetLastError());
     } else {
         void* args[] = {&m, (void*)&fc, &from, &to, &cp, &cu, &state};
-        CK(cudaLaunchCooperativeKernel((const void*)frameKernelGrid, dim3(S.gridBlocks), dim3(kFrameThreads), args, 0, S.stream));
+        const bool ext = fc.guarded || fc.friction;
+        CK(cudaLaunchCooperativeKernel(ext ? (const void*)frameKernelGridExt : (const void*)frameKernelGrid, dim3(ext ? S.gridBlocksExt : S.gridBlocks),
+                                       dim3(kFrameThreads), args, 0, S.stream));
     }
     unsigned status = 0;
     CK(cudaMemcpyAsync(&status, state + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));

@@ -259,7 +259,7 @@ __device__ __forceinline__ TetRecord loadTet(const DeviceMesh& m, int k) {
 // Unguarded: hydrostatic row J - 1.  Guarded (tissue guard armed): row log J with a linear floor
 // below J = 0.05, its own bulk damping, and a trust region capping every corner's move at 0.15 over
 // the longest row of Dm^-1.
-__device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t, const FrameCoeffs& fc) {
+__device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t, const FrameCoeffs& fc, bool guardedForm = false) {
     int meta = t.meta;
     if ((meta & 8) == 0) return;
     const float* Bm = m.typeB[meta & 7];
@@ -280,7 +280,7 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
     float CD = sqrtf(fmaxf(q, 1e-12f));
     float devScale = 1.f / CD;
     float volGrad = J > .05f ? iso * I1 / (3.f * pJ) : 0.f;
-    const bool guarded = fc.guarded != 0;
+    const bool guarded = guardedForm;   // a compile-time false in the kernels built without the tissue guard
     float CH = guarded ? logPositive(pJ) + fminf(0.f, (J - .05f) / .05f) : J - 1.f;
     f3 gd[4], gh[4];
 #pragma unroll
@@ -327,7 +327,9 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
         m.pos[id[c]] = make_float4(o.x, o.y, o.z, w[c]);
     }
 }
-__device__ __forceinline__ void projectTet(const DeviceMesh& m, int k, const FrameCoeffs& fc) { applyTet(m, loadTet(m, k), fc); }
+__device__ __forceinline__ void projectTet(const DeviceMesh& m, int k, const FrameCoeffs& fc, bool guardedForm = false) {
+    applyTet(m, loadTet(m, k), fc, guardedForm);
+}
 
 // Liveness of one colour-ordered element from the live topology, k_RefreshLiveness
 // (xpbd_solver.cu:429-466).
