@@ -142,6 +142,62 @@ def run_reference_arm(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def workload_measurement(lib, name, steps, warmup, cpu_budget_s=6.0):
+    """Steps/s of another plain-path workload through the C ABI: device time from the library's
+    events around each frame (CUDA events), plus its CPU restatement on all host cores over a
+    bounded sample.  C1: 16x8x16 cells, 10 substeps, no tool.  C3: the C2 block with the blade swept
+    along its polyline; each step is LCS_Step plus the rod-phase LCS_DetectCut."""
+    import ctypes
+
+    import torch
+
+    from genesis_tissue_simulation_gb300 import workloads as W
+
+    w = W.make(name, steps=warmup + steps + 1)
+    s = w.open(lib)
+    try:
+        tets, edges = s.tet_count, int(s.functions["LCS_EdgeCount"]())
+        for k in range(warmup):
+            s.step(detect_cut=w.command(s, k))
+        torch.cuda.synchronize()
+        s.functions["LCS_ProfileEnable"](1)
+        t0 = time.perf_counter()
+        for k in range(warmup, warmup + steps):
+            s.step(detect_cut=w.command(s, k))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        ms = np.zeros(3, dtype=np.float32)
+        s.check("LCS_ProfileRead", steps, ms.ctypes.data_as(ctypes.c_void_p))
+        s.functions["LCS_ProfileEnable"](0)
+        revision = s.topology_revision() if w.blade_path else 0
+    finally:
+        s.close()
+    device_s = float(ms[0]) / 1e3
+    substeps = int(w.params["substeps"])
+    out = {"workload": w.name, "value": steps / device_s, "unit": "steps/s", "ms_per_step": 1e3 * device_s / steps,
+           "wall_steps_per_s": steps / wall, "proj_per_s": steps / device_s * substeps * (edges + tets), "tets": tets,
+           "substeps": substeps, "steps": steps, "timing": "CUDA events around each LCS_Step (rod-phase detection timed on the wall clock only)"}
+    if w.blade_path:
+        out["topology_revision_after"] = int(revision)
+    # CPU restatement, bounded sample
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+    s = w.open(ROOT / "oracle" / "_build" / "liboracle_f32.so")
+    try:
+        threads = int(s.dll.ORC_Threads())
+        s.step(detect_cut=w.command(s, 0))
+        n, t0 = 0, time.perf_counter()
+        while n < steps and time.perf_counter() - t0 < cpu_budget_s:
+            s.step(detect_cut=w.command(s, n + 1))
+            n += 1
+        cpu = n / (time.perf_counter() - t0)
+    finally:
+        s.close()
+    out["cpu_baseline"] = {"value": cpu, "unit": "steps/s", "cores": threads, "kind": "port",
+                           "sample": f"steps 2..{n + 1} of {w.name}, CPU restatement FP32, OpenMP {threads} threads"}
+    out["gpu_over_cpu"] = out["value"] / cpu
+    return out
+
+
 def cpu_baseline_sample(workload_name, budget_s=15.0, max_steps=40):
     """Time the CPU restatement on a bounded sample of the workload: consecutive steps from the start."""
     from genesis_tissue_simulation_gb300 import workloads as W
@@ -323,6 +379,7 @@ def main():
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--no-batched", action="store_true")
     parser.add_argument("--no-adjoint", action="store_true")
+    parser.add_argument("--no-workloads", action="store_true", help="skip the C1 and C3 lines")
     parser.add_argument("--only", default="all", choices=("all", "batched", "adjoint"),
                         help="run one section alone and print its JSON object (for profiling)")
     parser.add_argument("--batched-frames", type=int, default=20)
@@ -432,6 +489,8 @@ def main():
                      "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": substeps * bytes_per_substep},
         "clocks": clocks.summary(),
     }
+    if not args.no_workloads:
+        line["workloads"] = {"c1": workload_measurement(lib, "c1", 100, 5), "c3": workload_measurement(lib, "c3", 30, 3)}
     if not args.no_adjoint:
         line["adjoint"] = adjoint_measurement(lib)
     if not args.no_batched:

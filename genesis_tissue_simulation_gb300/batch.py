@@ -113,7 +113,7 @@ class TissueBatch:
         self.check("GBT_BatchSetLaunch", mode, threads)
 
     def autotune(self, trial_steps=3):
-        mode, threads, ms = I(), I(), (F * 3)()
+        mode, threads, ms = I(), I(), (F * 6)()
         self.check("GBT_BatchAutotune", self.dt, trial_steps, ct.byref(mode), ct.byref(threads), ms)
         return {"mode": mode.value, "threads": threads.value, "ms_per_frame": [float(v) for v in ms]}
 

@@ -66,7 +66,8 @@ struct Batch {
     ContactParams cp{0.02f, 1.0e-7f, 0.5f, 0.045f, 0.25f};
     float lastH = -1.f;
     // launch
-    int mode = 0, threads = 256, ctas = 0;            // mode 0 lockstep grid, 1 one CTA per instance
+    int mode = 0, threads = 256, ctas = 0;            // mode 0 lockstep grid, 1 one CTA per instance, 2 clusters
+    int clusterLogK = 1, clusterSlots = 0;            // mode 2: CTAs per cluster (2^logK), shared-memory slots per CTA
     cudaGraphExec_t graph = nullptr; int graphSteps = 0; int graphMode = -1; float graphDt = 0.f;
     bool profile = false; std::vector<cudaEvent_t> events;
 };
@@ -223,13 +224,54 @@ int launchFrame(const FrameCoeffs& fc, const ContactFrame* frames) {
         cfg.attrs = attr; cfg.numAttrs = 1;
         CK(cudaMemsetAsync(state + 1, 0, sizeof(unsigned), G.stream));
         CK(cudaLaunchKernelEx(&cfg, frameKernelGrid, m, fc, none, none, cp, cu, state));
-    } else {
+    } else if (G.mode == 1) {
         InstanceTable it{G.nodeBaseD.p, G.nodeCountD.p, G.instEdge.p, G.instBend.p, G.instTet.p, G.order.p, G.ctaStart.p, G.derived.p};
         if (G.threads == 512) frameKernelInstances512<<<G.ctas, 512, 0, G.stream>>>(m, fc, G.cp, it);
         else frameKernelInstances256<<<G.ctas, 256, 0, G.stream>>>(m, fc, G.cp, it);
         CK(cudaGetLastError());
+    } else {
+        InstanceTable it{G.nodeBaseD.p, G.nodeCountD.p, G.instEdge.p, G.instBend.p, G.instTet.p, G.order.p, G.ctaStart.p, G.derived.p};
+        const int K = 1 << G.clusterLogK;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(G.ctas * K); cfg.blockDim = dim3(kClusterThreads); cfg.stream = G.stream;
+        cfg.dynamicSmemBytes = (size_t)G.clusterSlots * sizeof(float4);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = K; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr; cfg.numAttrs = 1;
+        ContactParams cp = G.cp;
+        int logK = G.clusterLogK;
+        CK(cudaLaunchKernelEx(&cfg, frameKernelCluster, m, fc, cp, it, logK));
     }
     return 0;
+}
+
+// Cluster launch shape for K CTAs per cluster: the shared-memory slots of the largest instance
+// (interleaved in blocks of kClusterThreads nodes over the K CTAs), the number of clusters that
+// fit on the GPU at once, and the LPT packing of the instances over those clusters.
+int packClusters(int K) {
+    int logK = 0;
+    while ((1 << logK) < K) logK++;
+    const int block = kClusterThreads * K;
+    int slots = 0;
+    for (int i = 0; i < G.count; i++) slots = std::max(slots, ((G.nodeCount[i] + block - 1) / block) * kClusterThreads);
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, G.device));
+    const size_t bytes = (size_t)slots * sizeof(float4);
+    if (bytes + 1024 > (size_t)optin) return LCS_ERR_UNSUPPORTED;   // an instance does not fit this cluster size
+    CK(cudaFuncSetAttribute((const void*)frameKernelCluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(K); cfg.blockDim = dim3(kClusterThreads); cfg.dynamicSmemBytes = bytes;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = K; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr; cfg.numAttrs = 1;
+    int clusters = 0;
+    CK(cudaOccupancyMaxActiveClusters(&clusters, (const void*)frameKernelCluster, &cfg));
+    if (clusters <= 0) return LCS_ERR_UNSUPPORTED;
+    G.clusterLogK = logK;
+    G.clusterSlots = slots;
+    return packInstances(clusters);
 }
 
 int prepareAlphas(float h) {
@@ -508,19 +550,21 @@ LCS_API int GBT_BatchNodeRange(int instance, int* base, int* count) {
 }
 
 LCS_API int GBT_BatchSetLaunch(int mode, int threads) {
-    if (!G.ready || mode < 0 || mode > 1 || (threads != 256 && threads != 512)) return XPBD_ERR_BAD_ARG;
-    G.mode = mode; G.threads = threads;
-    int perSm = threads == 512 ? 1 : 2;
-    int rc = packInstances(G.smCount * perSm);
+    if (!G.ready || mode < 0 || mode > 2) return XPBD_ERR_BAD_ARG;
+    if (mode < 2 && threads != 256 && threads != 512) return XPBD_ERR_BAD_ARG;
+    if (mode == 2 && threads != 2 && threads != 4 && threads != 8) return XPBD_ERR_BAD_ARG;   // CTAs per cluster
+    int rc = mode == 2 ? packClusters(threads) : packInstances(G.smCount * (threads == 512 ? 1 : 2));
     if (rc) return rc;
+    G.mode = mode; G.threads = threads;
     dropGraph();
     return 0;
 }
 
 // Try every launch shape for `trialSteps` frames from the current state, keep the fastest, and put
 // the state back (all shapes give bit-identical results, so the trial frames leave no trace).
-// Out: mode, threads, and the ms per frame of each candidate (3 floats).
-LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threadsOut, float* msOut3) {
+// Out: mode, threads, and the ms per frame of each candidate (kAutotuneShapes floats; a shape the
+// batch cannot use, e.g. a cluster too small for its largest instance, reports -1).
+LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threadsOut, float* msOut6) {
     if (!G.ready || trialSteps <= 0) return XPBD_ERR_BAD_ARG;
     Buf<float4> savePos, savePrev, saveVel;
     CK(savePos.alloc(G.N)); CK(savePrev.alloc(G.N)); CK(saveVel.alloc(G.N));
@@ -528,12 +572,13 @@ LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threa
     CK(cudaMemcpyAsync(savePrev.p, G.prev.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
     CK(cudaMemcpyAsync(saveVel.p, G.vel.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
     std::vector<ToolPose> keepFrom = G.toolFrom, keepTool = G.tool;
-    const int modes[3][2] = {{0, 256}, {1, 256}, {1, 512}};
+    const int modes[6][2] = {{0, 256}, {1, 256}, {1, 512}, {2, 2}, {2, 4}, {2, 8}};
     float best = 1e30f; int bestK = 0;
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a)); CK(cudaEventCreate(&b));
-    for (int k = 0; k < 3; k++) {
+    for (int k = 0; k < 6; k++) {
         int rc = GBT_BatchSetLaunch(modes[k][0], modes[k][1]);
+        if (rc == LCS_ERR_UNSUPPORTED) { if (msOut6) msOut6[k] = -1.f; continue; }
         if (rc) return rc;
         rc = stepFrames(dt, 1, nullptr, false);   // warm-up
         if (rc) return rc;
@@ -544,7 +589,7 @@ LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threa
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, a, b));
         ms /= trialSteps;
-        if (msOut3) msOut3[k] = ms;
+        if (msOut6) msOut6[k] = ms;
         if (ms < best) { best = ms; bestK = k; }
         CK(cudaMemcpyAsync(G.pos.p, savePos.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
         CK(cudaMemcpyAsync(G.prev.p, savePrev.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));

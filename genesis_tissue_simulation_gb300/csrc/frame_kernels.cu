@@ -9,6 +9,8 @@
 // Work inside a colour is strided over the participating threads; per-node phases use the same
 // node-to-thread map in every phase, so a node's contact, velocity update and next predict need
 // no barrier between them.
+#include <cooperative_groups.h>
+
 #include "tissue_device.cuh"
 #include "grid_sync.cuh"
 #include "friction_contact.cuh"
@@ -21,8 +23,9 @@ namespace gbt {
 // ---------------------------------------------------------------------------------------------
 // The substep's instrument frame (contactFrame) lives in tissue_device.cuh: batches evaluate it on
 // the host, single meshes on the device, with the same operations.
+template <bool Dsm = false>
 __device__ __forceinline__ void contactNode(const DeviceMesh& m, int c, const ContactFrame& f, const ContactParams& cp) {
-    float4 P = m.pos[c];
+    float4 P = posRef<Dsm>(m, c);
     float wc = P.w;
     if (wc <= 0.f) return;
     f3 p = xyz(P);
@@ -63,7 +66,7 @@ __device__ __forceinline__ void contactNode(const DeviceMesh& m, int c, const Co
             }
         }
     }
-    m.pos[c] = make_float4(p.x, p.y, p.z, wc);
+    posRef<Dsm>(m, c) = make_float4(p.x, p.y, p.z, wc);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -274,7 +277,8 @@ __device__ __noinline__ void frictionPhase(const DeviceMesh& m, const FrameCoeff
 // ---------------------------------------------------------------------------------------------
 // Extended: the tissue guard and contact model 1 are compiled in.  Kernels without them keep the
 // plain path's register allocation (the extended kernel launches only when either is armed).
-template <class Sync, bool Extended>
+// Dsm: node positions live in the cluster's distributed shared memory (cluster batch kernel).
+template <class Sync, bool Extended, bool Dsm = false>
 __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
                          const ContactParams& cp, const CutParams& cu, unsigned* state, Sync& sync) {
     const int r = sync.rank(), R = sync.size();
@@ -318,7 +322,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         const int nodeEnd = m.nodeBase + m.nNodes;
         // -- predict (k_predict) --
         for (int i = m.nodeBase + r; i < nodeEnd; i += R) {
-            float4 P = m.pos[i];
+            float4 P = posRef<Dsm>(m, i);
             if (stale) P.w = nodeInvMass(m, i);
             m.prev[i] = make_float4(P.x, P.y, P.z, 0.f);
             if (P.w > 0.f) {
@@ -329,7 +333,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 f3 x = xyz(P) + v * fc.h;
                 P = make_float4(x.x, x.y, x.z, P.w);
             }
-            m.pos[i] = P;
+            posRef<Dsm>(m, i) = P;
         }
         if (!sync.sync()) return;
         mark(s, kPhasePredict);
@@ -341,14 +345,14 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         if (fc.doEdges)
             for (int c = 0; c < m.nEdgeColors; c++) {
                 int2 rg = m.edgeRange[c];
-                for (int e = rg.x + r; e < rg.y; e += R) applyEdge(m, loadEdge(m, e, fc), fc);
+                for (int e = rg.x + r; e < rg.y; e += R) applyEdge<Dsm>(m, loadEdge(m, e, fc), fc);
                 if (!sync.sync()) return;
                 mark(s, kPhaseEdges);
             }
         if (fc.doBend)
             for (int c = 0; c < m.nBendColors; c++) {
                 int2 rg = m.bendRange[c];
-                for (int e = rg.x + r; e < rg.y; e += R) projectBend(m, e, fc);
+                for (int e = rg.x + r; e < rg.y; e += R) projectBend<Dsm>(m, e, fc);
                 if (!sync.sync()) return;
                 mark(s, kPhaseBends);
             }
@@ -364,8 +368,8 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 int2 nrg = c + 1 < m.nTetColors ? m.tetRange[c + 1] : make_int2(0, 0);
                 hasNext = nrg.x + r < nrg.y;
                 if (hasNext) next = loadTet(m, nrg.x + r);
-                if (hasCur) applyTet(m, cur, fc, guarded);
-                for (int k = rg.x + r + R; k < rg.y; k += R) projectTet(m, k, fc, guarded);
+                if (hasCur) applyTet<Dsm>(m, cur, fc, guarded);
+                for (int k = rg.x + r + R; k < rg.y; k += R) projectTet<Dsm>(m, k, fc, guarded);
                 if (!sync.sync()) return;
                 mark(s, kPhaseTets);
             }
@@ -392,12 +396,12 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
             if (fc.contact && !guarded) {
                 if (m.nodeInstance) {   // batched instances: each node meets its own instance's tool
                     const ContactFrame& own = m.contactFrames[(size_t)(fc.firstSubstep + s) * m.nInstances + m.nodeInstance[i]];
-                    contactNode(m, i, own, cp);
+                    contactNode<Dsm>(m, i, own, cp);
                 } else {
-                    contactNode(m, i, cf, cp);
+                    contactNode<Dsm>(m, i, cf, cp);
                 }
             }
-            float4 P = m.pos[i], Q = m.prev[i];
+            float4 P = posRef<Dsm>(m, i), Q = m.prev[i];
             f3 v = P.w > 0.f ? (xyz(P) - xyz(Q)) * fc.invH : mk(0.f, 0.f, 0.f);
             if (!fc.perpDamp) v = P.w > 0.f ? v * fc.velScale : mk(0.f, 0.f, 0.f);
             m.vel[i] = make_float4(v.x, v.y, v.z, 0.f);
@@ -409,7 +413,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 for (int e = rg.x + r; e < rg.y; e += R) {
                     if (m.edgeLive[e] == 0) continue;
                     int2 ij = m.edgeEnds[e];
-                    float4 Pi = m.pos[ij.x], Pj = m.pos[ij.y];
+                    float4 Pi = posRef<Dsm>(m, ij.x), Pj = posRef<Dsm>(m, ij.y);
                     float wi = Pi.w, wj = Pj.w;
                     if (wi + wj <= 0.f) continue;
                     f3 d = xyz(Pi) - xyz(Pj);
@@ -424,7 +428,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
             }
             for (int i = m.nodeBase + r; i < nodeEnd; i += R) {
                 float4 V = m.vel[i];
-                f3 v = m.pos[i].w > 0.f ? xyz(V) * fc.velScale : mk(0.f, 0.f, 0.f);
+                f3 v = posRef<Dsm>(m, i).w > 0.f ? xyz(V) * fc.velScale : mk(0.f, 0.f, 0.f);
                 m.vel[i] = make_float4(v.x, v.y, v.z, 0.f);
             }
         }
@@ -463,6 +467,54 @@ __device__ __forceinline__ void runInstances(const DeviceMesh& m, const FrameCoe
         __syncthreads();
     }
 }
+// ---------------------------------------------------------------------------------------------
+// batched instances on thread-block clusters: positions in distributed shared memory
+// ---------------------------------------------------------------------------------------------
+// Each cluster of K CTAs (512 threads each) runs its list of instances one after another.  An
+// instance's positions are copied into the cluster's shared memory for the frame, interleaved in
+// blocks of 512 nodes over the K CTAs (posRef<true>), which puts every node a thread updates in its
+// own phases (predict, contact, velocity) in its own CTA; the colour sweeps gather and scatter the
+// other nodes through distributed shared memory, and each colour ends at the hardware cluster
+// barrier (release/acquire at cluster scope).  Everything else (prev, vel, element tables) stays in
+// device memory.
+struct ClusterSync {
+    int r, n; bool lead;
+    __device__ int rank() const { return r; }
+    __device__ int size() const { return n; }
+    __device__ bool leader() const { return lead; }
+    __device__ bool sync() { cooperative_groups::this_cluster().sync(); return true; }
+};
+
+__global__ void __launch_bounds__(kClusterThreads) frameKernelCluster(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it,
+                                                                       int logK) {
+    extern __shared__ float4 clusterSlots[];
+    __shared__ float4* bases[8];
+    cooperative_groups::cluster_group cluster = cooperative_groups::this_cluster();
+    const int K = 1 << logK, rank = (int)cluster.block_rank();
+    if ((int)threadIdx.x < K) bases[threadIdx.x] = cluster.map_shared_rank(clusterSlots, (int)threadIdx.x);
+    __syncthreads();
+    ClusterSync sync{rank * kClusterThreads + (int)threadIdx.x, K * kClusterThreads, rank == 0 && threadIdx.x == 0};
+    const int cid = blockIdx.x >> logK;      // the CTAs of one cluster are consecutive in x
+    CutParams noCut{};
+    ToolPose none{};
+    for (int j = it.ctaStart[cid]; j < it.ctaStart[cid + 1]; j++) {
+        const int i = it.order[j];
+        DeviceMesh v = m;
+        v.nodeBase = it.nodeBase[i];
+        v.nNodes = it.nodeCount[i];
+        v.edgeRange = it.edgeRange + (size_t)i * m.nEdgeColors;
+        v.bendRange = it.bendRange + (size_t)i * m.nBendColors;
+        v.tetRange = it.tetRange + (size_t)i * m.nTetColors;
+        v.dsm = bases; v.dsmLogB = kClusterLogThreads; v.dsmLogK = logK;
+        for (int n = sync.r; n < v.nNodes; n += sync.n) posRef<true>(v, v.nodeBase + n) = m.pos[v.nodeBase + n];
+        cluster.sync();
+        runFrame<ClusterSync, false, true>(v, fc, none, none, cp, noCut, it.derived + i, sync);
+        cluster.sync();
+        for (int n = sync.r; n < v.nNodes; n += sync.n) m.pos[v.nodeBase + n] = posRef<true>(v, v.nodeBase + n);
+    }
+    cluster.sync();   // no CTA leaves while another may still read its shared memory
+}
+
 __global__ void __launch_bounds__(256) frameKernelInstances256(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it) {
     runInstances(m, fc, cp, it);
 }

@@ -25,6 +25,11 @@ struct InstanceTable {
     unsigned* derived;                                                     // per instance: revision its liveness was derived at
 };
 __global__ void frameKernelInstances256(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it);
+// Instances on thread-block clusters of 2^logK CTAs x kClusterThreads, positions in distributed
+// shared memory (dynamic shared memory: the per-CTA slots of the largest instance, 16 B each);
+// it.ctaStart indexes clusters.
+constexpr int kClusterThreads = 512, kClusterLogThreads = 9;
+__global__ void frameKernelCluster(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it, int logK);
 __global__ void frameKernelInstances512(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it);
 
 __global__ void tetAlphaKernel(int n, float invH2, const float2* stiff, float2* alpha);

@@ -51,7 +51,21 @@ struct DeviceMesh {
     // chain's candidate positions and marks [N], incident live-tet lists (CSR over colour slots),
     // and two flags (candidate below the minimum volume; still below after the repair)
     float* fiberLambda; float4* feasTarget; int* needed; const int* incOff; const int* incTet; unsigned* guardFlags;
+    // instance positions in a cluster's distributed shared memory (cluster batch kernel): node j of
+    // the instance (j = i - nodeBase) lives in CTA (j >> logB) & (K - 1), slot
+    // ((j >> (logB + logK)) << logB) | (j & (B - 1)); dsm[k] is CTA k's array (a generic pointer)
+    float4* const* dsm; int dsmLogB, dsmLogK;
 };
+
+// A node's position: plain device memory, or its slot in the cluster's distributed shared memory.
+template <bool Dsm>
+__device__ __forceinline__ float4& posRef(const DeviceMesh& m, int i) {
+    if (!Dsm) return m.pos[i];
+    const int j = i - m.nodeBase;
+    const int owner = (j >> m.dsmLogB) & ((1 << m.dsmLogK) - 1);
+    const int slot = ((j >> (m.dsmLogB + m.dsmLogK)) << m.dsmLogB) | (j & ((1 << m.dsmLogB) - 1));
+    return m.dsm[owner][slot];
+}
 
 // Per-frame coefficients, computed on the host in FP32 exactly as xpbd_begin_frame does
 // (xpbd_solver.cu:2481-2514).
@@ -190,12 +204,13 @@ __device__ __forceinline__ EdgeRecord loadEdge(const DeviceMesh& m, int e, const
 
 // Lattice-edge distance constraint, k_solve_edges (xpbd_solver.cu:484-524).  Multipliers restart
 // at zero every substep and each edge is projected once, so the lambda term vanishes.
+template <bool Dsm = false>
 __device__ __forceinline__ void applyEdge(const DeviceMesh& m, const EdgeRecord& r, const FrameCoeffs& fc) {
     if (r.live == 0) return;
     float alphaTilde = fc.alphaTilde;
     if (fc.fallback) alphaTilde = fc.fallbackInvEh2 / r.rest;
     int2 ij = r.ij;
-    float4 pi = m.pos[ij.x], pj = m.pos[ij.y];
+    float4 pi = posRef<Dsm>(m, ij.x), pj = posRef<Dsm>(m, ij.y);
     float wi = pi.w, wj = pj.w, ws = wi + wj;
     if (ws <= 0.f) return;
     f3 d = xyz(pi) - xyz(pj);
@@ -209,15 +224,16 @@ __device__ __forceinline__ void applyEdge(const DeviceMesh& m, const EdgeRecord&
     float ap = fc.omega * dl;
     f3 a = xyz(pi) + n * (wi * ap);
     f3 b = xyz(pj) - n * (wj * ap);
-    m.pos[ij.x] = make_float4(a.x, a.y, a.z, wi);
-    m.pos[ij.y] = make_float4(b.x, b.y, b.z, wj);
+    posRef<Dsm>(m, ij.x) = make_float4(a.x, a.y, a.z, wi);
+    posRef<Dsm>(m, ij.y) = make_float4(b.x, b.y, b.z, wj);
 }
 
 // Bending angle constraint, k_solve_bending (xpbd_solver.cu:534-573); off unless kb > 0.
+template <bool Dsm = false>
 __device__ __forceinline__ void projectBend(const DeviceMesh& m, int e, const FrameCoeffs& fc) {
     if (m.bendLive[e] == 0) return;
     int4 r = m.bendIJK[e];
-    float4 Pi = m.pos[r.x], Pj = m.pos[r.y], Pk = m.pos[r.z];
+    float4 Pi = posRef<Dsm>(m, r.x), Pj = posRef<Dsm>(m, r.y), Pk = posRef<Dsm>(m, r.z);
     float wi = Pi.w, wj = Pj.w, wk = Pk.w;
     if (wi + wj + wk <= 0.f) return;
     f3 u = xyz(Pi) - xyz(Pj), v = xyz(Pi) - xyz(Pk);
@@ -237,9 +253,9 @@ __device__ __forceinline__ void projectBend(const DeviceMesh& m, int e, const Fr
     if (den < 1e-12f) return;
     float ap = fc.omega * ((-C - g * gdx) / den);
     f3 a = xyz(Pi) + gi * (wi * ap), b = xyz(Pj) + gj * (wj * ap), cc = xyz(Pk) + gk * (wk * ap);
-    m.pos[r.x] = make_float4(a.x, a.y, a.z, wi);
-    m.pos[r.y] = make_float4(b.x, b.y, b.z, wj);
-    m.pos[r.z] = make_float4(cc.x, cc.y, cc.z, wk);
+    posRef<Dsm>(m, r.x) = make_float4(a.x, a.y, a.z, wi);
+    posRef<Dsm>(m, r.y) = make_float4(b.x, b.y, b.z, wj);
+    posRef<Dsm>(m, r.z) = make_float4(cc.x, cc.y, cc.z, wk);
 }
 
 // What a tet projection reads that no phase of the Gauss-Seidel sweep writes: its record and the
@@ -259,12 +275,13 @@ __device__ __forceinline__ TetRecord loadTet(const DeviceMesh& m, int k) {
 // Unguarded: hydrostatic row J - 1.  Guarded (tissue guard armed): row log J with a linear floor
 // below J = 0.05, its own bulk damping, and a trust region capping every corner's move at 0.15 over
 // the longest row of Dm^-1.
+template <bool Dsm = false>
 __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t, const FrameCoeffs& fc, bool guardedForm = false) {
     int meta = t.meta;
     if ((meta & 8) == 0) return;
     const float* Bm = m.typeB[meta & 7];
     int id[4] = {t.ids.x, t.ids.y, t.ids.z, t.ids.w};
-    float4 P[4] = {m.pos[id[0]], m.pos[id[1]], m.pos[id[2]], m.pos[id[3]]};
+    float4 P[4] = {posRef<Dsm>(m, id[0]), posRef<Dsm>(m, id[1]), posRef<Dsm>(m, id[2]), posRef<Dsm>(m, id[3])};
     f3 p[4] = {xyz(P[0]), xyz(P[1]), xyz(P[2]), xyz(P[3])};
     f3 br[3] = {mk(Bm[0], Bm[1], Bm[2]), mk(Bm[3], Bm[4], Bm[5]), mk(Bm[6], Bm[7], Bm[8])};
     f3 e1 = p[1] - p[0], e2 = p[2] - p[0], e3 = p[3] - p[0];
@@ -324,11 +341,12 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         f3 o = p[c] + (gd[c] * dlD + gh[c] * dlH) * w[c];
-        m.pos[id[c]] = make_float4(o.x, o.y, o.z, w[c]);
+        posRef<Dsm>(m, id[c]) = make_float4(o.x, o.y, o.z, w[c]);
     }
 }
+template <bool Dsm = false>
 __device__ __forceinline__ void projectTet(const DeviceMesh& m, int k, const FrameCoeffs& fc, bool guardedForm = false) {
-    applyTet(m, loadTet(m, k), fc, guardedForm);
+    applyTet<Dsm>(m, loadTet(m, k), fc, guardedForm);
 }
 
 // Liveness of one colour-ordered element from the live topology, k_RefreshLiveness

@@ -8,9 +8,10 @@
  *
  * Status: 0 ok; -(cudaError_t); -1000..-1005 solver (xpbd_solver.h:25-33); -2000..-2004 physics
  * init (V/physics.cu:219-228); -3000..-3002 cut init (V/cut.cu:1109-1206);
- * LCS_ERR_UNSUPPORTED (-4001): a switch of the unified contact/grasp solver or of the tissue
- * guard that this library does not provide; LCS_ERR_DEVICE_TIMEOUT (-4002): a device barrier
- * exceeded its spin budget and the frame was abandoned.
+ * LCS_ERR_UNSUPPORTED (-4001): a switch of the reference's unified contact/grasp solver that this
+ * library does not provide (contact model 2, grasp capture on model 0, surface-contact entry
+ * points); LCS_ERR_DEVICE_TIMEOUT (-4002): a device barrier exceeded its spin budget and the frame
+ * was abandoned.
  */
 #ifndef GBTISSUE_H
 #define GBTISSUE_H
@@ -68,8 +69,12 @@ LCS_API int LCS_DetectCut(void);                                     /* cut_dete
 LCS_API void LCS_SetPressureCutMode(int enabled);                    /* pressure mode: detection off here */
 LCS_API int LCS_SetGraspTool(const void* xpbdToolState);             /* xpbd_set_tool; capture -> -4001 */
 LCS_API void LCS_SetGraspParams(const GraspParamsAbi* params);       /* xpbd_set_grasp_params */
-LCS_API int LCS_SetContactModel(int enabled, float muS, float muD, float thickness, float radius); /* model 0 only */
-LCS_API int LCS_SetTissueGuard(float minimum, int passes, int count, const int* inside, int capture); /* passes 0 only */
+/* xpbd_set_contact_model: 0 capsule/jaw-slab CCD gate; 1 tool SDFs (shaft capsule, two jaw boxes)
+ * with swept contact and Coulomb friction on lattice nodes (no reconstructed surface); 2 -> -4001. */
+LCS_API int LCS_SetContactModel(int enabled, float muS, float muD, float thickness, float radius);
+/* xpbd_set_tissue_guard: passes > 0 arms the guarded tet form, `passes` tensile sweeps and the
+ * feasibility chain (minimum relative volume `minimum`); `inside`/`capture` concern grasp capture. */
+LCS_API int LCS_SetTissueGuard(float minimum, int passes, int count, const int* inside, int capture);
 LCS_API int LCS_SetTissueMaterial(float tensileStrength, float bulkDampingSeconds);
 
 /* ---- readback (plugin_api.cpp:38, 170-177) ----------------------------------------------------- */
@@ -132,8 +137,13 @@ LCS_API int GBT_BatchStepMany(float dt, int steps, const void* tools, int useGra
 LCS_API int GBT_BatchGetPositions(float* out3N);                      /* all nodes, instance after instance */
 LCS_API int GBT_BatchNodeRange(int instance, int* base, int* count);
 LCS_API int GBT_BatchInfo(int* counts8);                               /* instances, nodes, edges, tets, edge colours, tet colours, mode, threads */
-LCS_API int GBT_BatchSetLaunch(int mode, int threads);                 /* 0 lockstep grid | 1 one CTA per instance; 256 | 512 */
-LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threadsOut, float* msPerFrame3);
+/* Launch shape: mode 0 lockstep grid (threads 256), 1 one CTA per instance (threads 256 | 512),
+ * 2 one thread-block cluster per instance list with positions in distributed shared memory
+ * (`threads` = CTAs per cluster: 2 | 4 | 8; -4001 when the largest instance does not fit). */
+LCS_API int GBT_BatchSetLaunch(int mode, int threads);
+/* Times the six shapes {0/256, 1/256, 1/512, 2/2, 2/4, 2/8} and keeps the fastest; msPerFrame6 gets
+ * each one's ms per frame (-1: not usable for this batch). */
+LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threadsOut, float* msPerFrame6);
 LCS_API void GBT_BatchProfileEnable(int enabled);
 LCS_API int GBT_BatchProfileRead(float* msTotal);                      /* device ms of the profiled step calls */
 LCS_API void GBT_BatchShutdown(void);

@@ -3,7 +3,8 @@
 A batch packs each instance's own topology into one table, so every instance must evolve exactly as
 it does alone: the test compares each instance's nodes after every frame with a solo FP32 oracle
 session driven with the same commands, in each launch shape (lockstep grid, one CTA per instance at
-256 and 512 threads) and with the frames replayed from a CUDA graph.
+256 and 512 threads, thread-block clusters of 2, 4 and 8 CTAs with the positions in distributed shared
+memory) and with the frames replayed from a CUDA graph.
 """
 import numpy as np
 import pytest
@@ -60,7 +61,8 @@ def batched(workload, lib, mode, threads, use_graph):
     return frames, info
 
 
-@pytest.mark.parametrize("mode,threads,use_graph", [(0, 256, False), (0, 256, True), (1, 256, True), (1, 512, False)])
+@pytest.mark.parametrize("mode,threads,use_graph", [(0, 256, False), (0, 256, True), (1, 256, True), (1, 512, False),
+                                                    (2, 2, False), (2, 4, True), (2, 8, False)])
 def test_batched_instances_match_solo_oracle(gpu_lib, oracle_libs, small_batch, mode, threads, use_graph):
     frames, info = batched(small_batch, gpu_lib, mode, threads, use_graph)
     assert info["instances"] == len(small_batch.grids) and info["mode"] == mode and info["threads"] == threads
@@ -79,6 +81,7 @@ def test_autotune_keeps_state(gpu_lib, small_batch):
         b.set_capsules(small_batch.capsules_at(0))
         before = b.positions()
         choice = b.autotune(trial_steps=2)
-        assert choice["mode"] in (0, 1) and choice["threads"] in (256, 512)
-        assert all(ms > 0 for ms in choice["ms_per_frame"])
+        assert (choice["mode"] in (0, 1) and choice["threads"] in (256, 512)) or (choice["mode"] == 2 and choice["threads"] in (2, 4, 8))
+        assert len(choice["ms_per_frame"]) == 6 and all(ms > 0 or ms == -1 for ms in choice["ms_per_frame"])
+        assert all(ms > 0 for ms in choice["ms_per_frame"][:3])
         assert np.array_equal(b.positions(), before)
