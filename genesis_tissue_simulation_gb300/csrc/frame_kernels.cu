@@ -14,6 +14,7 @@
 #include "tissue_device.cuh"
 #include "grid_sync.cuh"
 #include "friction_contact.cuh"
+#include "particle_frame.cuh"
 #include "frame_kernels.h"
 
 namespace gbt {
@@ -278,7 +279,8 @@ __device__ __noinline__ void frictionPhase(const DeviceMesh& m, const FrameCoeff
 // Extended: the tissue guard and contact model 1 are compiled in.  Kernels without them keep the
 // plain path's register allocation (the extended kernel launches only when either is armed).
 // Dsm: node positions live in the cluster's distributed shared memory (cluster batch kernel).
-template <class Sync, bool Extended, bool Dsm = false>
+// Rotations: the session kernels, which also compute the particle frames (batched instances do not).
+template <class Sync, bool Extended, bool Dsm = false, bool Rotations = false>
 __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
                          const ContactParams& cp, const CutParams& cu, unsigned* state, Sync& sync) {
     const int r = sync.rank(), R = sync.size();
@@ -295,6 +297,17 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
             asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(ns));
             fc.phaseClock[(size_t)s * kPhaseRecordsPerSubstep + slot++] = ((unsigned long long)tag << 56) | (ns & 0x00FFFFFFFFFFFFFFull);
         }
+    };
+    // particle frames from the current state into the other buffer (physics_compute_rotations,
+    // V/physics.cu:399-411); every thread takes its own nodes, the caller synchronises around it.
+    // Session kernels only, where positions are plain memory (Dsm is false).
+    const bool rotations = Rotations && fc.rotations != 0;
+    int rotParity = fc.rotParity;
+    auto framePass = [&]() {
+        const float* prevRot = m.particleRot[rotParity];
+        float* rot = m.particleRot[rotParity ^ 1];
+        for (int i = m.nodeBase + r; i < m.nodeBase + m.nNodes; i += R) particleFrame(i, m.pos, m.nbr, m.active, m.pinned, prevRot, rot);
+        rotParity ^= 1;
     };
     for (int s = 0; s < fc.substeps; s++) {
         slot = 0;
@@ -436,15 +449,31 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         // -- blade ribbon tick between substeps --
         if (fc.cut) {   // the first tick after the blade is set only takes the position snapshot
             if (havePrev) {
+                // cut points emitted so far (the surface revision); nothing changes it between the
+                // previous tick's closing barrier and this tick's opening one
+                const unsigned pointsBefore = rotations ? *(volatile unsigned*)(cu.counters + 1) : 0u;
                 if (!sync.sync()) return;
                 for (int e = r; e < cu.nGridEdges; e += R) tickEdge(m, cu, e, true);
                 if (!sync.sync()) return;
                 mark(s, kPhaseTick);
+                // a tick that emitted cut points is followed by fresh frames before the next substep
+                // (V/physics.cu:368-379)
+                if (rotations && fc.firstSubstep + s + 1 < fc.numSubsteps && *(volatile unsigned*)(cu.counters + 1) != pointsBefore) {
+                    framePass();
+                    if (!sync.sync()) return;
+                }
             }
             havePrev = true;
         }
     }
-    if (sync.leader()) *(volatile unsigned*)state = derivedAt;
+    if (rotations && fc.firstSubstep + fc.substeps == fc.numSubsteps) {   // LCS_Step's closing frames
+        if (!sync.sync()) return;
+        framePass();
+    }
+    if (sync.leader()) {
+        *(volatile unsigned*)state = derivedAt;
+        if (rotations) state[3] = (unsigned)rotParity;
+    }
 }
 
 // Batched instances, one CTA per instance at a time: CTA b serves the instances
@@ -526,13 +555,13 @@ template <bool Extended>
 __device__ __forceinline__ void gridFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
                                           const ContactParams& cp, const CutParams& cu, unsigned* state) {
     GridSync g{state + 1, state + 2, gridDim.x, 0u, fc.spinBudget, (unsigned)fc.syncTestExtra};
-    runFrame<GridSync, Extended>(m, fc, from, to, cp, cu, state, g);
+    runFrame<GridSync, Extended, false, true>(m, fc, from, to, cp, cu, state, g);
 }
-__global__ void __launch_bounds__(kFrameThreads) frameKernelGrid(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
+__global__ void __launch_bounds__(kFrameThreads, 2) frameKernelGrid(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                   ContactParams cp, CutParams cu, unsigned* state) {
     gridFrame<false>(m, fc, from, to, cp, cu, state);
 }
-__global__ void __launch_bounds__(kFrameThreads) frameKernelGridExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
+__global__ void __launch_bounds__(kFrameThreads, 2) frameKernelGridExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                      ContactParams cp, CutParams cu, unsigned* state) {
     gridFrame<true>(m, fc, from, to, cp, cu, state);
 }
@@ -546,7 +575,7 @@ __device__ __forceinline__ void blockFrame(DeviceMesh m, const FrameCoeffs& fc, 
     extern __shared__ float4 staged[];
     BlockSync b{state + 2};
     if (!fc.stageNodes) {
-        runFrame<BlockSync, Extended>(m, fc, from, to, cp, cu, state, b);
+        runFrame<BlockSync, Extended, false, true>(m, fc, from, to, cp, cu, state, b);
         return;
     }
     float4* sPos = staged;
@@ -557,7 +586,7 @@ __device__ __forceinline__ void blockFrame(DeviceMesh m, const FrameCoeffs& fc, 
     float4* gPrev = m.prev;
     m.pos = sPos;
     m.prev = sPrev;
-    runFrame<BlockSync, Extended>(m, fc, from, to, cp, cu, state, b);
+    runFrame<BlockSync, Extended, false, true>(m, fc, from, to, cp, cu, state, b);
     __syncthreads();
     for (int i = threadIdx.x; i < m.nNodes; i += blockDim.x) { gPos[i] = sPos[i]; gPrev[i] = sPrev[i]; }
 }
@@ -568,6 +597,14 @@ __global__ void __launch_bounds__(kBlockThreads) frameKernelBlock(DeviceMesh m, 
 __global__ void __launch_bounds__(kBlockThreads) frameKernelBlockExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                       ContactParams cp, CutParams cu, unsigned* state) {
     blockFrame<true>(m, fc, from, to, cp, cu, state);
+}
+
+// Particle frames of every node from the current state, k_ComputeParticleRot (V/physics.cu:109-205):
+// prevRot -> rot, and the index of the buffer now current into *parityWord.
+__global__ void particleRotKernel(DeviceMesh m, const float* prevRot, float* rot, unsigned* parityWord, unsigned parity) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c == 0) *parityWord = parity;
+    if (c < m.nNodes) particleFrame(c, m.pos, m.nbr, m.active, m.pinned, prevRot, rot);
 }
 
 // Per-tet compliance of the frame, k_ComputeTetAlpha (xpbd_solver.cu:578-587).

@@ -74,7 +74,9 @@ struct Session {
     DBuf<int2> edgeEnds; DBuf<float> edgeRest; DBuf<int> edgeOwner, edgeLive;
     DBuf<int4> bendIJK; DBuf<int> bendSrc, bendLive; DBuf<BendRecord> bendPairs;
     DBuf<int4> tetIds; DBuf<int> tetMeta, tetOwner, edgeSupport; DBuf<float2> tetAlpha, tetStiff;
-    DBuf<unsigned> state;                   // [0] revision the liveness was derived at, [1] barrier counter, [2] status
+    DBuf<unsigned> state;                   // [0] revision the liveness was derived at, [1] barrier counter, [2] status,
+                                            // [3] current particle-frame buffer after the frame
+    DBuf<float> rotA, rotB; int rotParity = 0;   // particle frames, 9 floats per node; rotParity: current buffer
     unsigned* hostState = nullptr;          // pinned mirror of state + cut counters
     // tool / contact
     bool toolArmed = false; ToolPose tool{}, toolFrom{};
@@ -115,6 +117,7 @@ void freePhysics() {
     S.edgeEnds.release(); S.edgeRest.release(); S.bendIJK.release(); S.bendPairs.release(); S.tetIds.release();
     S.tetAlpha.release(); S.tetStiff.release(); S.state.release();
     S.fiberLambda.release(); S.feasTarget.release(); S.needed.release(); S.incOff.release(); S.incTet.release(); S.guardFlags.release();
+    S.rotA.release(); S.rotB.release(); S.rotParity = 0;
     S.volumePasses = 0; S.minVolume = 0.f;
     S.physReady = false; S.toolArmed = false; S.E = S.B = S.T = 0; S.lastH = -1.f;
 }
@@ -181,6 +184,7 @@ DeviceMesh deviceMesh() {
     std::memcpy(m.typeB, S.typeB, sizeof(S.typeB));
     m.fiberLambda = S.fiberLambda.p; m.feasTarget = S.feasTarget.p; m.needed = S.needed.p;
     m.incOff = S.incOff.p; m.incTet = S.incTet.p; m.guardFlags = S.guardFlags.p;
+    m.particleRot[0] = S.rotA.p; m.particleRot[1] = S.rotB.p;
     return m;
 }
 
@@ -311,6 +315,11 @@ LCS_API int LCS_InitPhysics(const PhysicsInitDesc* desc, const float* mass, cons
     CK(S.tetAlpha.alloc(T));
     std::vector<int> zeros((size_t)6 * cc, 0);
     CK(S.edgeSupport.upload(zeros.data(), (size_t)6 * cc, S.stream));
+    std::vector<float> identity((size_t)9 * cc, 0.f);   // particle frames start at the identity (V/physics.cu:258-267)
+    for (int i = 0; i < cc; i++) identity[9 * (size_t)i] = identity[9 * (size_t)i + 4] = identity[9 * (size_t)i + 8] = 1.f;
+    CK(S.rotA.upload(identity.data(), identity.size(), S.stream));
+    CK(S.rotB.upload(identity.data(), identity.size(), S.stream));
+    S.rotParity = 0;
     rc = uploadFrameState();
     if (rc) return rc;
     CK(cudaStreamSynchronize(S.stream));
@@ -521,6 +530,7 @@ LCS_API int LCS_Step(float dt) {
     fc.cut = (S.cutReady && S.toolSet && !S.pressure) ? 1 : 0;
     fc.spinBudget = (long long)((double)S.syncBudgetSeconds * 1e3 * S.clockKHz);
     fc.syncTestExtra = S.syncTestExtra;
+    fc.rotations = 1; fc.rotParity = S.rotParity;
     if (fc.doStrain && h != S.lastH) {
         tetAlphaKernel<<<(S.T + 255) / 256, 256, 0, S.stream>>>(S.T, fc.invH2, S.tetStiff.p, S.tetAlpha.p);
         CK(cudaGetLastError());
@@ -540,7 +550,7 @@ LCS_API int LCS_Step(float dt) {
     int rc = launchFrame(fc);
     if (rc) return rc;
     if (S.profile) { CK(cudaEventRecord(e1, S.stream)); S.events.push_back(e0); S.events.push_back(e1); }
-    CK(cudaMemcpyAsync(S.hostState, S.state.p, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaMemcpyAsync(S.hostState, S.state.p, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
     if (S.sections) {
         S.phaseHost.resize(records);
         CK(cudaMemcpyAsync(S.phaseHost.data(), S.phaseClock.p, records * sizeof(unsigned long long), cudaMemcpyDeviceToHost, S.stream));
@@ -564,10 +574,27 @@ LCS_API int LCS_Step(float dt) {
     if (fc.cut) S.havePrev = true;
     if (S.toolArmed) S.toolFrom = S.tool;
     if (S.hostState[2] != 0u) return LCS_ERR_DEVICE_TIMEOUT;
+    S.rotParity = (int)(S.hostState[3] & 1u);
     return 0;
 }
 
-LCS_API int LCS_Finalize() { return S.physReady ? 0 : -1; }
+// Frames again from the post-sever lattice, then the surface rebuild (plugin_api.cpp:157-165); the
+// surface itself is not built here.
+LCS_API int LCS_Finalize() {
+    if (!S.physReady) return -1;
+    const int p = S.rotParity;
+    particleRotKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(deviceMesh(), p ? S.rotB.p : S.rotA.p, p ? S.rotA.p : S.rotB.p,
+                                                               S.state.p + 3, (unsigned)(p ^ 1));
+    CK(cudaGetLastError());
+    S.rotParity = p ^ 1;
+    return cudaStatus(cudaStreamSynchronize(S.stream));
+}
+LCS_API int GBT_GetParticleRot(float* out9) {
+    if (!S.physReady || !out9) return -1;
+    CK(cudaMemcpyAsync(out9, S.rotParity ? S.rotB.p : S.rotA.p, (size_t)9 * S.N * sizeof(float), cudaMemcpyDeviceToHost, S.stream));
+    return cudaStatus(cudaStreamSynchronize(S.stream));
+}
+LCS_API void* GBT_ParticleRotDevice() { return S.physReady ? (void*)(S.rotParity ? S.rotB.p : S.rotA.p) : nullptr; }
 
 // ---------------------------------------------------------------------------------------------
 // readback
@@ -743,6 +770,7 @@ LCS_API int LCS_StepNoAlloc(float dt) {
     fc.cut = (S.cutReady && S.toolSet && !S.pressure) ? 1 : 0;
     fc.spinBudget = (long long)((double)S.syncBudgetSeconds * 1e3 * S.clockKHz);
     fc.syncTestExtra = S.syncTestExtra;
+    fc.rotations = 1; fc.rotParity = S.rotParity;
 
     // The array keeps whatever the previous call left: the liveness record restarts at "never
     // derived" (word 0 = ~0u), the barrier counter and status at zero, and the compliances are
@@ -768,12 +796,14 @@ LCS_API int LCS_StepNoAlloc(float dt) {
         CK(cudaLaunchCooperativeKernel(ext ? (const void*)frameKernelGridExt : (const void*)frameKernelGrid, dim3(ext ? S.gridBlocksExt : S.gridBlocks),
                                        dim3(kFrameThreads), args, 0, S.stream));
     }
-    unsigned status = 0;
-    CK(cudaMemcpyAsync(&status, state + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    unsigned words[2] = {0u, 0u};   // status, current particle-frame buffer
+    CK(cudaMemcpyAsync(words, state + 2, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
     CK(cudaStreamSynchronize(S.stream));
     if (fc.cut) S.havePrev = true;
     if (S.toolArmed) S.toolFrom = S.tool;
-    return status != 0u ? LCS_ERR_DEVICE_TIMEOUT : 0;
+    if (words[0] != 0u) return LCS_ERR_DEVICE_TIMEOUT;
+    S.rotParity = (int)(words[1] & 1u);
+    return 0;
 }
 
 LCS_API int LCS_SetBarrierTest(int extraArrivals, float budgetSeconds) {

@@ -55,6 +55,9 @@ struct DeviceMesh {
     // the instance (j = i - nodeBase) lives in CTA (j >> logB) & (K - 1), slot
     // ((j >> (logB + logK)) << logB) | (j & (B - 1)); dsm[k] is CTA k's array (a generic pointer)
     float4* const* dsm; int dsmLogB, dsmLogK;
+    // particle frames (9 floats per node, rows of R): two buffers, current and previous, that
+    // alternate on every frame pass
+    float* particleRot[2];
 };
 
 // A node's position: plain device memory, or its slot in the cluster's distributed shared memory.
@@ -79,6 +82,8 @@ struct FrameCoeffs {
     float tensileStrength, bulkDampingOverH, minVolume;
     int friction;                    // contact model 1: tool SDFs, swept contact, Coulomb friction
     float muS, muD, jawThickness, contactRadius;
+    int rotations, rotParity;        // particle frames after the frame (and after a tick that emitted
+                                     // cut points); particleRot[rotParity] holds the current frames
     long long spinBudget;            // grid-barrier spin budget, SM clock cycles
     int syncTestExtra;               // > 0: barriers await arrivals that never come (timeout test)
     int stageNodes;                  // one-CTA kernel: node state staged in shared memory

@@ -191,7 +191,7 @@ EXTENSION_SIGNATURES = (
     ("LCS_SetTetStiffness", (I, P, P), I), ("LCS_GetTetStiffness", (P, P), I), ("LCS_TetCount", (), I), ("LCS_TetColorCount", (), I),
     ("LCS_EdgeColorCount", (), I), ("LCS_EdgeCount", (), I), ("LCS_GetTetIds", (P,), I),
     ("LCS_GetTetColors", (P,), I), ("LCS_GetEdgeColors", (P,), I), ("LCS_GetVelocities", (P,), I),
-    ("LCS_GetBendPairs", (P,), I), ("LCS_GetVoxelCutMask", (P,), I),
+    ("LCS_GetBendPairs", (P,), I), ("LCS_GetVoxelCutMask", (P,), I), ("GBT_GetParticleRot", (P,), I),
 )
 UNIFIED_SIGNATURES = (
     ("LCS_PressureBladeAbiVersion", (), I), ("LCS_SetPressureBlade", (P,), I),
@@ -446,6 +446,19 @@ class PlainTissue(_Session):
         self.check("LCS_GetNbrIdx", pointer(out))
         return out
 
+    def particle_frames(self):
+        """Current particle frames, (nodes, 3, 3) float32: R with column k the world direction of the
+        node's lattice axis k (physics_particle_rot, V/physics.cu:414)."""
+        n = len(self.grid.positions)
+        if not self.reference:
+            out = np.empty((n, 3, 3), dtype=np.float32)
+            self.check("GBT_GetParticleRot", pointer(out))
+            return out
+        # a reference build keeps them in device memory behind its physics module's accessor
+        accessor = getattr(self.dll, "_Z20physics_particle_rotv")
+        accessor.restype = ct.c_void_p
+        return _device_floats(accessor(), 9 * n).reshape(n, 3, 3)
+
     def bend_alive(self):
         out = np.empty(len(self.grid.positions) * 15 * 8, dtype=np.int32)
         self.check("LCS_GetBendPairs", pointer(out))
@@ -478,6 +491,17 @@ class PlainTissue(_Session):
             raise RuntimeError("Non-finite native state; simulation stopped")
         return Observation(nodes, self.neighbors(), np.zeros(len(nodes), np.int32), np.zeros(3), 0.0, 0, 0.0,
                            np.zeros(10, np.float32), np.zeros(3, np.float32))
+
+
+def _device_floats(address, count):
+    """Copy `count` float32 values at a CUDA device address (current device) to a host array."""
+    import torch
+
+    class _View:
+        __cuda_array_interface__ = {"shape": (count,), "typestr": "<f4", "data": (int(address), True), "version": 2}
+
+    torch.cuda.synchronize()
+    return torch.as_tensor(_View(), device="cuda").cpu().numpy()
 
 
 def blade_sweep(prev_start, prev_end, start, end, thickness=0.02):

@@ -62,8 +62,10 @@ LCS_API int LCS_ContactModelVersion(void);      /* = 28, plugin_api.cpp:225 */
 
 /* ---- per-frame control (plugin_api.cpp:103, 125-166, 145-155, 198-201, 210-214, 263) ---------- */
 LCS_API int LCS_SetGravity(float gx, float gy, float gz);           /* physics_set_gravity */
-LCS_API int LCS_Step(float dt);                                      /* physics_step: N substeps + ribbon ticks */
-LCS_API int LCS_Finalize(void);                                      /* frame commit (no surface rebuild here) */
+/* physics_step: N substeps + ribbon ticks, then the particle frames (plugin_api.cpp:125-134); a tick
+ * that emitted cut points before the last substep is followed by fresh frames (V/physics.cu:368-379) */
+LCS_API int LCS_Step(float dt);
+LCS_API int LCS_Finalize(void);            /* particle frames from the post-sever lattice (plugin_api.cpp:157-165); no surface rebuild */
 LCS_API void LCS_SetTool(const CutToolDesc* tool);                   /* cut_set_tool */
 LCS_API int LCS_DetectCut(void);                                     /* cut_detect: swept quad + sever */
 LCS_API void LCS_SetPressureCutMode(int enabled);                    /* pressure mode: detection off here */
@@ -98,6 +100,12 @@ LCS_API int LCS_EdgeColorCount(void);            /* xpbd_color_count (xpbd_solve
 LCS_API int LCS_EdgeCount(void);                 /* xpbd_get_edge_count (xpbd_solver.h:183) */
 LCS_API int LCS_GetTetIds(int* out4T);           /* xpbd_readback_tet_ids (xpbd_solver.h:208): storage order */
 LCS_API int LCS_GetVelocities(float* out3N);     /* xpbd_get_velocities (xpbd_solver.h:174) */
+/* physics_particle_rot (V/physics.h:66, V/physics.cu:414): the current particle frames, 9 floats per
+ * node (rows of R, RotGpu V/cut.cuh:67).  GBT_GetParticleRot copies them to the host; the device
+ * pointer of GBT_ParticleRotDevice stays valid until the next LCS_Step / LCS_Finalize (the frames
+ * alternate between two buffers). */
+LCS_API int GBT_GetParticleRot(float* out9N);
+LCS_API void* GBT_ParticleRotDevice(void);
 
 /* ---- extensions (no counterpart in the reference ABI) ------------------------------------------ */
 /* Per-tet material: mu*V and kappa*V of every tet in storage order (the order of LCS_GetTetIds);

@@ -14,7 +14,8 @@
 // inside a colour does not change results); it is also the timed CPU baseline.
 //
 // Reference files followed ("V/" = endoscopic_tissue/native/vendor/cuda/):
-//   V/physics.cu:214-315 (physics_init), 317-329 (gravity), 331-394 (physics_step)
+//   V/physics.cu:214-315 (physics_init), 317-329 (gravity), 331-394 (physics_step),
+//     109-205 + 399-411 particle frames (frames_oracle.inc)
 //   V/xpbd/xpbd_solver.cu:393-412 predict, 429-466 liveness, 469-479 tet edge support,
 //     484-524 edges, 534-573 bending, 578-587 tet alpha, 749-829 tets, 871-919 velocity,
 //     1049-1123 CCD capsule/jaw contact, 1204-1279 edge colouring, 1332-1400 bend colouring,
@@ -156,6 +157,7 @@ struct Session {
     Real typeB[6][3][3]; std::vector<Real> muV, kappaV, aDev, aHyd;
     std::vector<int> edgeSupport;             // [6N]
     std::vector<Real> invMass;
+    std::vector<Real> particleRot, particleRotPrev;   // [9N] particle frames, rows of R
     bool livenessStale = true; unsigned livenessRevision = 0xffffffffu;
     // frame
     bool frameReady = false; Real h = 0, alphaTilde = 0, velScale = 1, betaGammaHS = 0, alphaB = 0, betaGammaHB = 0;
@@ -182,6 +184,7 @@ struct Session {
 static Session S;
 
 static int cid(int x, int y, int z) { return x + (S.dx + 1) * (y + (S.dy + 1) * z); }
+#include "frames_oracle.inc"
 
 // ---------------------------------------------------------------------------------------------
 // greedy colouring: first free colour (< 64) not used by any member vertex (xpbd_solver.cu:1213-1230)
@@ -432,6 +435,7 @@ API int LCS_InitPhysics(const PhysicsInitDesc* desc, const float* mass, const in
     S.jawLambda.assign(cc, 0); S.shaftLambda.assign(cc, 0);
     rc = buildTets();
     if (rc) return rc;
+    resetParticleFrames();   // identity frames (V/physics.cu:258-267)
     S.physReady = true;
     S.livenessStale = true;
     return 0;
@@ -1203,12 +1207,22 @@ API int LCS_Step(float dt) {
     for (int n = 0; n < N; n++) {
         rc = substep();
         if (rc) return rc;
-        if (S.cutReady) ribbonTick();
+        if (S.cutReady) {
+            const unsigned before = S.cutPoints;   // cut_surface_revision (V/cut.cu:1259-1262)
+            ribbonTick();
+            if (S.cutPoints != before && n + 1 < N) computeParticleFrames();   // V/physics.cu:368-379
+        }
     }
+    computeParticleFrames();   // LCS_Step's closing frames (plugin_api.cpp:125-134)
     if (S.profile) S.stepMs.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
     return 0;
 }
-API int LCS_Finalize() { return S.physReady ? 0 : -1; }
+// plugin_api.cpp:157-165: frames from the post-sever lattice; the surface rebuild is not restated
+API int LCS_Finalize() {
+    if (!S.physReady) return -1;
+    computeParticleFrames();
+    return 0;
+}
 API int LCS_GetCornerPos(float* out) {
     if (!S.reconReady || !out) return -1;
     for (int i = 0; i < S.N; i++) { out[3 * i] = (float)S.pos[i].x; out[3 * i + 1] = (float)S.pos[i].y; out[3 * i + 2] = (float)S.pos[i].z; }
