@@ -212,24 +212,21 @@ def test_lost_axes(oracle_libs):
 # ---------------------------------------------------------------------------------------------
 # GPU
 # ---------------------------------------------------------------------------------------------
-def frames_run(workload, lib, steps, every, launch_mode=None, step_only=False):
+def frames_run(workload, lib, steps, every, launch_mode=None):
     s = workload.open(lib)
     try:
         if launch_mode is not None:
-            s.check("LCS_SetLaunchMode", launch_mode)
+            s.dll.LCS_SetLaunchMode(launch_mode)
         out = []
         for k in range(steps):
             detect = workload.command(s, k)
-            if step_only:   # the closing frames of LCS_Step itself, before any LCS_Finalize
-                s.check("LCS_Step", s.dt)
-            else:
-                s.step(detect_cut=detect)
+            s.step(detect_cut=detect)
             if (k + 1) % every == 0:
                 out.append(dict(rot=s.particle_frames(), dbg=s.cut_debug()[15:17].copy()))
         return out
     finally:
         if launch_mode is not None:
-            s.check("LCS_SetLaunchMode", 0)
+            s.dll.LCS_SetLaunchMode(0)
         s.close()
 
 
@@ -244,15 +241,64 @@ def test_gpu_frames_bit_exact_c1(gpu_lib, oracle_libs, mode):
     assert np.abs(cpu[-1]["rot"] - np.eye(3)).max() > 1e-4
 
 
+def ticking_blade(workload):
+    """A static blade segment along z just below the second node layer from the top: the first
+    frame's sag carries lattice edges across it, so ribbon ticks inside LCS_Step emit cut points."""
+    from genesis_tissue_simulation_gb300.native_backend import blade_sweep
+    g = workload.grid
+    act = g.active != 0
+    lo, hi = g.positions[act].min(axis=0), g.positions[act].max(axis=0)
+    y = float(hi[1]) - 0.2 - 0.002
+    x = 0.5 * float(lo[0] + hi[0]) + 0.013
+    start, end = (x, y, float(lo[2]) - 0.2), (x, y, float(hi[2]) + 0.2)
+    return blade_sweep(start, end, start, end)
+
+
+def tick_run(lib, steps=6):
+    w = W.make("c3", steps=steps, scale=SMALL)
+    s = w.open(lib)
+    try:
+        s.set_blade(ticking_blade(w))
+        out = []
+        for _ in range(steps):
+            s.check("LCS_Step", s.dt)
+            out.append(dict(rot=s.particle_frames(), dbg=s.cut_debug()[15:17].copy(), nbr=s.neighbors()))
+        passes = int(s.dll.ORC_FramePasses()) if hasattr(s.dll, "ORC_FramePasses") else None
+        return out, passes
+    finally:
+        s.close()
+
+
+def test_oracle_tick_runs_mid_frame_pass(oracle_libs):
+    """The ticking blade scenario emits cut points inside LCS_Step before the last substep, so the
+    oracle runs more than one frame pass per step (the mid-frame pass, V/physics.cu:368-379)."""
+    import ctypes as c
+    dll = c.CDLL(str(oracle_libs[0]))
+    dll.ORC_FramePasses.restype = c.c_longlong
+    before = dll.ORC_FramePasses()
+    out, _ = tick_run(oracle_libs[0], steps=2)
+    assert out[0]["dbg"][1] > 0
+    assert dll.ORC_FramePasses() - before > 2
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("step_only", [False, True])
-def test_gpu_frames_bit_exact_cut(gpu_lib, oracle_libs, step_only):
-    """A blade severs the lattice: frames after ticks that emitted cut points (mid-frame), at the end
-    of LCS_Step and after LCS_Finalize, bit for bit.  ``step_only`` drives LCS_Step alone, so the
-    frames read are the step's own closing frames."""
+def test_gpu_frames_bit_exact_tick(gpu_lib, oracle_libs):
+    """Frames at the end of LCS_Step after ribbon ticks that emitted cut points mid-frame."""
+    gpu, _ = tick_run(gpu_lib)
+    cpu, _ = tick_run(oracle_libs[0])
+    assert cpu[0]["dbg"][1] > 0, "the ticks emitted no cut points"
+    for a, b in zip(gpu, cpu):
+        assert np.array_equal(a["dbg"], b["dbg"]) and np.array_equal(a["nbr"], b["nbr"])
+        assert np.array_equal(a["rot"], b["rot"]), float(np.abs(a["rot"] - b["rot"]).max())
+
+
+@pytest.mark.gpu
+def test_gpu_frames_bit_exact_quad_cut(gpu_lib, oracle_libs):
+    """The swept blade of the rod phase severs the lattice (LCS_DetectCut); LCS_Finalize's frames
+    follow the post-sever lattice, bit for bit."""
     w = W.make("c3", steps=40, scale=SMALL)
-    gpu = frames_run(w, gpu_lib, 40, 5, step_only=step_only)
-    cpu = frames_run(w, oracle_libs[0], 40, 5, step_only=step_only)
+    gpu = frames_run(w, gpu_lib, 40, 5)
+    cpu = frames_run(w, oracle_libs[0], 40, 5)
     assert cpu[-1]["dbg"][1] > 0, "the blade emitted no cut points"
     for a, b in zip(gpu, cpu):
         assert np.array_equal(a["dbg"], b["dbg"])
@@ -279,8 +325,10 @@ def _reference_frame_pass(session):
     torch.cuda.synchronize()
 
 
-def _reference_session(grid, lib, blade=False):
-    return PlainTissue(grid, dt=1 / 60, substeps=20, ks=1e6, young_pa=6000.0, strain_damping_s=0.04, dll_path=lib, reference=True)
+def _pair_session(grid, lib, reference):
+    """The configuration the reference parity tests drive both libraries with."""
+    return PlainTissue(grid, dt=1 / 60, substeps=20, ks=1e6, young_pa=6000.0, poisson=0.25, strain_damping_s=0.04,
+                       dll_path=lib, reference=reference)
 
 
 @pytest.mark.gpu
@@ -300,9 +348,9 @@ def test_oracle_frames_against_reference_build(reference_lib, oracle_libs):
     g2 = g.__class__(**{**vars(g), "active": active})
     rng = np.random.default_rng(11)
     centre = g.positions.mean(axis=0)
-    ref = _reference_session(g2, reference_lib)
+    ref = _pair_session(g2, reference_lib, True)
     try:
-        with open_session(oracle_libs[0], g2) as orc:
+        with _pair_session(g2, oracle_libs[0], False) as orc:
             view = _reference_positions(ref)
             errors = []
             for k, (axis, angle) in enumerate(((0.3, 1.0, -0.5), 0.5), ((1.0, 0.0, 0.2), 1.4), ((0.0, 0.2, 1.0), -0.8)):
@@ -333,9 +381,9 @@ def test_oracle_frames_after_blade_match_reference(reference_lib, oracle_libs):
     w = W.make("c3", steps=10, scale=SMALL)
     sessions = []
     try:
-        ref = _reference_session(w.grid, reference_lib)
+        ref = _pair_session(w.grid, reference_lib, True)
         sessions.append(ref)
-        orc = open_session(oracle_libs[0], w.grid)
+        orc = _pair_session(w.grid, oracle_libs[0], False)
         sessions.append(orc)
         for s in (ref, orc):
             s.set_gravity(0.0, -981.0, 0.0)
