@@ -353,7 +353,7 @@ def test_oracle_frames_against_reference_build(reference_lib, oracle_libs):
         with _pair_session(g2, oracle_libs[0], False) as orc:
             view = _reference_positions(ref)
             errors = []
-            for k, (axis, angle) in enumerate(((0.3, 1.0, -0.5), 0.5), ((1.0, 0.0, 0.2), 1.4), ((0.0, 0.2, 1.0), -0.8)):
+            for axis, angle in (((0.3, 1.0, -0.5), 0.5), ((1.0, 0.0, 0.2), 1.4), ((0.0, 0.2, 1.0), -0.8)):
                 Q = rotation(axis, angle)
                 pos = ((g.positions - centre) @ Q.T + centre + rng.normal(scale=0.02, size=g.positions.shape)).astype(np.float32)
                 view.copy_(torch.from_numpy(pos).cuda())
