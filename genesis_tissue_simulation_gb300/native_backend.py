@@ -498,7 +498,7 @@ def _device_floats(address, count):
     import torch
 
     class _View:
-        __cuda_array_interface__ = {"shape": (count,), "typestr": "<f4", "data": (int(address), True), "version": 2}
+        __cuda_array_interface__ = {"shape": (count,), "typestr": "<f4", "data": (int(address), False), "version": 2}
 
     torch.cuda.synchronize()
     return torch.as_tensor(_View(), device="cuda").cpu().numpy()
