@@ -369,6 +369,44 @@ def adjoint_measurement(lib, reps=3):
             "gradients": "theta [98,304] and capsule path [51, 6]", "substeps": frames * substeps}
 
 
+def frames_measurement(lib, calls=50, warmup=3):
+    """Particle frames (k_ComputeParticleRot) on the C2 lattice after 3 sagging frames.  LCS_Finalize
+    runs one frame pass (its own launch) and synchronises: wall clock per call, median.  The device
+    time of the kernel and its DRAM bytes come from the committed ncu summary."""
+    from genesis_tissue_simulation_gb300 import workloads as W
+
+    w = W.make("c2", steps=3)
+    s = w.open(lib)
+    try:
+        w.run(s, steps=3)
+        times = []
+        for k in range(calls + warmup):
+            t0 = time.perf_counter()
+            s.check("LCS_Finalize")
+            if k >= warmup:
+                times.append(time.perf_counter() - t0)
+        R = s.particle_frames().astype(np.float64)
+    finally:
+        s.close()
+    gram_err = float(np.abs(np.einsum("nji,njk->nik", R, R) - np.eye(3)).max())
+    nodes = len(w.grid.positions)
+    ms = 1e3 * float(np.median(times))
+    out = {"workload": f"c2 lattice, {nodes:,} nodes ({int((w.grid.active != 0).sum()):,} active), after 3 frames",
+           "ms_per_pass_wall": ms, "nodes_per_s_wall": nodes / (ms * 1e-3), "algorithmic_bytes_per_node": 120,
+           "timing": f"wall clock around LCS_Finalize (launch + kernel + stream sync), median of {calls}",
+           "max_orthonormality_error": gram_err}
+    path = ROOT / "profiles" / "ncu_particle_frames_c2.md"
+    if path.exists():
+        for line in path.read_text().splitlines():
+            if line.startswith("kernel_us_per_launch:"):
+                us = float(line.split(":", 1)[1].split()[0])
+                out["kernel_us_ncu"] = us
+                out["achieved_gbs_ncu"] = 120 * nodes / (us * 1e-6) / 1e9
+            if line.startswith("traffic_bytes_per_launch:"):
+                out["traffic"] = float(line.split(":", 1)[1].split()[0])
+    return out
+
+
 def main():
     parser = argparse.ArgumentParser()
     parser.add_argument("--gpus", type=int, default=1)
@@ -380,7 +418,7 @@ def main():
     parser.add_argument("--no-batched", action="store_true")
     parser.add_argument("--no-adjoint", action="store_true")
     parser.add_argument("--no-workloads", action="store_true", help="skip the C1 and C3 lines")
-    parser.add_argument("--only", default="all", choices=("all", "batched", "adjoint"),
+    parser.add_argument("--only", default="all", choices=("all", "batched", "adjoint", "frames"),
                         help="run one section alone and print its JSON object (for profiling)")
     parser.add_argument("--batched-frames", type=int, default=20)
     args = parser.parse_args()
@@ -405,6 +443,7 @@ def main():
     lib = native_build.build()
     if args.only != "all":   # one section alone (profiling runs): its JSON object, no bench line
         section = (batched_measurement(lib, args.batched_frames, max(args.warmup, 3)) if args.only == "batched"
+                   else frames_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1)) if args.only == "frames"
                    else adjoint_measurement(lib, reps=max(args.steps, 1)))
         print(json.dumps({"only": args.only, **section}), flush=True)
         return
@@ -493,6 +532,8 @@ def main():
         line["workloads"] = {"c1": workload_measurement(lib, "c1", 100, 5), "c3": workload_measurement(lib, "c3", 30, 3)}
     if not args.no_adjoint:
         line["adjoint"] = adjoint_measurement(lib)
+    if not args.no_workloads:
+        line["particle_frames"] = frames_measurement(lib)
     if not args.no_batched:
         batched = batched_measurement(lib, args.batched_frames, max(args.warmup, 3))
         batched["roofline"].update(peak=peak, frac=batched["roofline"]["achieved"] / peak, peak_kind=peak_kind)
