@@ -466,7 +466,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
             havePrev = true;
         }
     }
-    if (rotations && fc.firstSubstep + fc.substeps == fc.numSubsteps) {   // LCS_Step's closing frames
+    if (rotations && fc.closingPass && fc.firstSubstep + fc.substeps == fc.numSubsteps) {   // LCS_Step's closing frames
         if (!sync.sync()) return;
         framePass();
     }
@@ -599,12 +599,13 @@ __global__ void __launch_bounds__(kBlockThreads) frameKernelBlockExt(DeviceMesh 
     blockFrame<true>(m, fc, from, to, cp, cu, state);
 }
 
-// Particle frames of every node from the current state, k_ComputeParticleRot (V/physics.cu:109-205):
-// prevRot -> rot, and the index of the buffer now current into *parityWord.
-__global__ void particleRotKernel(DeviceMesh m, const float* prevRot, float* rot, unsigned* parityWord, unsigned parity) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c == 0) *parityWord = parity;
-    if (c < m.nNodes) particleFrame(c, m.pos, m.nbr, m.active, m.pinned, prevRot, rot);
+// One frame pass over every node, k_ComputeParticleRot (V/physics.cu:109-205): frames from
+// particleRot[p] into particleRot[p ^ 1], p = *parityWord when given (the parity a frame kernel left
+// on the device), else `parity`.
+__global__ void particleRotKernel(DeviceMesh m, const unsigned* parityWord, int parity) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int p = parityWord ? (int)(*parityWord & 1u) : parity;
+    if (c < m.nNodes) particleFrame(c, m.pos, m.nbr, m.active, m.pinned, m.particleRot[p], m.particleRot[p ^ 1]);
 }
 
 // Per-tet compliance of the frame, k_ComputeTetAlpha (xpbd_solver.cu:578-587).

@@ -32,7 +32,7 @@ constexpr int kClusterThreads = 512, kClusterLogThreads = 9;
 __global__ void frameKernelCluster(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it, int logK);
 __global__ void frameKernelInstances512(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it);
 
-__global__ void particleRotKernel(DeviceMesh m, const float* prevRot, float* rot, unsigned* parityWord, unsigned parity);
+__global__ void particleRotKernel(DeviceMesh m, const unsigned* parityWord, int parity);
 __global__ void tetAlphaKernel(int n, float invH2, const float2* stiff, float2* alpha);
 __global__ void gravityKernel(int n, float gx, float gy, float gz, float4* ext);
 

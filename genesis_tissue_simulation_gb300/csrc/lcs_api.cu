@@ -199,7 +199,10 @@ CutParams cutParams() {
     return c;
 }
 
-int launchFrame(const FrameCoeffs& fc) {
+// The frame kernel; when it runs on one CTA, the closing frame pass follows as a whole-GPU launch
+// (*followUp set), so the host flips the parity the kernel leaves in state[3].
+int launchFrame(const FrameCoeffs& fc, bool* followUp) {
+    *followUp = false;
     DeviceMesh m = deviceMesh();
     CutParams cu = cutParams();
     unsigned* state = S.state.p;
@@ -210,13 +213,21 @@ int launchFrame(const FrameCoeffs& fc) {
     if (single) {
         FrameCoeffs f = fc;
         f.stageNodes = stage ? 1 : 0;
+        f.closingPass = 0;
         const bool ext = fc.guarded || fc.friction;
         (ext ? frameKernelBlockExt : frameKernelBlock)<<<1, kBlockThreads, stage ? stageBytes : 0, S.stream>>>(m, f, S.toolFrom, S.tool, S.cp, cu, state);
         CK(cudaGetLastError());
+        if (fc.rotations) {
+            particleRotKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(m, state + 3, 0);
+            CK(cudaGetLastError());
+            *followUp = true;
+        }
     } else {
         ToolPose from = S.toolFrom, to = S.tool;
         ContactParams cp = S.cp;
-        void* args[] = {&m, (void*)&fc, &from, &to, &cp, &cu, &state};
+        FrameCoeffs f = fc;
+        f.closingPass = 1;
+        void* args[] = {&m, (void*)&f, &from, &to, &cp, &cu, &state};
         const bool ext = fc.guarded || fc.friction;
         CK(cudaLaunchCooperativeKernel(ext ? (const void*)frameKernelGridExt : (const void*)frameKernelGrid, dim3(ext ? S.gridBlocksExt : S.gridBlocks),
                                        dim3(kFrameThreads), args, 0, S.stream));
@@ -547,7 +558,8 @@ LCS_API int LCS_Step(float dt) {
         CK(cudaMemsetAsync(S.phaseClock.p, 0, records * sizeof(unsigned long long), S.stream));
         fc.phaseClock = S.phaseClock.p;
     }
-    int rc = launchFrame(fc);
+    bool followUp = false;
+    int rc = launchFrame(fc, &followUp);
     if (rc) return rc;
     if (S.profile) { CK(cudaEventRecord(e1, S.stream)); S.events.push_back(e0); S.events.push_back(e1); }
     CK(cudaMemcpyAsync(S.hostState, S.state.p, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
@@ -574,7 +586,7 @@ LCS_API int LCS_Step(float dt) {
     if (fc.cut) S.havePrev = true;
     if (S.toolArmed) S.toolFrom = S.tool;
     if (S.hostState[2] != 0u) return LCS_ERR_DEVICE_TIMEOUT;
-    S.rotParity = (int)(S.hostState[3] & 1u);
+    S.rotParity = (int)((S.hostState[3] & 1u) ^ (followUp ? 1u : 0u));
     return 0;
 }
 
@@ -583,8 +595,7 @@ LCS_API int LCS_Step(float dt) {
 LCS_API int LCS_Finalize() {
     if (!S.physReady) return -1;
     const int p = S.rotParity;
-    particleRotKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(deviceMesh(), p ? S.rotB.p : S.rotA.p, p ? S.rotA.p : S.rotB.p,
-                                                               S.state.p + 3, (unsigned)(p ^ 1));
+    particleRotKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(deviceMesh(), nullptr, p);
     CK(cudaGetLastError());
     S.rotParity = p ^ 1;
     return cudaStatus(cudaStreamSynchronize(S.stream));
@@ -787,10 +798,14 @@ LCS_API int LCS_StepNoAlloc(float dt) {
     ToolPose from = S.toolFrom, to = S.tool;
     ContactParams cp = S.cp;
     bool single = S.launchMode == 2 || (S.launchMode == 0 && S.T < 65536 && S.N < 32768);
-    if (single) {
+    if (single) {   // closing frame pass as a whole-GPU launch after the one-CTA frame
+        fc.closingPass = 0;
         (fc.guarded || fc.friction ? frameKernelBlockExt : frameKernelBlock)<<<1, kFrameThreads, 0, S.stream>>>(m, fc, from, to, cp, cu, state);
         CK(cudaGetLastError());
+        particleRotKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(m, state + 3, 0);
+        CK(cudaGetLastError());
     } else {
+        fc.closingPass = 1;
         void* args[] = {&m, (void*)&fc, &from, &to, &cp, &cu, &state};
         const bool ext = fc.guarded || fc.friction;
         CK(cudaLaunchCooperativeKernel(ext ? (const void*)frameKernelGridExt : (const void*)frameKernelGrid, dim3(ext ? S.gridBlocksExt : S.gridBlocks),
@@ -802,7 +817,7 @@ LCS_API int LCS_StepNoAlloc(float dt) {
     if (fc.cut) S.havePrev = true;
     if (S.toolArmed) S.toolFrom = S.tool;
     if (words[0] != 0u) return LCS_ERR_DEVICE_TIMEOUT;
-    S.rotParity = (int)(words[1] & 1u);
+    S.rotParity = (int)((words[1] & 1u) ^ (single ? 1u : 0u));
     return 0;
 }
 

@@ -82,8 +82,9 @@ struct FrameCoeffs {
     float tensileStrength, bulkDampingOverH, minVolume;
     int friction;                    // contact model 1: tool SDFs, swept contact, Coulomb friction
     float muS, muD, jawThickness, contactRadius;
-    int rotations, rotParity;        // particle frames after the frame (and after a tick that emitted
-                                     // cut points); particleRot[rotParity] holds the current frames
+    int rotations, rotParity;        // particle frames after a tick that emitted cut points and, with
+                                     // closingPass, after the frame; particleRot[rotParity] is current
+    int closingPass;                 // 0: the host launches the closing frame pass on the whole GPU
     long long spinBudget;            // grid-barrier spin budget, SM clock cycles
     int syncTestExtra;               // > 0: barriers await arrivals that never come (timeout test)
     int stageNodes;                  // one-CTA kernel: node state staged in shared memory
