@@ -40,11 +40,6 @@ GBT_HD Rows3 inverseTranspose(const Rows3& m) {
     return t;
 }
 
-__device__ __forceinline__ bool sameBits(f3 a, f3 b) {
-    return __float_as_uint(a.x) == __float_as_uint(b.x) && __float_as_uint(a.y) == __float_as_uint(b.y) &&
-           __float_as_uint(a.z) == __float_as_uint(b.z);
-}
-
 __device__ __forceinline__ void storeRows(float* out, const Rows3& R) {
     out[0] = R.r0.x; out[1] = R.r0.y; out[2] = R.r0.z;
     out[3] = R.r1.x; out[4] = R.r1.y; out[5] = R.r1.z;
@@ -118,18 +113,12 @@ static __device__ __noinline__ void particleFrame(int c, const float4* pos, cons
     M.r1 = mk(axis[0].y, axis[1].y, axis[2].y);
     M.r2 = mk(axis[0].z, axis[1].z, axis[2].z);
     if (det3(M) <= 1e-4f) { storeRows(out, R); return; }
-    // 16 Higham steps; an iterate that reproduces itself bit for bit is a fixed point of the
-    // remaining steps, so the loop may stop there with the same result
     Rows3 P = M;
     for (int it = 0; it < 16; it++) {
         const Rows3 T = inverseTranspose(P);
-        Rows3 Q;
-        Q.r0 = (P.r0 + T.r0) * 0.5f;
-        Q.r1 = (P.r1 + T.r1) * 0.5f;
-        Q.r2 = (P.r2 + T.r2) * 0.5f;
-        const bool same = sameBits(Q.r0, P.r0) && sameBits(Q.r1, P.r1) && sameBits(Q.r2, P.r2);
-        P = Q;
-        if (same) break;
+        P.r0 = (P.r0 + T.r0) * 0.5f;
+        P.r1 = (P.r1 + T.r1) * 0.5f;
+        P.r2 = (P.r2 + T.r2) * 0.5f;
     }
     const f3 c0 = mk(P.r0.x, P.r1.x, P.r2.x), c1 = mk(P.r0.y, P.r1.y, P.r2.y), c2 = mk(P.r0.z, P.r1.z, P.r2.z);
     float ortho = fmaxf(fmaxf(fabsf(dot(c0, c0) - 1.f), fabsf(dot(c1, c1) - 1.f)), fabsf(dot(c2, c2) - 1.f));
