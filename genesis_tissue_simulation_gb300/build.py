@@ -22,7 +22,8 @@ CSRC = PACKAGE_DIR / "csrc"
 BUILD = CSRC / "_build"
 INCLUDE = PACKAGE_DIR.parent / "include"
 LIBRARY = BUILD / "libgbtissue.so"
-SOURCES = ("frame_kernels.cu", "lcs_api.cu", "mesh_build.cu", "batch_api.cu", "adjoint_kernels.cu", "adjoint_api.cu")
+SOURCES = ("frame_kernels.cu", "lcs_api.cu", "mesh_build.cu", "batch_api.cu", "adjoint_kernels.cu", "adjoint_api.cu",
+           "surface_kernels.cu")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -19,6 +19,7 @@
 #include "frame_kernels.h"
 #include "mesh_build.h"
 #include "session_view.h"
+#include "surface.h"
 #include "../../include/gbtissue.h"
 
 using namespace gbt;
@@ -77,6 +78,12 @@ struct Session {
     DBuf<unsigned> state;                   // [0] revision the liveness was derived at, [1] barrier counter, [2] status,
                                             // [3] current particle-frame buffer after the frame
     DBuf<float> rotA, rotB; int rotParity = 0;   // particle frames, 9 floats per node; rotParity: current buffer
+    // dual-contouring surface (LCS_Init's voxel tables); rebuilt at LCS_Init and in LCS_Finalize
+    bool surfaceReady = false, haveRestSurface = false;
+    int nVox = 0, nSurfVox = 0, nSurfEdges = 0, triCapacity = 0, qefIters = 8, surfBlocks = 0;
+    DBuf<int> voxelCorner, isectOff, isectCnt, surfVox, tri, nrmFixed, blockTotal;
+    DBuf<IsectRec> isect; DBuf<int4> surfEdges; DBuf<float4> fp, fpRest, nrm, outAux; DBuf<float> outPos, outNrm;
+    DBuf<unsigned> surfSync, triCount;
     unsigned* hostState = nullptr;          // pinned mirror of state + cut counters
     // tool / contact
     bool toolArmed = false; ToolPose tool{}, toolFrom{};
@@ -124,6 +131,10 @@ void freePhysics() {
 void freeAll() {
     freePhysics();
     S.pos.release(); S.rest.release();
+    for (auto* b : {&S.voxelCorner, &S.isectOff, &S.isectCnt, &S.surfVox, &S.tri, &S.nrmFixed, &S.blockTotal}) b->release();
+    S.isect.release(); S.surfEdges.release(); S.fp.release(); S.fpRest.release(); S.nrm.release(); S.outAux.release();
+    S.outPos.release(); S.outNrm.release(); S.surfSync.release(); S.triCount.release();
+    S.surfaceReady = S.haveRestSurface = false;
     S.reconReady = false;
 }
 
@@ -145,6 +156,84 @@ int ensureStream() {
     if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, S.device) == cudaSuccess && khz > 0) S.clockKHz = khz;
     S.gridBlocks = std::max(1, perSm) * S.smCount;
     S.gridBlocksExt = std::max(1, perSmExt) * S.smCount;
+    int perSmSurface = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSmSurface, surfaceKernel, kSurfaceThreads, 0));
+    S.surfBlocks = std::max(1, perSmSurface) * S.smCount;
+    return 0;
+}
+
+// One rebuild of the dual-contouring surface from the live lattice (recon_build_static,
+// V/dc_recon.cu:507-541).  With the cut buffers present, severed crossings are rebuilt from the
+// current particle frames and cut voxels keep their QEF point.
+int buildSurface() {
+    if (!S.surfaceReady) return 0;
+    SurfaceMesh m{};
+    m.dx = S.dx; m.dy = S.dy; m.dz = S.dz;
+    m.nSurfVox = S.nSurfVox; m.nEdges = S.nSurfEdges; m.triCapacity = S.triCapacity; m.qefIters = S.qefIters;
+    m.haveRest = S.haveRestSurface ? 1 : 0;
+    m.cutActive = S.cutReady ? 1 : 0;
+    m.surfVox = S.surfVox.p; m.voxelCorner = S.voxelCorner.p; m.isectOff = S.isectOff.p; m.isectCnt = S.isectCnt.p;
+    m.isect = S.isect.p; m.edges = S.surfEdges.p; m.pos = S.pos.p; m.rest = S.rest.p;
+    if (S.cutReady) {
+        m.nbr = S.nbr.p; m.rot = S.rotParity ? S.rotB.p : S.rotA.p; m.cutT = S.edgeCutT.p; m.cutMask = S.cutMask.p;
+    }
+    m.fp = S.fp.p; m.fpRest = S.fpRest.p; m.nrmFixed = S.nrmFixed.p; m.nrm = S.nrm.p;
+    m.tri = S.tri.p; m.triCount = S.triCount.p; m.blockTotal = S.blockTotal.p;
+    m.outPos = S.outPos.p; m.outNrm = S.outNrm.p; m.outAux = S.outAux.p;
+    unsigned* sync = S.surfSync.p;
+    long long budget = (long long)((double)S.syncBudgetSeconds * 1e3 * S.clockKHz);
+    CK(cudaMemsetAsync(sync, 0, 2 * sizeof(unsigned), S.stream));
+    void* args[] = {&m, &sync, &budget};
+    CK(cudaLaunchCooperativeKernel((const void*)surfaceKernel, dim3(S.surfBlocks), dim3(kSurfaceThreads), args, 0, S.stream));
+    CK(cudaMemcpyAsync(S.hostState + 7, sync + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    return S.hostState[7] != 0u ? LCS_ERR_DEVICE_TIMEOUT : 0;
+}
+
+// Voxel tables of LCS_Init, checked so that every index the surface kernel follows stays inside
+// its array; returns 0 or -1001.
+int uploadSurface(const ReconInitDescAbi* d, const int* voxelCorner, const int* isectOffset, const int* isectCount,
+                  const IsectAbi* isect, const int* surfaceEdges) {
+    const int V = d->voxelCount, I = d->isectCount, E = d->surfaceEdgeCount, N = S.N;
+    const int nx = S.dx + 1, nxy = (S.dx + 1) * (S.dy + 1);
+    if (V != S.dx * S.dy * S.dz || I < 0 || E < 0 || d->qefIters < 0 || d->qefIters > 1000) return -1001;
+    if (!voxelCorner || !isectOffset || !isectCount || (I > 0 && !isect) || (E > 0 && !surfaceEdges)) return -1001;
+    for (size_t k = 0; k < (size_t)8 * V; k++) if (voxelCorner[k] < 0 || voxelCorner[k] >= N) return -1001;
+    std::vector<int> surf;
+    for (int v = 0; v < V; v++) {
+        const int o = isectOffset[v], c = isectCount[v];
+        if (c < 0 || c > 12 || o < 0 || (long long)o + c > I) return -1001;
+        if (c > 0) surf.push_back(v);
+    }
+    for (int i = 0; i < I; i++) {
+        const int a = isect[i].a, b = isect[i].b, dd = std::abs(b - a);
+        if (a < 0 || a >= N || b < 0 || b >= N || !(dd == 1 || dd == nx || dd == nxy)) return -1001;
+    }
+    std::vector<int4> edges(E);
+    for (int e = 0; e < E; e++) {
+        const int* r = surfaceEdges + 8 * (size_t)e;
+        const int axis = r[0], x = r[1], y = r[2], z = r[3], inA = r[4];
+        const bool okx = axis == 0 ? (x >= 0 && x < S.dx) : (x >= 1 && x < S.dx);
+        const bool oky = axis == 1 ? (y >= 0 && y < S.dy) : (y >= 1 && y < S.dy);
+        const bool okz = axis == 2 ? (z >= 0 && z < S.dz) : (z >= 1 && z < S.dz);
+        if (axis < 0 || axis > 2 || !okx || !oky || !okz || (inA != 0 && inA != 1)) return -1001;
+        edges[e] = make_int4(axis | (inA << 2), x, y, z);
+    }
+    S.nVox = V; S.nSurfVox = (int)surf.size(); S.nSurfEdges = E; S.triCapacity = d->triCapacity; S.qefIters = d->qefIters;
+    CK(S.voxelCorner.upload(voxelCorner, (size_t)8 * V, S.stream));
+    CK(S.isectOff.upload(isectOffset, V, S.stream));
+    CK(S.isectCnt.upload(isectCount, V, S.stream));
+    CK(S.surfVox.upload(surf.data(), surf.size(), S.stream));
+    CK(S.isect.upload((const IsectRec*)isect, I, S.stream));
+    CK(S.surfEdges.upload(edges.data(), E, S.stream));
+    const size_t idx = (size_t)3 * S.triCapacity;
+    CK(S.fp.alloc(V)); CK(S.fpRest.alloc(V)); CK(S.nrm.alloc(V)); CK(S.nrmFixed.alloc((size_t)3 * V));
+    CK(cudaMemsetAsync(S.fp.p, 0, (size_t)V * sizeof(float4), S.stream));
+    CK(cudaMemsetAsync(S.fpRest.p, 0, (size_t)V * sizeof(float4), S.stream));
+    CK(cudaMemsetAsync(S.nrm.p, 0, (size_t)V * sizeof(float4), S.stream));
+    CK(S.tri.alloc(idx)); CK(S.outPos.alloc(3 * idx)); CK(S.outNrm.alloc(3 * idx)); CK(S.outAux.alloc(idx));
+    CK(S.blockTotal.alloc(S.surfBlocks)); CK(S.surfSync.alloc(2)); CK(S.triCount.alloc(1));
+    CK(cudaMemsetAsync(S.triCount.p, 0, sizeof(unsigned), S.stream));
     return 0;
 }
 
@@ -242,7 +331,6 @@ int launchFrame(const FrameCoeffs& fc, bool* followUp) {
 // =============================================================================================
 LCS_API int LCS_Init(const ReconInitDescAbi* desc, const float* cornerPos, const int* voxelCorner, const int* voxelIsectOffset,
                      const int* voxelIsectCount, const void* isect, const void* surfaceEdges) {
-    (void)voxelCorner; (void)voxelIsectOffset; (void)voxelIsectCount; (void)surfaceEdges;
     freeAll();
     if (!desc) return -1000;
     if (desc->voxelCount <= 0 || desc->cornerCount <= 0 || desc->triCapacity <= 0 || !cornerPos) return -1001;
@@ -261,8 +349,17 @@ LCS_API int LCS_Init(const ReconInitDescAbi* desc, const float* cornerPos, const
         S.skinT[directedSlot(is[i].a, is[i].b)] = is[i].t;
         S.skinT[directedSlot(is[i].b, is[i].a)] = 1.f - is[i].t;
     }
-    CK(cudaStreamSynchronize(S.stream));
     S.reconReady = true;
+    if (voxelCorner) {   // the static surface of the rest lattice, then its rest snapshot (V/dc_recon.cu:612-621)
+        rc = uploadSurface(desc, voxelCorner, voxelIsectOffset, voxelIsectCount, is, (const int*)surfaceEdges);
+        if (rc) { freeAll(); return rc; }
+        S.surfaceReady = true;
+        rc = buildSurface();
+        if (rc) { freeAll(); return rc; }
+        CK(cudaMemcpyAsync(S.fpRest.p, S.fp.p, (size_t)S.nVox * sizeof(float4), cudaMemcpyDeviceToDevice, S.stream));
+        S.haveRestSurface = true;
+    }
+    CK(cudaStreamSynchronize(S.stream));
     return 0;
 }
 
@@ -598,6 +695,44 @@ LCS_API int LCS_Finalize() {
     particleRotKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(deviceMesh(), nullptr, p);
     CK(cudaGetLastError());
     S.rotParity = p ^ 1;
+    return buildSurface();
+}
+// Surface readback (plugin_api.cpp:84-100): a non-indexed triangle soup, 3 vertices per triangle.
+LCS_API int LCS_GetSurfaceCounts(int* vertexCount, int* indexCount) {
+    if (!S.surfaceReady) return -1;
+    CK(cudaMemcpyAsync(S.hostState + 7, S.triCount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    if (vertexCount) *vertexCount = (int)S.hostState[7];
+    if (indexCount) *indexCount = (int)S.hostState[7];
+    return 0;
+}
+LCS_API int LCS_GetSurface(float* outPos3, float* outNrm3, int* outIdx) {
+    if (!S.surfaceReady) return -1;
+    CK(cudaMemcpyAsync(S.hostState + 7, S.triCount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    const size_t n = S.hostState[7];
+    if (outPos3 && n) CK(cudaMemcpyAsync(outPos3, S.outPos.p, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, S.stream));
+    if (outNrm3 && n) CK(cudaMemcpyAsync(outNrm3, S.outNrm.p, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    if (outIdx) for (size_t i = 0; i < n; i++) outIdx[i] = (int)i;
+    return 0;
+}
+// Voxel ids of the triangles (3 per triangle, the order of LCS_GetSurface): the indexed form of the
+// soup, whose vertex v is voxel v's feature point (recon_tri, V/dc_recon.cu:693).
+LCS_API int GBT_GetSurfaceTriangles(int* out3T) {
+    if (!S.surfaceReady || !out3T) return -1;
+    CK(cudaMemcpyAsync(S.hostState + 7, S.triCount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    const size_t n = S.hostState[7];
+    if (n) CK(cudaMemcpyAsync(out3T, S.tri.p, n * sizeof(int), cudaMemcpyDeviceToHost, S.stream));
+    return cudaStatus(cudaStreamSynchronize(S.stream));
+}
+LCS_API int LCS_GetSurfaceAux(float* outAux4) {
+    if (!S.surfaceReady || !outAux4) return -1;
+    CK(cudaMemcpyAsync(S.hostState + 7, S.triCount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    const size_t n = S.hostState[7];
+    if (n) CK(cudaMemcpyAsync(outAux4, S.outAux.p, n * sizeof(float4), cudaMemcpyDeviceToHost, S.stream));
     return cudaStatus(cudaStreamSynchronize(S.stream));
 }
 LCS_API int GBT_GetParticleRot(float* out9) {

@@ -186,12 +186,14 @@ CORE_SIGNATURES = (
     ("LCS_GetCornerPos", (P,), I), ("LCS_GetNbrIdx", (P,), I), ("LCS_GetTopologyRevision", (P,), I),
     ("LCS_GetCutEdgeFractions", (P,), I), ("LCS_GetCutDebug", (P, P), I),
     ("LCS_ProfileEnable", (I,), None), ("LCS_ProfileRead", (I, P), I), ("LCS_Shutdown", (), None),
+    ("LCS_GetSurfaceCounts", (P, P), I), ("LCS_GetSurface", (P, P, P), I), ("LCS_GetSurfaceAux", (P,), I),
 )
 EXTENSION_SIGNATURES = (
     ("LCS_SetTetStiffness", (I, P, P), I), ("LCS_GetTetStiffness", (P, P), I), ("LCS_TetCount", (), I), ("LCS_TetColorCount", (), I),
     ("LCS_EdgeColorCount", (), I), ("LCS_EdgeCount", (), I), ("LCS_GetTetIds", (P,), I),
     ("LCS_GetTetColors", (P,), I), ("LCS_GetEdgeColors", (P,), I), ("LCS_GetVelocities", (P,), I),
     ("LCS_GetBendPairs", (P,), I), ("LCS_GetVoxelCutMask", (P,), I), ("GBT_GetParticleRot", (P,), I),
+    ("GBT_GetSurfaceTriangles", (P,), I),
 )
 UNIFIED_SIGNATURES = (
     ("LCS_PressureBladeAbiVersion", (), I), ("LCS_SetPressureBlade", (P,), I),
@@ -201,7 +203,6 @@ UNIFIED_SIGNATURES = (
     ("LCS_RefineContactSurface", (I,), I), ("LCS_SurfaceDepth", (P,), I),
     ("LCS_SetGraspPatch", (F, F, F), I), ("LCS_SetToolDynamics", (F, F, F, F), I),
     ("LCS_SetJawDynamics", (F, F, F, F), I), ("LCS_SetInstrumentControl", (I,), I),
-    ("LCS_GetSurfaceCounts", (P, P), I), ("LCS_GetSurface", (P, P, P), I), ("LCS_GetSurfaceAux", (P,), I),
     ("LCS_GetGraspCoreFlags", (I, P), I), ("LCS_GetSolvedTool", (P, P, P), I), ("LCS_GetSolvedJaw", (P,), I),
     ("LCS_GetPressureBlade", (P,), I), ("LCS_GetContactReaction", (P, P), I), ("LCS_GetJawLoad", (P,), I),
     ("LCS_GetMaterialQuality", (P,), I),
@@ -458,6 +459,27 @@ class PlainTissue(_Session):
         accessor = getattr(self.dll, "_Z20physics_particle_rotv")
         accessor.restype = ct.c_void_p
         return _device_floats(accessor(), 9 * n).reshape(n, 3, 3)
+
+    def surface(self):
+        """The reconstructed surface (LCS_GetSurface*): a triangle soup ``pos``, ``nrm`` (3T, 3) and
+        ``aux`` (3T, 4), plus ``tri`` (3T,) — the voxel id of each soup vertex (its feature point)."""
+        count, indices = ct.c_int32(0), ct.c_int32(0)
+        self.check("LCS_GetSurfaceCounts", ct.byref(count), ct.byref(indices))
+        n = count.value
+        pos, nrm = np.empty((n, 3), dtype=np.float32), np.empty((n, 3), dtype=np.float32)
+        idx, aux = np.empty(n, dtype=np.int32), np.empty((n, 4), dtype=np.float32)
+        if n:
+            self.check("LCS_GetSurface", pointer(pos), pointer(nrm), pointer(idx))
+            self.check("LCS_GetSurfaceAux", pointer(aux))
+        if not self.reference:
+            tri = np.empty(n, dtype=np.int32)
+            if n:
+                self.check("GBT_GetSurfaceTriangles", pointer(tri))
+        else:   # a reference build keeps the tagged voxel ids in device memory (recon_tri)
+            accessor = getattr(self.dll, "_Z9recon_triv")
+            accessor.restype = ct.c_void_p
+            tri = _device_floats(accessor(), n).view(np.int32) if n else np.empty(0, dtype=np.int32)
+        return dict(pos=pos, nrm=nrm, aux=aux, tri=tri)
 
     def bend_alive(self):
         out = np.empty(len(self.grid.positions) * 15 * 8, dtype=np.int32)

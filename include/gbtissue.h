@@ -79,6 +79,18 @@ LCS_API int LCS_SetContactModel(int enabled, float muS, float muD, float thickne
 LCS_API int LCS_SetTissueGuard(float minimum, int passes, int count, const int* inside, int capture);
 LCS_API int LCS_SetTissueMaterial(float tensileStrength, float bulkDampingSeconds);
 
+/* ---- dual-contouring surface (plugin_api.cpp:84-100; recon_get_counts / recon_get_surface /
+ * recon_get_surface_aux, V/dc_recon.cu:625-671).  Rebuilt from the live lattice at LCS_Init and in
+ * every LCS_Finalize.  A non-indexed triangle soup: vertexCount == indexCount == 3 x triangles
+ * (at most 3 x triCapacity), triangles in surface-edge order; outIdx[i] = i.  Aux = rest anchor xyz
+ * + wall flag (0 for the skin). ------------------------------------------------------------------ */
+LCS_API int LCS_GetSurfaceCounts(int* vertexCount, int* indexCount);
+LCS_API int LCS_GetSurface(float* outPos3, float* outNrm3, int* outIdx);
+LCS_API int LCS_GetSurfaceAux(float* outAux4);
+/* recon_tri (V/dc_recon.cu:693): the voxel id of every soup vertex, i.e. the indexed form of the
+ * surface (vertex v = voxel v's feature point). */
+LCS_API int GBT_GetSurfaceTriangles(int* out3T);
+
 /* ---- readback (plugin_api.cpp:38, 170-177) ----------------------------------------------------- */
 LCS_API int LCS_GetCornerPos(float* out3N);
 LCS_API int LCS_GetNbrIdx(int* out6N);

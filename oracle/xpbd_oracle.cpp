@@ -16,6 +16,7 @@
 // Reference files followed ("V/" = endoscopic_tissue/native/vendor/cuda/):
 //   V/physics.cu:214-315 (physics_init), 317-329 (gravity), 331-394 (physics_step),
 //     109-205 + 399-411 particle frames (frames_oracle.inc)
+//   V/dc_recon.cu:97-455, 469-487, 507-541 dual-contouring surface (surface_oracle.inc)
 //   V/xpbd/xpbd_solver.cu:393-412 predict, 429-466 liveness, 469-479 tet edge support,
 //     484-524 edges, 534-573 bending, 578-587 tet alpha, 749-829 tets, 871-919 velocity,
 //     1049-1123 CCD capsule/jaw contact, 1204-1279 edge colouring, 1332-1400 bend colouring,
@@ -231,10 +232,10 @@ static int slotOfDirected(int a, int b) {
     int axis = ad == 1 ? 0 : (ad == S.dx + 1 ? 1 : 2);
     return 6 * a + 2 * axis + (d > 0 ? 1 : 0);
 }
+#include "surface_oracle.inc"
 API int LCS_Init(const ReconInitDesc* desc, const float* cornerPos, const int* voxelCorner, const int* voxelIsectOffset,
                  const int* voxelIsectCount, const void* isect, const void* surfaceEdges) {
-    (void)voxelCorner; (void)voxelIsectOffset; (void)voxelIsectCount; (void)surfaceEdges;
-    resetCut(); resetPhysics(); S.reconReady = false;
+    resetCut(); resetPhysics(); S.reconReady = false; SS = SurfaceState();
     if (!desc) return -1000;
     int vc = desc->voxelCount, cc = desc->cornerCount;
     if (vc <= 0 || cc <= 0 || desc->triCapacity <= 0 || !cornerPos) return -1001;
@@ -249,6 +250,10 @@ API int LCS_Init(const ReconInitDesc* desc, const float* cornerPos, const int* v
         S.skinT[slotOfDirected(is[i].b, is[i].a)] = 1.f - is[i].t;
     }
     S.reconReady = true;
+    if (voxelCorner) {   // the static surface of the rest lattice and its rest snapshot
+        int rc = initSurfaceO(desc, voxelCorner, voxelIsectOffset, voxelIsectCount, is, (const int*)surfaceEdges);
+        if (rc) { S.reconReady = false; SS = SurfaceState(); return rc; }
+    }
     return 0;
 }
 
@@ -1221,6 +1226,7 @@ API int LCS_Step(float dt) {
 API int LCS_Finalize() {
     if (!S.physReady) return -1;
     computeParticleFrames();
+    buildSurfaceO();
     return 0;
 }
 API int LCS_GetCornerPos(float* out) {
