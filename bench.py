@@ -369,10 +369,11 @@ def adjoint_measurement(lib, reps=3):
             "gradients": "theta [98,304] and capsule path [51, 6]", "substeps": frames * substeps}
 
 
-def frames_measurement(lib, calls=50, warmup=3):
-    """Particle frames (k_ComputeParticleRot) on the C2 lattice after 3 sagging frames.  LCS_Finalize
-    runs one frame pass (its own launch) and synchronises: wall clock per call, median.  The device
-    time of the kernel and its DRAM bytes come from the committed ncu summary."""
+def finalize_measurement(lib, calls=50, warmup=3):
+    """LCS_Finalize on the C2 lattice after 3 sagging frames: one particle frame pass
+    (k_ComputeParticleRot) and one dual-contouring surface rebuild, each its own launch, then a
+    stream synchronise; wall clock per call, median.  Device times and DRAM bytes of the two kernels
+    come from the committed ncu summaries."""
     from genesis_tissue_simulation_gb300 import workloads as W
 
     w = W.make("c2", steps=3)
@@ -386,24 +387,27 @@ def frames_measurement(lib, calls=50, warmup=3):
             if k >= warmup:
                 times.append(time.perf_counter() - t0)
         R = s.particle_frames().astype(np.float64)
+        surf = s.surface()
     finally:
         s.close()
     gram_err = float(np.abs(np.einsum("nji,njk->nik", R, R) - np.eye(3)).max())
     nodes = len(w.grid.positions)
     ms = 1e3 * float(np.median(times))
     out = {"workload": f"c2 lattice, {nodes:,} nodes ({int((w.grid.active != 0).sum()):,} active), after 3 frames",
-           "ms_per_pass_wall": ms, "nodes_per_s_wall": nodes / (ms * 1e-3), "algorithmic_bytes_per_node": 120,
-           "timing": f"wall clock around LCS_Finalize (launch + kernel + stream sync), median of {calls}",
-           "max_orthonormality_error": gram_err}
-    path = ROOT / "profiles" / "ncu_particle_frames_c2.md"
-    if path.exists():
+           "ms_per_finalize_wall": ms, "frame_nodes": nodes, "surface_triangles": int(len(surf["tri"]) // 3),
+           "surface_voxels": int((w.grid.counts > 0).sum()), "surface_edges": int(len(w.grid.surface_edges)),
+           "timing": f"wall clock around LCS_Finalize (two launches + stream sync), median of {calls}",
+           "max_frame_orthonormality_error": gram_err}
+    for key, name in (("particle_frames", "ncu_particle_frames_c2"), ("surface", "ncu_surface_c2")):
+        path = ROOT / "profiles" / f"{name}.md"
+        if not path.exists():
+            continue
+        entry = {}
         for line in path.read_text().splitlines():
-            if line.startswith("kernel_us_per_launch:"):
-                us = float(line.split(":", 1)[1].split()[0])
-                out["kernel_us_ncu"] = us
-                out["achieved_gbs_ncu"] = 120 * nodes / (us * 1e-6) / 1e9
-            if line.startswith("traffic_bytes_per_launch:"):
-                out["traffic"] = float(line.split(":", 1)[1].split()[0])
+            for field in ("kernel_us_per_launch", "traffic_bytes_per_launch", "algorithmic_bytes_per_launch"):
+                if line.startswith(field + ":"):
+                    entry[field] = float(line.split(":", 1)[1].split()[0])
+        out[key] = entry
     return out
 
 
@@ -418,7 +422,7 @@ def main():
     parser.add_argument("--no-batched", action="store_true")
     parser.add_argument("--no-adjoint", action="store_true")
     parser.add_argument("--no-workloads", action="store_true", help="skip the C1 and C3 lines")
-    parser.add_argument("--only", default="all", choices=("all", "batched", "adjoint", "frames"),
+    parser.add_argument("--only", default="all", choices=("all", "batched", "adjoint", "finalize"),
                         help="run one section alone and print its JSON object (for profiling)")
     parser.add_argument("--batched-frames", type=int, default=20)
     args = parser.parse_args()
@@ -443,7 +447,7 @@ def main():
     lib = native_build.build()
     if args.only != "all":   # one section alone (profiling runs): its JSON object, no bench line
         section = (batched_measurement(lib, args.batched_frames, max(args.warmup, 3)) if args.only == "batched"
-                   else frames_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1)) if args.only == "frames"
+                   else finalize_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1)) if args.only == "finalize"
                    else adjoint_measurement(lib, reps=max(args.steps, 1)))
         print(json.dumps({"only": args.only, **section}), flush=True)
         return
@@ -533,7 +537,7 @@ def main():
     if not args.no_adjoint:
         line["adjoint"] = adjoint_measurement(lib)
     if not args.no_workloads:
-        line["particle_frames"] = frames_measurement(lib)
+        line["finalize"] = finalize_measurement(lib)
     if not args.no_batched:
         batched = batched_measurement(lib, args.batched_frames, max(args.warmup, 3))
         batched["roofline"].update(peak=peak, frac=batched["roofline"]["achieved"] / peak, peak_kind=peak_kind)
