@@ -82,7 +82,7 @@ struct Session {
     bool surfaceReady = false, haveRestSurface = false;
     int nVox = 0, nSurfVox = 0, nSurfEdges = 0, triCapacity = 0, qefIters = 8, surfBlocks = 0;
     DBuf<int> voxelCorner, isectOff, isectCnt, surfVox, tri, nrmFixed, blockTotal;
-    DBuf<IsectRec> isect; DBuf<int4> surfEdges; DBuf<float4> fp, fpRest, nrm, outAux; DBuf<float> outPos, outNrm;
+    DBuf<IsectRec> isect; DBuf<int4> surfEdges; DBuf<float4> fp, fpRest, outAux; DBuf<float> outPos, outNrm;
     DBuf<unsigned> surfSync, triCount;
     unsigned* hostState = nullptr;          // pinned mirror of state + cut counters
     // tool / contact
@@ -132,7 +132,7 @@ void freeAll() {
     freePhysics();
     S.pos.release(); S.rest.release();
     for (auto* b : {&S.voxelCorner, &S.isectOff, &S.isectCnt, &S.surfVox, &S.tri, &S.nrmFixed, &S.blockTotal}) b->release();
-    S.isect.release(); S.surfEdges.release(); S.fp.release(); S.fpRest.release(); S.nrm.release(); S.outAux.release();
+    S.isect.release(); S.surfEdges.release(); S.fp.release(); S.fpRest.release(); S.outAux.release();
     S.outPos.release(); S.outNrm.release(); S.surfSync.release(); S.triCount.release();
     S.surfaceReady = S.haveRestSurface = false;
     S.reconReady = false;
@@ -156,9 +156,11 @@ int ensureStream() {
     if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, S.device) == cudaSuccess && khz > 0) S.clockKHz = khz;
     S.gridBlocks = std::max(1, perSm) * S.smCount;
     S.gridBlocksExt = std::max(1, perSmExt) * S.smCount;
+    // one CTA per SM: the surface work is small, and every grid barrier costs in proportion to the CTAs
     int perSmSurface = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSmSurface, surfaceKernel, kSurfaceThreads, 0));
-    S.surfBlocks = std::max(1, perSmSurface) * S.smCount;
+    if (perSmSurface < 1) return -(int)cudaErrorLaunchOutOfResources;
+    S.surfBlocks = S.smCount;
     return 0;
 }
 
@@ -177,7 +179,7 @@ int buildSurface() {
     if (S.cutReady) {
         m.nbr = S.nbr.p; m.rot = S.rotParity ? S.rotB.p : S.rotA.p; m.cutT = S.edgeCutT.p; m.cutMask = S.cutMask.p;
     }
-    m.fp = S.fp.p; m.fpRest = S.fpRest.p; m.nrmFixed = S.nrmFixed.p; m.nrm = S.nrm.p;
+    m.fp = S.fp.p; m.fpRest = S.fpRest.p; m.nrmFixed = S.nrmFixed.p;
     m.tri = S.tri.p; m.triCount = S.triCount.p; m.blockTotal = S.blockTotal.p;
     m.outPos = S.outPos.p; m.outNrm = S.outNrm.p; m.outAux = S.outAux.p;
     unsigned* sync = S.surfSync.p;
@@ -227,10 +229,9 @@ int uploadSurface(const ReconInitDescAbi* d, const int* voxelCorner, const int* 
     CK(S.isect.upload((const IsectRec*)isect, I, S.stream));
     CK(S.surfEdges.upload(edges.data(), E, S.stream));
     const size_t idx = (size_t)3 * S.triCapacity;
-    CK(S.fp.alloc(V)); CK(S.fpRest.alloc(V)); CK(S.nrm.alloc(V)); CK(S.nrmFixed.alloc((size_t)3 * V));
+    CK(S.fp.alloc(V)); CK(S.fpRest.alloc(V)); CK(S.nrmFixed.alloc((size_t)3 * V));
     CK(cudaMemsetAsync(S.fp.p, 0, (size_t)V * sizeof(float4), S.stream));
     CK(cudaMemsetAsync(S.fpRest.p, 0, (size_t)V * sizeof(float4), S.stream));
-    CK(cudaMemsetAsync(S.nrm.p, 0, (size_t)V * sizeof(float4), S.stream));
     CK(S.tri.alloc(idx)); CK(S.outPos.alloc(3 * idx)); CK(S.outNrm.alloc(3 * idx)); CK(S.outAux.alloc(idx));
     CK(S.blockTotal.alloc(S.surfBlocks)); CK(S.surfSync.alloc(2)); CK(S.triCount.alloc(1));
     CK(cudaMemsetAsync(S.triCount.p, 0, sizeof(unsigned), S.stream));

@@ -1,6 +1,6 @@
 // Dual-contouring surface of the deformed lattice (V/dc_recon.cu): one persistent launch rebuilds
 // the feature point of every surface voxel, stitches the quads of the surface edges, accumulates
-// and normalises the vertex normals and expands the indexed triangles into a vertex soup.
+// the vertex normals and expands the indexed triangles into a vertex soup.
 #pragma once
 #include "tissue_device.cuh"
 
@@ -22,7 +22,7 @@ struct SurfaceMesh {
     const float4* pos; const float4* rest;
     const int* nbr; const float* rot; const float* cutT; const unsigned* cutMask;
     float4* fp; const float4* fpRest;   // [V] feature points (w = 1 when set), rest snapshot
-    int* nrmFixed; float4* nrm;         // [3V] fixed-point normal sums, [V] unit normals
+    int* nrmFixed;                      // [3V] fixed-point normal sums
     int* tri; unsigned* triCount;       // [3 cap] voxel ids, 3 x emitted triangles
     int* blockTotal;                    // [gridDim] triangles of each CTA's edge range
     float* outPos; float* outNrm; float4* outAux;   // [3 cap] vertex soup: xyz, xyz, rest anchor + wall flag

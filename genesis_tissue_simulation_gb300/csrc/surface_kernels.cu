@@ -8,9 +8,10 @@
 //      The CTAs own contiguous edge ranges and write at the prefix sum of the ranges before them,
 //      so the triangle list is in surface-edge order on every run (the reference appends with an
 //      atomic counter, in arrival order);
-//   3. area-weighted face normals scattered to the vertices as 2^20 fixed point (integer sums: the
-//      same result in any order);  4. normalised;  5. the indexed triangles expanded into the
-//      vertex soup the getters return (position, normal, rest anchor + wall flag).
+//      Each written triangle scatters its area-weighted face normal to its vertices as 2^20 fixed
+//      point (integer sums: the same result in any order);
+//   3. the indexed triangles expanded into the vertex soup the getters return (position, unit
+//      normal of the vertex's sum, rest anchor + wall flag).
 // Arithmetic follows the reference's expressions and order (no contraction), like the frame
 // kernels, so the CPU restatement reproduces every bit.
 #include "surface.h"
@@ -211,40 +212,34 @@ __global__ void __launch_bounds__(kSurfaceThreads) surfaceKernel(SurfaceMesh s, 
 #pragma unroll
         for (int k = 0; k < 2; k++) {
             if (!ok[k]) continue;
-            if (t < s.triCapacity) { s.tri[3 * t] = ids[3 * k]; s.tri[3 * t + 1] = ids[3 * k + 1]; s.tri[3 * t + 2] = ids[3 * k + 2]; }
+            if (t < s.triCapacity) {   // kept triangles scatter their face normal (k_NormalsScatter, V/dc_recon.cu:321-355)
+                const int a = ids[3 * k], b = ids[3 * k + 1], c = ids[3 * k + 2];
+                s.tri[3 * t] = a; s.tri[3 * t + 1] = b; s.tri[3 * t + 2] = c;
+                const f3 p0 = fpAt(s, a), n = cross(fpAt(s, b) - p0, fpAt(s, c) - p0);
+                const int fx = (int)(n.x * kNormalScale), fy = (int)(n.y * kNormalScale), fz = (int)(n.z * kNormalScale);
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    const int v = ids[3 * k + q];
+                    atomicAdd(s.nrmFixed + 3 * v, fx); atomicAdd(s.nrmFixed + 3 * v + 1, fy); atomicAdd(s.nrmFixed + 3 * v + 2, fz);
+                }
+            }
             t++;
         }
         running += roundTotal;
     }
     if (!g.sync()) return;
-    // 3. face normals (k_NormalsScatter, V/dc_recon.cu:321-355)
+    // 3. vertex soup (k_ExpandVertices V/dc_recon.cu:363-400, external vertices), each vertex's unit
+    // normal formed from its fixed-point sum (k_NormalsNormalize, 442-455)
     const int nTri = (int)(*(volatile unsigned*)s.triCount / 3u);
-    for (int t = r; t < nTri; t += R) {
-        const int a = s.tri[3 * t], b = s.tri[3 * t + 1], c = s.tri[3 * t + 2];
-        const f3 p0 = fpAt(s, a), p1 = fpAt(s, b), p2 = fpAt(s, c);
-        const f3 n = cross(p1 - p0, p2 - p0);
-        const int fx = (int)(n.x * kNormalScale), fy = (int)(n.y * kNormalScale), fz = (int)(n.z * kNormalScale);
-        for (int k = 0; k < 3; k++) {
-            const int v = k == 0 ? a : (k == 1 ? b : c);
-            atomicAdd(s.nrmFixed + 3 * v, fx); atomicAdd(s.nrmFixed + 3 * v + 1, fy); atomicAdd(s.nrmFixed + 3 * v + 2, fz);
-        }
-    }
-    if (!g.sync()) return;
-    // 4. unit normals (k_NormalsNormalize, V/dc_recon.cu:442-455)
-    for (int j = r; j < s.nSurfVox; j += R) {
-        const int v = s.surfVox[j];
+    for (int i = r; i < 3 * nTri; i += R) {
+        const int v = s.tri[i];
+        const float4 p = s.fp[v], q = s.fpRest[v];
         const f3 n = mk((float)s.nrmFixed[3 * v] / kNormalScale, (float)s.nrmFixed[3 * v + 1] / kNormalScale,
                         (float)s.nrmFixed[3 * v + 2] / kNormalScale);
         const float l = len(n);
-        s.nrm[v] = l > 1e-6f ? make_float4(n.x / l, n.y / l, n.z / l, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    if (!g.sync()) return;
-    // 5. vertex soup (k_ExpandVertices, V/dc_recon.cu:363-400, external vertices)
-    for (int i = r; i < 3 * nTri; i += R) {
-        const int v = s.tri[i];
-        const float4 p = s.fp[v], n = s.nrm[v], q = s.fpRest[v];
+        const f3 u = l > 1e-6f ? mk(n.x / l, n.y / l, n.z / l) : mk(0.f, 0.f, 0.f);
         s.outPos[3 * i] = p.x; s.outPos[3 * i + 1] = p.y; s.outPos[3 * i + 2] = p.z;
-        s.outNrm[3 * i] = n.x; s.outNrm[3 * i + 1] = n.y; s.outNrm[3 * i + 2] = n.z;
+        s.outNrm[3 * i] = u.x; s.outNrm[3 * i + 1] = u.y; s.outNrm[3 * i + 2] = u.z;
         s.outAux[i] = make_float4(q.x, q.y, q.z, 0.f);
     }
 }
