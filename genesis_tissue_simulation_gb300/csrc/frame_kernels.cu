@@ -100,9 +100,26 @@ __device__ bool cutHitsMaterial(float t, float skin, int ia, int ib) {
     if (!(skin >= 0.f && skin <= 1.f)) return false;
     return ia ? t <= skin : t >= skin;
 }
+// EmitCutPoint (V/cut.cu:186-215): the cut point of owner p on the undeformed edge (`along`) plus
+// the half-kerf on p's side of the cut plane, and the outward cut normal, both in p's frame `rot`.
+__device__ void emitCutPoint(const DeviceMesh& m, const CutParams& cu, const float* rot, f3 hit, f3 along, int p, int slot, f3 ncut) {
+    const f3 pp = xyz(m.pos[p]);
+    const float sd = dot(pp - hit, ncut);
+    float side = sd > 0.f ? 1.f : (sd < 0.f ? -1.f : 0.f);
+    if (side == 0.f) side = 1.f;
+    const float* q = rot + 9 * (size_t)p;
+    const f3 r0 = mk(q[0], q[1], q[2]), r1 = mk(q[3], q[4], q[5]), r2 = mk(q[6], q[7], q[8]);
+    const f3 g = ncut * (side * (cu.toolD * 0.5f)), n = ncut * side;
+    const f3 local = along + ((r0 * g.x + r1 * g.y) + r2 * g.z);
+    const f3 mat = (r0 * n.x + r1 * n.y) + r2 * n.z;
+    cu.cutRec[2 * (size_t)slot] = make_float4(local.x, local.y, local.z, 1.f);
+    cu.cutRec[2 * (size_t)slot + 1] = make_float4(mat.x, mat.y, mat.z, 0.f);
+}
+
 // MarkAndEmit (V/cut.cu:218-254): mark the edge in its occupied stencil voxels; on its first cut
-// record the fractions and count the two cut-point records of a crossing inside the material.
-__device__ void markEdge(const DeviceMesh& m, const CutParams& cu, int4 g, int a, int b, float t) {
+// record the fractions and, for a crossing inside the material, the two cut points (the owners'
+// frames `rot`; `hit` and `ncut` place the kerf).
+__device__ void markEdge(const DeviceMesh& m, const CutParams& cu, const float* rot, int4 g, int a, int b, float t, f3 hit, f3 ncut) {
     bool first = false, saw = false, occ = false;
     for (int s = 0; s < 4; s++) {
         int x = g.y + kStencilOff[g.x][s][0], y = g.z + kStencilOff[g.x][s][1], z = g.w + kStencilOff[g.x][s][2];
@@ -119,9 +136,14 @@ __device__ void markEdge(const DeviceMesh& m, const CutParams& cu, int4 g, int a
     cu.edgeCutT[directedSlot(m, b, a)] = 1.f - t;
     if (!cutHitsMaterial(t, cu.skinT[directedSlot(m, a, b)], cu.inside[a], cu.inside[b])) return;
     atomicAdd(cu.counters + 1, 2u);
+    if (cu.cutRec && rot) {
+        const f3 rest = xyz(cu.rest[b]) - xyz(cu.rest[a]);
+        emitCutPoint(m, cu, rot, hit, rest * t, a, 6 * a + 2 * g.x + 1, ncut);
+        emitCutPoint(m, cu, rot, hit, rest * (t - 1.f), b, 6 * b + 2 * g.x, ncut);
+    }
 }
 
-__device__ void tickEdge(const DeviceMesh& m, const CutParams& cu, int e, bool ccd) {
+__device__ void tickEdge(const DeviceMesh& m, const CutParams& cu, int e, bool ccd, const float* rot) {
     int4 g = cu.gridEdges[e];          // (axis, x, y, z)
     int axis = g.x;
     int a = nodeId(m, g.y, g.z, g.w);
@@ -162,7 +184,13 @@ __device__ void tickEdge(const DeviceMesh& m, const CutParams& cu, int e, bool c
                 f3 wv = S - pa;
                 float u = dot(cross(wv, D), n2) / n2l, v = dot(cross(wv, e1), n2) / n2l;
                 if (u <= 0.f || u > 1.f || v < -2e-2f || v > 1.f + 2e-2f) continue;
-                markEdge(m, cu, g, a, b, u);
+                // hit on the current edge; kerf normal = blade x relative tissue motion, else the
+                // last valid blade normal (V/cut.cu:576-587)
+                const f3 hit = a1 + (b1 - a1) * u;
+                const f3 relV = (Pv + Qv) * 0.5f, nHit = cross(D, relV);
+                const float nLen = len(nHit);
+                const f3 nEmit = nLen > 1e-8f ? mk(nHit.x / nLen, nHit.y / nLen, nHit.z / nLen) : mk(cu.ncx, cu.ncy, cu.ncz);
+                markEdge(m, cu, rot, g, a, b, u, hit, nEmit);
                 break;
             }
         }
@@ -178,9 +206,10 @@ __device__ void tickEdge(const DeviceMesh& m, const CutParams& cu, int e, bool c
             float l2 = dot(d, d);
             f3 r = xyz(cu.rest[b]) - xyz(cu.rest[a]);
             float tl2 = cu.tearLen2 * (dot(r, r) / (cu.voxelL * cu.voxelL));
-            if (l2 > tl2) {
+            if (l2 > tl2) {   // tear plane normal to the edge through its midpoint (V/cut.cu:674-683)
                 atomicAdd(cu.counters + 2, 1u);
-                markEdge(m, cu, g, a, b, 0.5f);
+                const float l = sqrtf(l2);
+                markEdge(m, cu, rot, g, a, b, 0.5f, xyz(m.pos[a]) + d * 0.5f, mk(d.x / l, d.y / l, d.z / l));
             }
         }
     }
@@ -453,7 +482,8 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 // previous tick's closing barrier and this tick's opening one
                 const unsigned pointsBefore = rotations ? *(volatile unsigned*)(cu.counters + 1) : 0u;
                 if (!sync.sync()) return;
-                for (int e = r; e < cu.nGridEdges; e += R) tickEdge(m, cu, e, true);
+                const float* rot = rotations ? m.particleRot[rotParity] : nullptr;
+                for (int e = r; e < cu.nGridEdges; e += R) tickEdge(m, cu, e, true, rot);
                 if (!sync.sync()) return;
                 mark(s, kPhaseTick);
                 // a tick that emitted cut points is followed by fresh frames before the next substep
@@ -637,7 +667,7 @@ __device__ bool mollerTrumbore(f3 O, f3 D, f3 V0, f3 V1, f3 V2, float& t) {
     return u >= -EPS && v >= -EPS && u + v <= 1.f + EPS && t > 0.f && t <= 1.f;
 }
 
-__global__ void detectQuadKernel(DeviceMesh m, CutParams cu, QuadTool tool) {
+__global__ void detectQuadKernel(DeviceMesh m, CutParams cu, QuadTool tool, const float* rot) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= cu.nGridEdges || !tool.valid) return;
     int4 g = cu.gridEdges[e];
@@ -655,7 +685,7 @@ __global__ void detectQuadKernel(DeviceMesh m, CutParams cu, QuadTool tool) {
     if (!h1 && !h2) return;
     float tr = (h1 && h2) ? fminf(t1, t2) : (h1 ? t1 : t2);
     tr = fminf(fmaxf(tr, 0.f), 1.f);
-    markEdge(m, cu, g, a, b, tr);
+    markEdge(m, cu, rot, g, a, b, tr, O + D * tr, tool.ncut);
 }
 
 __global__ void severKernel(DeviceMesh m, CutParams cu) {
@@ -663,7 +693,7 @@ __global__ void severKernel(DeviceMesh m, CutParams cu) {
     if (e >= cu.nGridEdges) return;
     CutParams noTear = cu;
     noTear.tearLen2 = 0.f;
-    tickEdge(m, noTear, e, false);
+    tickEdge(m, noTear, e, false, nullptr);
 }
 
 }  // namespace gbt

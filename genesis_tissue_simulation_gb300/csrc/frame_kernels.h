@@ -36,8 +36,8 @@ __global__ void particleRotKernel(DeviceMesh m, const unsigned* parityWord, int 
 __global__ void tetAlphaKernel(int n, float invH2, const float2* stiff, float2* alpha);
 __global__ void gravityKernel(int n, float gx, float gy, float gz, float4* ext);
 
-struct QuadTool { f3 t1[3], t2[3], lo, hi; int valid; };
-__global__ void detectQuadKernel(DeviceMesh m, CutParams cu, QuadTool tool);
+struct QuadTool { f3 t1[3], t2[3], lo, hi, ncut; int valid; };
+__global__ void detectQuadKernel(DeviceMesh m, CutParams cu, QuadTool tool, const float* rot);
 __global__ void severKernel(DeviceMesh m, CutParams cu);
 
 }  // namespace gbt

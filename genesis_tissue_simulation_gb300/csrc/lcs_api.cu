@@ -84,6 +84,7 @@ struct Session {
     DBuf<int> voxelCorner, isectOff, isectCnt, surfVox, tri, nrmFixed, blockTotal;
     DBuf<IsectRec> isect; DBuf<int4> surfEdges; DBuf<float4> fp, fpRest, outAux; DBuf<float> outPos, outNrm;
     DBuf<unsigned> surfSync, triCount;
+    DBuf<float4> cutFP; DBuf<int> cutNrmFixed, rawTri; DBuf<int4> faces; int faceCap = 0;   // cut voxels' surface
     unsigned* hostState = nullptr;          // pinned mirror of state + cut counters
     // tool / contact
     bool toolArmed = false; ToolPose tool{}, toolFrom{};
@@ -94,6 +95,9 @@ struct Session {
     // cut
     CutInitDesc cd{};
     DBuf<int4> gridEdges; DBuf<unsigned> occupied, cutMask, counters; DBuf<int> inside; DBuf<float> skinTD, edgeCutT;
+    DBuf<int> conn;                         // [4096 x 9] components of the voxel corners per 12-bit cut mask
+    DBuf<float4> cutRec;                    // [2 x 6N] cut points per directed lattice slot
+    float emitNcut[3] = {0.f, 1.f, 0.f};    // last valid world cut normal of the blade
     bool toolSet = false, havePrev = false, pressure = false; CutToolDesc cutTool{};
     float tearLen2 = 0.f;
     // launch choice and profiling
@@ -113,6 +117,9 @@ int cudaStatus(cudaError_t e) { return e == cudaSuccess ? 0 : -(int)e; }
 
 void freeCut() {
     S.gridEdges.release(); S.occupied.release(); S.cutMask.release(); S.counters.release(); S.inside.release();
+    S.conn.release(); S.cutRec.release();
+    S.cutFP.release(); S.cutNrmFixed.release(); S.rawTri.release(); S.faces.release(); S.faceCap = 0;
+    S.emitNcut[0] = 0.f; S.emitNcut[1] = 1.f; S.emitNcut[2] = 0.f;
     S.skinTD.release(); S.edgeCutT.release();
     S.cutReady = false; S.toolSet = false; S.havePrev = false;
 }
@@ -176,8 +183,12 @@ int buildSurface() {
     m.cutActive = S.cutReady ? 1 : 0;
     m.surfVox = S.surfVox.p; m.voxelCorner = S.voxelCorner.p; m.isectOff = S.isectOff.p; m.isectCnt = S.isectCnt.p;
     m.isect = S.isect.p; m.edges = S.surfEdges.p; m.pos = S.pos.p; m.rest = S.rest.p;
+    m.nVox = S.nVox;
     if (S.cutReady) {
         m.nbr = S.nbr.p; m.rot = S.rotParity ? S.rotB.p : S.rotA.p; m.cutT = S.edgeCutT.p; m.cutMask = S.cutMask.p;
+        m.conn = S.conn.p; m.occupied = S.occupied.p; m.inside = S.inside.p; m.skinT = S.skinTD.p; m.active = S.active.p;
+        m.cutRec = S.cutRec.p; m.cutFP = S.cutFP.p; m.cutNrmFixed = S.cutNrmFixed.p; m.raw = S.rawTri.p;
+        m.faces = S.faces.p; m.faceCap = S.faceCap;
     }
     m.fp = S.fp.p; m.fpRest = S.fpRest.p; m.nrmFixed = S.nrmFixed.p;
     m.tri = S.tri.p; m.triCount = S.triCount.p; m.blockTotal = S.blockTotal.p;
@@ -233,7 +244,7 @@ int uploadSurface(const ReconInitDescAbi* d, const int* voxelCorner, const int* 
     CK(cudaMemsetAsync(S.fp.p, 0, (size_t)V * sizeof(float4), S.stream));
     CK(cudaMemsetAsync(S.fpRest.p, 0, (size_t)V * sizeof(float4), S.stream));
     CK(S.tri.alloc(idx)); CK(S.outPos.alloc(3 * idx)); CK(S.outNrm.alloc(3 * idx)); CK(S.outAux.alloc(idx));
-    CK(S.blockTotal.alloc(S.surfBlocks)); CK(S.surfSync.alloc(2)); CK(S.triCount.alloc(1));
+    CK(S.blockTotal.alloc((size_t)2 * S.surfBlocks)); CK(S.surfSync.alloc(2)); CK(S.triCount.alloc(1));
     CK(cudaMemsetAsync(S.triCount.p, 0, sizeof(unsigned), S.stream));
     return 0;
 }
@@ -286,6 +297,7 @@ CutParams cutParams() {
     c.sx = S.cutTool.t2v2[0]; c.sy = S.cutTool.t2v2[1]; c.sz = S.cutTool.t2v2[2];
     c.ex = S.cutTool.t1v2[0]; c.ey = S.cutTool.t1v2[1]; c.ez = S.cutTool.t1v2[2];
     c.voxelL = S.cd.voxelL; c.tearLen2 = S.tearLen2; c.havePrev = S.havePrev ? 1 : 0;
+    c.cutRec = S.cutRec.p; c.toolD = S.cutTool.d; c.ncx = S.emitNcut[0]; c.ncy = S.emitNcut[1]; c.ncz = S.emitNcut[2];
     return c;
 }
 
@@ -550,7 +562,6 @@ LCS_API int LCS_SetGraspTool(const void* toolState) {
 // ---------------------------------------------------------------------------------------------
 LCS_API int LCS_InitCut(const CutInitDesc* desc, const void* conn4096, const void* gridEdges, const int* voxelOccupied,
                         const int* cornerInside) {
-    (void)conn4096;
     freeCut();
     if (!desc) return -3000;
     if (desc->voxelCount <= 0 || desc->cornerCount <= 0) return -3001;
@@ -568,6 +579,28 @@ LCS_API int LCS_InitCut(const CutInitDesc* desc, const void* conn4096, const voi
     CK(S.edgeCutT.upload(minus.data(), minus.size(), S.stream));
     CK(S.counters.alloc(4));
     CK(cudaMemsetAsync(S.counters.p, 0, 4 * sizeof(unsigned), S.stream));
+    // connectivity table (Conn4096Gpu, V/cut.cuh:50-56): component count and component of each local
+    // corner for every cut mask; checked so every feature-point slot 8 v + component stays in range
+    if (conn4096) {
+        const int* t = (const int*)conn4096;
+        for (int k = 0; k < 4096; k++) {
+            const int n = t[9 * k];
+            if (n < 0 || n > 8) return -3001;
+            for (int c = 0; c < 8; c++) if (t[9 * k + 1 + c] < 0 || t[9 * k + 1 + c] >= 8) return -3001;
+        }
+        CK(S.conn.upload(t, (size_t)9 * 4096, S.stream));
+    }
+    CK(S.cutRec.alloc((size_t)12 * S.N));
+    CK(cudaMemsetAsync(S.cutRec.p, 0, (size_t)12 * S.N * sizeof(float4), S.stream));
+    if (S.surfaceReady && S.conn.p) {   // the cut voxels' share of the surface: component points, walls
+        CK(S.cutFP.alloc((size_t)8 * S.nVox)); CK(S.cutNrmFixed.alloc((size_t)24 * S.nVox));
+        CK(cudaMemsetAsync(S.cutFP.p, 0, (size_t)8 * S.nVox * sizeof(float4), S.stream));
+        CK(S.rawTri.alloc((size_t)3 * S.triCapacity));
+        int cap = 1;
+        while (cap < 2 * S.triCapacity) cap <<= 1;
+        CK(S.faces.alloc(cap));
+        S.faceCap = cap;
+    }
     float tau = desc->tearStretchRatio;
     S.tearLen2 = (tau >= 1.0f && tau == tau) ? (tau * desc->voxelL) * (tau * desc->voxelL) : 0.f;
     CK(cudaStreamSynchronize(S.stream));
@@ -577,6 +610,7 @@ LCS_API int LCS_InitCut(const CutInitDesc* desc, const void* conn4096, const voi
 LCS_API void LCS_SetTool(const CutToolDesc* tool) {
     if (!tool) return;
     S.cutTool = *tool;
+    if (tool->valid != 0) { S.emitNcut[0] = tool->ncut[0]; S.emitNcut[1] = tool->ncut[1]; S.emitNcut[2] = tool->ncut[2]; }
     if (!S.toolSet && S.cutReady) S.havePrev = true;   // the snapshot is the current positions
     S.toolSet = true;
 }
@@ -593,8 +627,8 @@ LCS_API int LCS_DetectCut() {
     auto v = [](const float* a) { f3 r; r.x = a[0]; r.y = a[1]; r.z = a[2]; return r; };
     q.t1[0] = v(c.t1v0); q.t1[1] = v(c.t1v1); q.t1[2] = v(c.t1v2);
     q.t2[0] = v(c.t2v0); q.t2[1] = v(c.t2v1); q.t2[2] = v(c.t2v2);
-    q.lo = v(c.aabbMin); q.hi = v(c.aabbMax); q.valid = c.valid;
-    detectQuadKernel<<<(n + 255) / 256, 256, 0, S.stream>>>(m, cu, q);
+    q.lo = v(c.aabbMin); q.hi = v(c.aabbMax); q.ncut = v(c.ncut); q.valid = c.valid;
+    detectQuadKernel<<<(n + 255) / 256, 256, 0, S.stream>>>(m, cu, q, S.rotParity ? S.rotB.p : S.rotA.p);
     severKernel<<<(n + 255) / 256, 256, 0, S.stream>>>(m, cu);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(S.stream));

@@ -23,8 +23,18 @@ struct SurfaceMesh {
     const int* nbr; const float* rot; const float* cutT; const unsigned* cutMask;
     float4* fp; const float4* fpRest;   // [V] feature points (w = 1 when set), rest snapshot
     int* nrmFixed;                      // [3V] fixed-point normal sums
-    int* tri; unsigned* triCount;       // [3 cap] voxel ids, 3 x emitted triangles
-    int* blockTotal;                    // [gridDim] triangles of each CTA's edge range
+    int* tri; unsigned* triCount;       // [3 cap] vertex tags (voxel id, or cut-point slot | 1 << 31
+                                        // [| 1 << 30 on cut walls]), 3 x emitted triangles
+    int* blockTotal;                    // [2 gridDim] triangles of each CTA's ranges
+    // cut voxels (V/cut.cu:761-1100): one feature point per (voxel, corner component)
+    int nVox;
+    const int* conn;                    // [4096 x 9] component count and component of local corners 0..7
+    const unsigned* occupied; const int* inside; const float* skinT; const int* active;
+    const float4* cutRec;               // [2 x 6N] cut points per directed lattice slot (owner frame)
+    float4* cutFP;                      // [8V] component feature points (w = 1 when set)
+    int* cutNrmFixed;                   // [3 x 8V] their fixed-point normal sums
+    int* raw;                           // [3 cap] triangles before internal faces cancel
+    int4* faces; int faceCap;           // hash table of triangle keys (power of two entries)
     float* outPos; float* outNrm; float4* outAux;   // [3 cap] vertex soup: xyz, xyz, rest anchor + wall flag
 };
 

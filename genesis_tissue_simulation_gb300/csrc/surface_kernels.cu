@@ -4,12 +4,16 @@
 //      rebuilt from its inside particle's frame), then either the advected rest feature point
 //      (intact voxels once the rest surface exists) or the QEF gradient walk clamped to the voxel
 //      box; the voxel's normal accumulator is cleared;
-//   2. stitch: every surface edge's four voxels form a quad, two triangles, degenerate ones dropped.
-//      The CTAs own contiguous edge ranges and write at the prefix sum of the ranges before them,
-//      so the triangle list is in surface-edge order on every run (the reference appends with an
-//      atomic counter, in arrival order);
-//      Each written triangle scatters its area-weighted face normal to its vertices as 2^20 fixed
-//      point (integer sums: the same result in any order);
+//      with cut voxels present, one feature point per (voxel, corner component) from its crossings
+//      and cut points (the cut feature-point chain, V/cut.cu:761-985);
+//   2. stitch: every surface edge's four voxels form a quad, two triangles, degenerate ones dropped,
+//      then the cut walls of the cut edges.  The CTAs own contiguous edge and voxel ranges and write
+//      at the prefix sums of the ranges before them, so the triangle list is in surface-edge order,
+//      then voxel order, on every run (the reference appends with an atomic counter, in arrival
+//      order).  With walls present, triangles over the same vertex set cancel (a hash table of
+//      sorted keys, then a second prefix-sum compaction in list order).  Each kept triangle scatters
+//      its area-weighted face normal to its vertices as 2^20 fixed point (integer sums: the same
+//      result in any order);
 //   3. the indexed triangles expanded into the vertex soup the getters return (position, unit
 //      normal of the vertex's sum, rest anchor + wall flag).
 // Arithmetic follows the reference's expressions and order (no contraction), like the frame
@@ -104,29 +108,289 @@ __device__ void featurePoint(const SurfaceMesh& s, int v) {
     s.fp[v] = make_float4(x.x, x.y, x.z, 1.f);
 }
 
-__device__ __forceinline__ f3 fpAt(const SurfaceMesh& s, int v) { return xyz(s.fp[v]); }
+constexpr unsigned kCutTag = 0x80000000u, kWallTag = 0x40000000u, kIdMask = 0x3FFFFFFFu;
+constexpr float kPosScale = 16384.0f;        // POS_SCALE (V/cut.cuh): cut-normal sums
+
+// Position of a triangle vertex tag (FetchPos, V/dc_recon.cu:228-234).
+__device__ __forceinline__ f3 tagPos(const SurfaceMesh& s, int tag) {
+    const unsigned u = (unsigned)tag;
+    return (u & kCutTag) ? xyz(s.cutFP[u & kIdMask]) : xyz(s.fp[u & kIdMask]);
+}
+
+__constant__ int kStencil[3][4][3] = {{{0, 0, 0}, {0, -1, 0}, {0, -1, -1}, {0, 0, -1}},
+                                      {{0, 0, 0}, {0, 0, -1}, {-1, 0, -1}, {-1, 0, 0}},
+                                      {{0, 0, 0}, {-1, 0, 0}, {-1, -1, 0}, {0, -1, 0}}};
+__constant__ int kStencilEdge[3][4] = {{0, 2, 6, 4}, {3, 7, 5, 1}, {8, 9, 10, 11}};
+__constant__ int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+__constant__ int kEdgeCorners[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+
+__device__ __forceinline__ bool voxIn(const SurfaceMesh& s, int x, int y, int z) {
+    return x >= 0 && y >= 0 && z >= 0 && x < s.dx && y < s.dy && z < s.dz;
+}
+__device__ __forceinline__ int voxId(const SurfaceMesh& s, int x, int y, int z) { return x + s.dx * (y + s.dy * z); }
+__device__ __forceinline__ int nodeOf(const SurfaceMesh& s, int x, int y, int z) { return x + (s.dx + 1) * (y + (s.dy + 1) * z); }
+// local corner (0..7) of a voxel at offset (dx, dy, dz) from its low corner, -1 if not a corner
+__device__ __forceinline__ int localCorner(int dx, int dy, int dz) {
+    if ((unsigned)dx > 1u || (unsigned)dy > 1u || (unsigned)dz > 1u) return -1;
+    const int b = dx | (dy << 1) | (dz << 2);
+    return b == 2 ? 3 : (b == 3 ? 2 : (b == 6 ? 7 : (b == 7 ? 6 : b)));
+}
+__device__ __forceinline__ int compOf(const SurfaceMesh& s, unsigned mask, int lc) { return s.conn[9 * mask + 1 + lc]; }
+
+__device__ __forceinline__ bool cutHitsMaterial(float t, float skin, int ia, int ib) {
+    if (ia && ib) return true;
+    if (!ia && !ib) return false;
+    if (!(skin >= 0.f && skin <= 1.f)) return false;
+    return ia ? t <= skin : t >= skin;
+}
+
+// Feature points of the components of cut voxel v (k_ClearCutFP, k_AccumulateCutFP,
+// k_ComputeComponentFP: V/cut.cu:761-771, 791-850, 852-985).  Each component's point is seeded by
+// the mean of its own crossings (the skin crossings whose owner corner lies in it) and its cut
+// points, walked along the crossings' QEF gradient inside the component's deformed box, clamped to
+// that box, and projected onto the plane of its cut points.  The cut points of v are those of its
+// 12 edges, gathered here in a fixed order (edge, then the low owner before the high one), so the
+// sums do not depend on scheduling (the reference adds them with float atomics).
+__device__ void componentPoints(const SurfaceMesh& s, int v) {
+    const unsigned mask = s.cutMask[v] & 0xFFFu;
+    const int vx = v % s.dx, vy = (v / s.dx) % s.dy, vz = v / (s.dx * s.dy);
+    const int* c = s.voxelCorner + 8 * (size_t)v;
+    const int compCount = s.conn[9 * mask];
+    f3 acc[8]; int cnt[8], nx[8], ny[8], nz[8];
+    for (int k = 0; k < 8; k++) { acc[k] = mk(0.f, 0.f, 0.f); cnt[k] = 0; nx[k] = ny[k] = nz[k] = 0; }
+    for (int le = 0; le < 12; le++) {
+        const int ca = kEdgeCorners[le][0], cb = kEdgeCorners[le][1];
+        const int axis = kCorner[ca][0] != kCorner[cb][0] ? 0 : (kCorner[ca][1] != kCorner[cb][1] ? 1 : 2);
+        const bool aLow = kCorner[ca][axis] < kCorner[cb][axis];
+        const int lcs[2] = {aLow ? ca : cb, aLow ? cb : ca};   // low end, high end
+        for (int h = 0; h < 2; h++) {
+            const int owner = c[lcs[h]];
+            const size_t slot = 6 * (size_t)owner + 2 * axis + (h == 0 ? 1 : 0);
+            const float4 L = s.cutRec[2 * slot];
+            if (L.w == 0.f || s.active[owner] == 0) continue;
+            const float4 Mn = s.cutRec[2 * slot + 1];
+            const int comp = compOf(s, mask, lcs[h]);
+            int root = 0;
+            while (root < 8 && compOf(s, mask, root) != comp) root++;
+            const f3 origin = xyz(s.pos[c[root]]);
+            const float* q = s.rot + 9 * (size_t)owner;
+            const f3 r0 = mk(q[0], q[1], q[2]), r1 = mk(q[3], q[4], q[5]), r2 = mk(q[6], q[7], q[8]);
+            const f3 lo = mk(L.x, L.y, L.z), mn = mk(Mn.x, Mn.y, Mn.z);
+            const f3 local = (xyz(s.pos[owner]) - origin) + mk(dot(r0, lo), dot(r1, lo), dot(r2, lo));
+            const f3 nw = mk(dot(r0, mn), dot(r1, mn), dot(r2, mn));
+            acc[comp] = acc[comp] + local;
+            cnt[comp]++;
+            nx[comp] += (int)rintf(nw.x * kPosScale); ny[comp] += (int)rintf(nw.y * kPosScale); nz[comp] += (int)rintf(nw.z * kPosScale);
+        }
+    }
+    // the voxel's skin crossings and the corner owning each after the cut
+    const int off = s.isectOff[v], ncross = s.isectCnt[v];
+    f3 world[12]; int owner[12];
+    for (int k = 0; k < ncross && k < 12; k++) {
+        const IsectRec& it = s.isect[off + k];
+        world[k] = crossingWorld(s, it);
+        const float cT = s.cutT ? s.cutT[directedSlot(s, it.a, it.b)] : -1.f;
+        const int in = skinOwnerA(it.t, cT, it.insideA) ? it.a : it.b;
+        const int nxn = s.dx + 1, nyn = s.dy + 1;
+        const int lc = localCorner(in % nxn - vx, (in / nxn) % nyn - vy, in / (nxn * nyn) - vz);
+        owner[k] = lc < 0 ? -1 : compOf(s, mask, lc);
+    }
+    f3 half = xyz(s.rest[c[6]]) - xyz(s.rest[c[0]]);
+    half = mk(fabsf(half.x) * .5f, fabsf(half.y) * .5f, fabsf(half.z) * .5f);
+    for (int comp = 0; comp < 8; comp++) {
+        const size_t slot = 8 * (size_t)v + comp;
+        s.cutNrmFixed[3 * slot] = 0; s.cutNrmFixed[3 * slot + 1] = 0; s.cutNrmFixed[3 * slot + 2] = 0;
+        if (comp >= compCount) { s.cutFP[slot] = make_float4(0.f, 0.f, 0.f, 0.f); continue; }
+        f3 bc = mk(0.f, 0.f, 0.f), origin = mk(0.f, 0.f, 0.f);
+        int nCorn = 0;
+        for (int lc = 0; lc < 8; lc++) {
+            if (compOf(s, mask, lc) != comp) continue;
+            const f3 p = xyz(s.pos[c[lc]]);
+            if (nCorn == 0) origin = p;
+            bc = bc + p;
+            nCorn++;
+        }
+        if (nCorn > 0) bc = mk(bc.x / (float)nCorn, bc.y / (float)nCorn, bc.z / (float)nCorn);
+        f3 sum = mk(0.f, 0.f, 0.f);
+        int nIncl = 0;
+        for (int k = 0; k < ncross && k < 12; k++) if (owner[k] == comp) { sum = sum + world[k]; nIncl++; }
+        const int ccnt = cnt[comp];
+        if (ccnt > 0) sum = (sum + acc[comp]) + origin * (float)ccnt;
+        const int total = nIncl + ccnt;
+        if (total == 0) { s.cutFP[slot] = make_float4(0.f, 0.f, 0.f, 0.f); continue; }
+        f3 x = mk(sum.x / (float)total, sum.y / (float)total, sum.z / (float)total);
+        if (nIncl > 0) {
+            for (int it = 0; it < s.qefIters; it++) {
+                f3 F = mk(0.f, 0.f, 0.f);
+                for (int k = 0; k < ncross && k < 12; k++) {
+                    if (owner[k] != comp) continue;
+                    const IsectRec& rec = s.isect[off + k];
+                    const f3 n = mk(rec.nx, rec.ny, rec.nz);
+                    F = F + n * dot(n, world[k] - x);
+                }
+                const float a = 0.1f * (1.0f - (float)it / (float)s.qefIters);
+                const f3 xn = x + F * a;
+                if (fabsf(xn.x - bc.x) >= half.x || fabsf(xn.y - bc.y) >= half.y || fabsf(xn.z - bc.z) >= half.z) break;
+                x = xn;
+            }
+        }
+        x = mk(fminf(fmaxf(x.x, bc.x - half.x), bc.x + half.x), fminf(fmaxf(x.y, bc.y - half.y), bc.y + half.y),
+               fminf(fmaxf(x.z, bc.z - half.z), bc.z + half.z));
+        if (ccnt > 0) {   // onto the plane of the component's own cut points
+            const f3 nAcc = mk((float)nx[comp] / kPosScale, (float)ny[comp] / kPosScale, (float)nz[comp] / kPosScale);
+            const float nLen = len(nAcc);
+            if (nLen > 1e-6f && nLen > 0.25f * (float)ccnt) {
+                const f3 nbar = mk(nAcc.x / nLen, nAcc.y / nLen, nAcc.z / nLen);
+                const f3 cutC = mk(acc[comp].x / (float)ccnt, acc[comp].y / (float)ccnt, acc[comp].z / (float)ccnt) + origin;
+                x = x - nbar * dot(nbar, x - cutC);
+            }
+        }
+        s.cutFP[slot] = make_float4(x.x, x.y, x.z, 1.f);
+    }
+}
+
+// Vertex of a skin quad (StitchVertId, V/dc_recon.cu:213-226): a cut, occupied voxel resolves to
+// the feature point of the component holding the crossing's inside corner, when it has one.
+__device__ int stitchVert(const SurfaceMesh& s, bool cutChain, int x, int y, int z, int icx, int icy, int icz) {
+    const int v = voxId(s, x, y, z);
+    if (!cutChain) return v;
+    const unsigned mask = s.cutMask[v] & 0xFFFu;
+    if (mask == 0u || s.occupied[v] == 0u) return v;
+    const int lc = localCorner(icx - x, icy - y, icz - z);
+    if (lc < 0) return v;
+    const int slot = 8 * v + compOf(s, mask, lc);
+    return s.cutFP[slot].w > .5f ? (int)(kCutTag | (unsigned)slot) : v;
+}
 
 // The quad of surface edge e as two triangles (k_Stitch, V/dc_recon.cu:241-289): voxel stencil
 // counter-clockwise about +axis, flipped when the base corner is outside; a triangle whose area
 // vector is below 1e-8 is dropped.
-__device__ void stitchEdge(const SurfaceMesh& s, int e, int ids[6], bool ok[2]) {
+__device__ void stitchEdge(const SurfaceMesh& s, bool cutChain, int e, int ids[6], bool ok[2]) {
     const int4 r = s.edges[e];
     const int axis = r.x & 3, insideA = r.x >> 2;
-    int ox[4], oy[4], oz[4];
-    if (axis == 0) { ox[0] = 0; oy[0] = 0; oz[0] = 0; ox[1] = 0; oy[1] = -1; oz[1] = 0; ox[2] = 0; oy[2] = -1; oz[2] = -1; ox[3] = 0; oy[3] = 0; oz[3] = -1; }
-    else if (axis == 1) { ox[0] = 0; oy[0] = 0; oz[0] = 0; ox[1] = 0; oy[1] = 0; oz[1] = -1; ox[2] = -1; oy[2] = 0; oz[2] = -1; ox[3] = -1; oy[3] = 0; oz[3] = 0; }
-    else { ox[0] = 0; oy[0] = 0; oz[0] = 0; ox[1] = -1; oy[1] = 0; oz[1] = 0; ox[2] = -1; oy[2] = -1; oz[2] = 0; ox[3] = 0; oy[3] = -1; oz[3] = 0; }
+    const int ax = axis == 0, ay = axis == 1, az = axis == 2;
+    int icx = r.y, icy = r.z, icz = r.w;
+    if (cutChain) {   // the inside corner after a cut between it and the skin
+        const int slot = 6 * nodeOf(s, r.y, r.z, r.w) + 2 * axis + 1;
+        const float cT = s.cutT ? s.cutT[slot] : -1.f;
+        if (!skinOwnerA(s.skinT[slot], cT, insideA)) { icx += ax; icy += ay; icz += az; }
+    }
     int v[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) v[k] = (r.y + ox[k]) + s.dx * ((r.z + oy[k]) + s.dy * (r.w + oz[k]));
+    for (int k = 0; k < 4; k++)
+        v[k] = stitchVert(s, cutChain, r.y + kStencil[axis][k][0], r.z + kStencil[axis][k][1], r.w + kStencil[axis][k][2], icx, icy, icz);
     int a = v[0], b = v[1], c = v[2], d = v[3];
     if (insideA == 0) { const int t = b; b = d; d = t; }
     ids[0] = a; ids[1] = b; ids[2] = c; ids[3] = a; ids[4] = c; ids[5] = d;
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-        const f3 p0 = fpAt(s, ids[3 * k]), p1 = fpAt(s, ids[3 * k + 1]), p2 = fpAt(s, ids[3 * k + 2]);
+        const f3 p0 = tagPos(s, ids[3 * k]), p1 = tagPos(s, ids[3 * k + 1]), p2 = tagPos(s, ids[3 * k + 2]);
         const f3 n = cross(p1 - p0, p2 - p0);
         ok[k] = !(dot(n, n) < 1e-16f);
+    }
+}
+
+// Wall faces of cut voxel v (k_BuildCutTriangles + EmitCutQuad, V/cut.cu:988-1089), for the cut
+// edges whose first marked stencil voxel is v: from each end p of the edge, the component points
+// of p's component in the four voxels around the edge, fanned (through the separated corners when
+// two opposite corners are shared), wound by the rest stencil and flipped for the far end; faces
+// made of shared points only, or of zero area, are dropped.  Writes up to 48 triangles from
+// out[3 * base] on (those at or beyond `cap` are skipped) and returns how many there are.
+__device__ int wallsOfVoxel(const SurfaceMesh& s, int v, int* out, int base, int cap) {
+    const unsigned mask = s.cutMask[v] & 0xFFFu;
+    if (mask == 0u || s.occupied[v] == 0u) return 0;
+    const int vx = v % s.dx, vy = (v / s.dx) % s.dy, vz = v / (s.dx * s.dy);
+    int count = 0;
+    for (int le = 0; le < 12; le++) {
+        if (((mask >> le) & 1u) == 0u) continue;
+        const int ca = kEdgeCorners[le][0], cb = kEdgeCorners[le][1];
+        const int axis = kCorner[ca][0] != kCorner[cb][0] ? 0 : (kCorner[ca][1] != kCorner[cb][1] ? 1 : 2);
+        const int bx = vx + min(kCorner[ca][0], kCorner[cb][0]), by = vy + min(kCorner[ca][1], kCorner[cb][1]),
+                  bz = vz + min(kCorner[ca][2], kCorner[cb][2]);
+        bool valid = true, canonical = true, seen = false;
+        for (int st = 0; st < 4; st++) {
+            const int x = bx + kStencil[axis][st][0], y = by + kStencil[axis][st][1], z = bz + kStencil[axis][st][2];
+            if (!voxIn(s, x, y, z)) { valid = false; continue; }
+            if (x == vx && y == vy && z == vz) seen = true;
+            else if (!seen && ((s.cutMask[voxId(s, x, y, z)] >> kStencilEdge[axis][st]) & 1u)) canonical = false;
+        }
+        if (!valid || !canonical) continue;
+        const int ax = axis == 0, ay = axis == 1, az = axis == 2;
+        const int A = nodeOf(s, bx, by, bz), B = nodeOf(s, bx + ax, by + ay, bz + az);
+        for (int end = 0; end < 2; end++) {
+            const bool basedHere = end == 0;
+            const int p = basedHere ? A : B, other = basedHere ? B : A;
+            const int px = bx + (basedHere ? 0 : ax), py = by + (basedHere ? 0 : ay), pz = bz + (basedHere ? 0 : az);
+            const int qx = bx + (basedHere ? ax : 0), qy = by + (basedHere ? ay : 0), qz = bz + (basedHere ? az : 0);
+            const int slot = 6 * p + 2 * axis + (basedHere ? 1 : 0);
+            if (!cutHitsMaterial(s.cutT[slot], s.skinT[slot], s.inside[p], s.inside[other])) continue;
+            int tag[4]; bool ok[4], shared[4]; int n = 0;
+            for (int st = 0; st < 4; st++) {
+                ok[st] = false; shared[st] = false; tag[st] = 0;
+                const int x = bx + kStencil[axis][st][0], y = by + kStencil[axis][st][1], z = bz + kStencil[axis][st][2];
+                const int w = voxId(s, x, y, z);
+                if (s.occupied[w] == 0u) continue;
+                const unsigned m2 = s.cutMask[w] & 0xFFFu;
+                if (m2 == 0u) continue;
+                const int lc = localCorner(px - x, py - y, pz - z);
+                if (lc < 0) continue;
+                const int comp = compOf(s, m2, lc);
+                const int lq = localCorner(qx - x, qy - y, qz - z);
+                shared[st] = lq >= 0 && comp == compOf(s, m2, lq);
+                const int fs = 8 * w + comp;
+                if (s.cutFP[fs].w < .5f) continue;
+                tag[st] = (int)(kCutTag | kWallTag | (unsigned)fs);
+                ok[st] = true;
+                n++;
+            }
+            if (n < 3) continue;
+            int ord[4], m = 0;
+            for (int st = 0; st < 4; st++) if (ok[st]) ord[m++] = st;
+            if (m == 4 && shared[ord[0]] && shared[ord[2]] && !shared[ord[1]] && !shared[ord[3]]) {
+                const int first = ord[0]; ord[0] = ord[1]; ord[1] = ord[2]; ord[2] = ord[3]; ord[3] = first;
+            }
+            f3 q[4];
+            for (int k = 0; k < m; k++) q[k] = tagPos(s, tag[ord[k]]);
+            for (int k = 1; k < m - 1; k++) {
+                if (shared[ord[0]] && shared[ord[k]] && shared[ord[k + 1]]) continue;
+                const f3 nrm = cross(q[k] - q[0], q[k + 1] - q[0]);
+                if (dot(nrm, nrm) < 1e-16f) continue;
+                const int t = base + count;
+                if (out && t < cap) {
+                    out[3 * t] = tag[ord[0]];
+                    out[3 * t + 1] = tag[ord[basedHere ? k : k + 1]];
+                    out[3 * t + 2] = tag[ord[basedHere ? k + 1 : k]];
+                }
+                count++;
+            }
+        }
+    }
+    return count;
+}
+
+// Triangle key for the internal-face cancellation (V/surface_cleanup.cuh): the three vertex tags
+// without the wall marker, sorted; `odd` is the parity of the sorting permutation.
+__device__ __forceinline__ void faceKey(const int* t, unsigned k[3], bool* odd) {
+    for (int i = 0; i < 3; i++) k[i] = (unsigned)t[i] & 0xBFFFFFFFu;
+    bool o = false;
+    if (k[0] > k[1]) { const unsigned x = k[0]; k[0] = k[1]; k[1] = x; o = !o; }
+    if (k[1] > k[2]) { const unsigned x = k[1]; k[1] = k[2]; k[2] = x; o = !o; }
+    if (k[0] > k[1]) { const unsigned x = k[0]; k[0] = k[1]; k[1] = x; o = !o; }
+    *odd = o;
+}
+__device__ __forceinline__ unsigned faceHash(const unsigned k[3], int fcap) {
+    return ((k[0] * 73856093u) ^ (k[1] * 19349663u) ^ (k[2] * 83492791u)) & (unsigned)(fcap - 1);
+}
+
+// Face normal of triangle t scattered to its vertices as fixed point (k_NormalsScatter).
+__device__ void scatterNormal(const SurfaceMesh& s, const int* t) {
+    const f3 p0 = tagPos(s, t[0]), n = cross(tagPos(s, t[1]) - p0, tagPos(s, t[2]) - p0);
+    const int fx = (int)(n.x * kNormalScale), fy = (int)(n.y * kNormalScale), fz = (int)(n.z * kNormalScale);
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const unsigned u = (unsigned)t[q];
+        int* d = (u & kCutTag) ? s.cutNrmFixed + 3 * (size_t)(u & kIdMask) : s.nrmFixed + 3 * (size_t)u;
+        atomicAdd(d, fx); atomicAdd(d + 1, fy); atomicAdd(d + 2, fz);
     }
 }
 
@@ -177,70 +441,159 @@ __device__ int blockExclusive(int v, int* sum) {
 
 __global__ void __launch_bounds__(kSurfaceThreads) surfaceKernel(SurfaceMesh s, unsigned* sync, long long spinBudget) {
     GridSync g{sync, sync + 1, gridDim.x, 0u, spinBudget, 0u};
-    const int r = g.rank(), R = g.size();
-    // 1. feature points; normal accumulators cleared
+    const int r = g.rank(), R = g.size(), G = (int)gridDim.x, b = (int)blockIdx.x;
+    const bool cutChain = s.cutActive && s.conn != nullptr;
+    // 1. feature points of the surface voxels and of the components of cut voxels; normal sums cleared
     for (int j = r; j < s.nSurfVox; j += R) {
         const int v = s.surfVox[j];
         featurePoint(s, v);
         s.nrmFixed[3 * v] = 0; s.nrmFixed[3 * v + 1] = 0; s.nrmFixed[3 * v + 2] = 0;
     }
+    if (cutChain)
+        for (int v = r; v < s.nVox; v += R)
+            if ((s.cutMask[v] & 0xFFFu) != 0u && s.occupied[v] != 0u) componentPoints(s, v);
     if (!g.sync()) return;
-    // 2. stitch, in surface-edge order
-    const int chunk = (s.nEdges + (int)gridDim.x - 1) / (int)gridDim.x;
-    const int e0 = min(s.nEdges, (int)blockIdx.x * chunk), e1 = min(s.nEdges, e0 + chunk);
-    int mine = 0;
+    // 2. count: skin quads of this CTA's surface-edge range, cut walls of its voxel range
+    const int ce = (s.nEdges + G - 1) / G, e0 = min(s.nEdges, b * ce), e1 = min(s.nEdges, e0 + ce);
+    const int cv = cutChain ? (s.nVox + G - 1) / G : 0, v0 = min(s.nVox, b * cv), v1 = cutChain ? min(s.nVox, v0 + cv) : v0;
+    int mine = 0, walls = 0;
     for (int e = e0 + (int)threadIdx.x; e < e1; e += blockDim.x) {
         int ids[6]; bool ok[2];
-        stitchEdge(s, e, ids, ok);
+        stitchEdge(s, cutChain, e, ids, ok);
         mine += (ok[0] ? 1 : 0) + (ok[1] ? 1 : 0);
     }
-    const int own = blockSum(mine);
-    if (threadIdx.x == 0) s.blockTotal[blockIdx.x] = own;
+    for (int v = v0 + (int)threadIdx.x; v < v1; v += blockDim.x) walls += wallsOfVoxel(s, v, nullptr, 0, 0);
+    const int ownSkin = blockSum(mine), ownWalls = blockSum(walls);
+    if (threadIdx.x == 0) { s.blockTotal[b] = ownSkin; s.blockTotal[G + b] = ownWalls; }
     if (!g.sync()) return;
-    int before = 0;
-    for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) before += *(volatile int*)(s.blockTotal + b);
-    before = blockSum(before);
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *s.triCount = 3u * (unsigned)min(before + own, s.triCapacity);
-    int running = before;
+    // write at the prefix: the skin in surface-edge order, then the walls in voxel order
+    int skinBefore = 0, skinAll = 0, wallBefore = 0, wallAll = 0;
+    for (int k = threadIdx.x; k < G; k += blockDim.x) {
+        const int a = *(volatile int*)(s.blockTotal + k), w = *(volatile int*)(s.blockTotal + G + k);
+        skinAll += a; wallAll += w;
+        if (k < b) { skinBefore += a; wallBefore += w; }
+    }
+    skinBefore = blockSum(skinBefore); skinAll = blockSum(skinAll); wallBefore = blockSum(wallBefore); wallAll = blockSum(wallAll);
+    const int T = min(skinAll + wallAll, s.triCapacity);
+    const bool cancel = wallAll > 0;   // faces can only repeat where walls meet the skin or each other
+    int* out = cancel ? s.raw : s.tri;
+    if (!cancel && b == G - 1 && threadIdx.x == 0) *s.triCount = 3u * (unsigned)T;
+    int running = skinBefore;
     for (int base = e0; base < e1; base += blockDim.x) {
         const int e = base + (int)threadIdx.x;
         int ids[6] = {0, 0, 0, 0, 0, 0};
         bool ok[2] = {false, false};
-        if (e < e1) stitchEdge(s, e, ids, ok);
+        if (e < e1) stitchEdge(s, cutChain, e, ids, ok);
         int roundTotal = 0;
         int t = running + blockExclusive((ok[0] ? 1 : 0) + (ok[1] ? 1 : 0), &roundTotal);
 #pragma unroll
         for (int k = 0; k < 2; k++) {
             if (!ok[k]) continue;
-            if (t < s.triCapacity) {   // kept triangles scatter their face normal (k_NormalsScatter, V/dc_recon.cu:321-355)
-                const int a = ids[3 * k], b = ids[3 * k + 1], c = ids[3 * k + 2];
-                s.tri[3 * t] = a; s.tri[3 * t + 1] = b; s.tri[3 * t + 2] = c;
-                const f3 p0 = fpAt(s, a), n = cross(fpAt(s, b) - p0, fpAt(s, c) - p0);
-                const int fx = (int)(n.x * kNormalScale), fy = (int)(n.y * kNormalScale), fz = (int)(n.z * kNormalScale);
-#pragma unroll
-                for (int q = 0; q < 3; q++) {
-                    const int v = ids[3 * k + q];
-                    atomicAdd(s.nrmFixed + 3 * v, fx); atomicAdd(s.nrmFixed + 3 * v + 1, fy); atomicAdd(s.nrmFixed + 3 * v + 2, fz);
-                }
+            if (t < s.triCapacity) {
+                out[3 * t] = ids[3 * k]; out[3 * t + 1] = ids[3 * k + 1]; out[3 * t + 2] = ids[3 * k + 2];
+                if (!cancel) scatterNormal(s, ids + 3 * k);
             }
             t++;
         }
         running += roundTotal;
     }
+    running = skinAll + wallBefore;
+    for (int base = v0; base < v1; base += blockDim.x) {
+        const int v = base + (int)threadIdx.x;
+        const int c = v < v1 ? wallsOfVoxel(s, v, nullptr, 0, 0) : 0;
+        int roundTotal = 0;
+        const int t = running + blockExclusive(c, &roundTotal);
+        if (c > 0) wallsOfVoxel(s, v, out, t, s.triCapacity);
+        running += roundTotal;
+    }
     if (!g.sync()) return;
-    // 3. vertex soup (k_ExpandVertices V/dc_recon.cu:363-400, external vertices), each vertex's unit
-    // normal formed from its fixed-point sum (k_NormalsNormalize, 442-455)
+    if (cancel) {
+        // internal faces (V/surface_cleanup.cuh): triangles with the same vertex set cancel in
+        // opposite orientation; of a surplus the first in list order stays.  Survivors keep list order.
+        int fcap = 1;
+        while (fcap < 2 * T) fcap <<= 1;
+        for (int k = r; k < fcap; k += R) s.faces[k] = make_int4(-1, 0, 0x7fffffff, 0x7fffffff);
+        if (!g.sync()) return;
+        for (int i = r; i < T; i += R) {
+            unsigned key[3]; bool odd;
+            faceKey(s.raw + 3 * i, key, &odd);
+            const unsigned h = faceHash(key, fcap);
+            for (int k = 0; k < fcap; k++) {
+                int4* entry = s.faces + ((h + (unsigned)k) & (unsigned)(fcap - 1));
+                const int old = atomicCAS(&entry->x, -1, i);
+                bool same = old < 0;
+                if (!same) { unsigned o[3]; bool oo; faceKey(s.raw + 3 * old, o, &oo); same = o[0] == key[0] && o[1] == key[1] && o[2] == key[2]; }
+                if (same) { atomicAdd(&entry->y, odd ? -1 : 1); atomicMin(odd ? &entry->w : &entry->z, i); break; }
+            }
+        }
+        if (!g.sync()) return;
+        const int ct = (T + G - 1) / G, t0 = min(T, b * ct), t1 = min(T, t0 + ct);
+        auto keep = [&](int i) {
+            unsigned key[3]; bool odd;
+            faceKey(s.raw + 3 * i, key, &odd);
+            const unsigned h = faceHash(key, fcap);
+            for (int k = 0; k < fcap; k++) {
+                const int4 e = s.faces[(h + (unsigned)k) & (unsigned)(fcap - 1)];   // the barrier's acquire makes it current
+                if (e.x < 0) return false;
+                unsigned o[3]; bool oo;
+                faceKey(s.raw + 3 * e.x, o, &oo);
+                if (o[0] == key[0] && o[1] == key[1] && o[2] == key[2]) return e.y != 0 && i == (e.y > 0 ? e.z : e.w);
+            }
+            return false;
+        };
+        int kept = 0;
+        for (int i = t0 + (int)threadIdx.x; i < t1; i += blockDim.x) kept += keep(i) ? 1 : 0;
+        const int ownKept = blockSum(kept);
+        if (threadIdx.x == 0) s.blockTotal[b] = ownKept;
+        if (!g.sync()) return;
+        int keptBefore = 0, keptAll = 0;
+        for (int k = threadIdx.x; k < G; k += blockDim.x) {
+            const int a = *(volatile int*)(s.blockTotal + k);
+            keptAll += a;
+            if (k < b) keptBefore += a;
+        }
+        keptBefore = blockSum(keptBefore); keptAll = blockSum(keptAll);
+        if (b == G - 1 && threadIdx.x == 0) *s.triCount = 3u * (unsigned)keptAll;
+        running = keptBefore;
+        for (int base = t0; base < t1; base += blockDim.x) {
+            const int i = base + (int)threadIdx.x;
+            const bool k = i < t1 && keep(i);
+            int roundTotal = 0;
+            const int t = running + blockExclusive(k ? 1 : 0, &roundTotal);
+            if (k) {
+                s.tri[3 * t] = s.raw[3 * i]; s.tri[3 * t + 1] = s.raw[3 * i + 1]; s.tri[3 * t + 2] = s.raw[3 * i + 2];
+                scatterNormal(s, s.raw + 3 * i);
+            }
+            running += roundTotal;
+        }
+        if (!g.sync()) return;
+    }
+    // 3. vertex soup (k_ExpandVertices V/dc_recon.cu:363-400), each vertex's unit normal formed from
+    // its fixed-point sum (k_NormalsNormalize 442-455, k_NormalizeCutFP V/cut.cu:1091-1098); the rest
+    // anchor of a component point is its voxel's rest skin point, else the voxel's rest centre
     const int nTri = (int)(*(volatile unsigned*)s.triCount / 3u);
     for (int i = r; i < 3 * nTri; i += R) {
-        const int v = s.tri[i];
-        const float4 p = s.fp[v], q = s.fpRest[v];
-        const f3 n = mk((float)s.nrmFixed[3 * v] / kNormalScale, (float)s.nrmFixed[3 * v + 1] / kNormalScale,
-                        (float)s.nrmFixed[3 * v + 2] / kNormalScale);
+        const unsigned u = (unsigned)s.tri[i];
+        const int id = (int)(u & kIdMask);
+        const bool cut = (u & kCutTag) != 0u;
+        const float4 p = cut ? s.cutFP[id] : s.fp[id];
+        const int* nf = cut ? s.cutNrmFixed + 3 * (size_t)id : s.nrmFixed + 3 * (size_t)id;
+        const f3 n = mk((float)nf[0] / kNormalScale, (float)nf[1] / kNormalScale, (float)nf[2] / kNormalScale);
         const float l = len(n);
-        const f3 u = l > 1e-6f ? mk(n.x / l, n.y / l, n.z / l) : mk(0.f, 0.f, 0.f);
+        const f3 un = l > 1e-6f ? mk(n.x / l, n.y / l, n.z / l) : mk(0.f, 0.f, 0.f);
+        float4 aux;
+        if (cut) {
+            const int v = id >> 3;
+            const float4 q = s.fpRest[v];
+            const f3 anchor = q.w > 0.f ? xyz(q) : (xyz(s.rest[s.voxelCorner[8 * (size_t)v]]) + xyz(s.rest[s.voxelCorner[8 * (size_t)v + 6]])) * .5f;
+            aux = make_float4(anchor.x, anchor.y, anchor.z, (float)((u >> 30) & 1u));
+        } else {
+            const float4 q = s.fpRest[id];
+            aux = make_float4(q.x, q.y, q.z, 0.f);
+        }
         s.outPos[3 * i] = p.x; s.outPos[3 * i + 1] = p.y; s.outPos[3 * i + 2] = p.z;
-        s.outNrm[3 * i] = u.x; s.outNrm[3 * i + 1] = u.y; s.outNrm[3 * i + 2] = u.z;
-        s.outAux[i] = make_float4(q.x, q.y, q.z, 0.f);
+        s.outNrm[3 * i] = un.x; s.outNrm[3 * i + 1] = un.y; s.outNrm[3 * i + 2] = un.z;
+        s.outAux[i] = aux;
     }
 }
 

@@ -106,6 +106,12 @@ struct CutParams {
     int nGridEdges; const int4* gridEdges; const unsigned* occupied; unsigned* cutMask;
     const int* inside; const float* skinT; float* edgeCutT; const float4* rest;
     unsigned* counters;   // [0] topology revision, [1] cut points, [2] tear marks
+    // cut points (EmitCutPoint, V/cut.cu:186-215), one per directed lattice slot 6p + s of the owner
+    // p: [2 (6p + s)] = offset from p on the undeformed edge plus the half-kerf, in p's frame (w = 1
+    // once set); [2 (6p + s) + 1] = the outward cut normal in p's frame
+    float4* cutRec;
+    float toolD;          // blade thickness D
+    float ncx, ncy, ncz;  // last valid world cut normal of the blade
     float sx, sy, sz, ex, ey, ez;     // current blade segment S -> E
     float voxelL, tearLen2;
     int havePrev;

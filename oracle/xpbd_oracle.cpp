@@ -27,7 +27,11 @@
 //     1235-1254 detect, 1303-1431 ribbon tick;  V/cut.cuh:113-188 lattice helpers, Moller-Trumbore
 //   V/dc_recon.cu:543-620 (recon_init: positions, rest snapshot, skin crossing fractions)
 #include <algorithm>
+#include <array>
 #include <chrono>
+#include <map>
+#include <climits>
+#include <cstdint>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -159,6 +163,8 @@ struct Session {
     std::vector<int> edgeSupport;             // [6N]
     std::vector<Real> invMass;
     std::vector<Real> particleRot, particleRotPrev;   // [9N] particle frames, rows of R
+    std::vector<Real> cutRec;                         // [8 x 6N] cut point per directed slot: local xyz w, normal xyz
+    std::vector<int> conn;                            // [9 x 4096] connectivity table (Conn4096Gpu)
     bool livenessStale = true; unsigned livenessRevision = 0xffffffffu;
     // frame
     bool frameReady = false; Real h = 0, alphaTilde = 0, velScale = 1, betaGammaHS = 0, alphaB = 0, betaGammaHB = 0;
@@ -1023,7 +1029,24 @@ static bool cutHitsMaterial(float t, float skin, int ia, int ib) {
     if (!(skin >= 0.f && skin <= 1.f)) return false;
     return ia ? t <= skin : t >= skin;
 }
-static void markAndEmit(const GridEdge2& g, int idA, int idB, float tRay) {
+// EmitCutPoint (V/cut.cu:186-215): owner p's cut point on the undeformed edge plus the half-kerf on
+// its side of the cut plane, and the outward cut normal, both in p's current frame; stored at p's
+// directed lattice slot (each lattice edge is first cut once, so a slot is written once).
+static void emitCutPointO(int p, int slot, V3 hit, V3 along, V3 ncut) {
+    const Real sd = dot(S.pos[p] - hit, ncut);
+    Real side = sd > 0 ? Real(1) : (sd < 0 ? Real(-1) : Real(0));
+    if (side == 0) side = 1;
+    const Real* q = &S.particleRot[(size_t)9 * p];
+    const V3 r0 = v3(q[0], q[1], q[2]), r1 = v3(q[3], q[4], q[5]), r2 = v3(q[6], q[7], q[8]);
+    const V3 g = ncut * (side * (Real(S.cutTool.d) * Real(0.5f))), n = ncut * side;
+    const V3 local = along + ((r0 * g.x + r1 * g.y) + r2 * g.z);
+    const V3 mat = (r0 * n.x + r1 * n.y) + r2 * n.z;
+    Real* rec = &S.cutRec[(size_t)8 * slot];
+    rec[0] = local.x; rec[1] = local.y; rec[2] = local.z; rec[3] = 1;
+    rec[4] = mat.x; rec[5] = mat.y; rec[6] = mat.z; rec[7] = 0;
+}
+
+static void markAndEmit(const GridEdge2& g, int idA, int idB, float tRay, V3 hit, V3 ncut) {
     bool first = false, saw = false, occ = false;
     for (int s = 0; s < 4; s++) {
         int x = g.bx + ES_OFF[g.axis][s][0], y = g.by + ES_OFF[g.axis][s][1], z = g.bz + ES_OFF[g.axis][s][2];
@@ -1039,7 +1062,10 @@ static void markAndEmit(const GridEdge2& g, int idA, int idB, float tRay) {
     S.edgeCutT[slotOfDirected(idA, idB)] = tRay;
     S.edgeCutT[slotOfDirected(idB, idA)] = 1.f - tRay;
     if (!cutHitsMaterial(tRay, S.skinT[slotOfDirected(idA, idB)], S.inside[idA], S.inside[idB])) return;
-    S.cutPoints += 2;     // two cut-point records per first cut (owner frames are not part of this path)
+    S.cutPoints += 2;
+    const V3 rest = S.rest[idB] - S.rest[idA];
+    emitCutPointO(idA, 6 * idA + 2 * g.axis + 1, hit, rest * Real(tRay), ncut);
+    emitCutPointO(idB, 6 * idB + 2 * g.axis, hit, rest * (Real(tRay) - Real(1)), ncut);
 }
 static bool mollerTrumbore(V3 O, V3 D, V3 V0, V3 V1, V3 V2, Real& t, Real& u, Real& v) {
     V3 L1 = V1 - V0, L2 = V2 - V0, Tv = V0 - O;
@@ -1073,7 +1099,6 @@ static void severLinks() {
 }
 
 API int LCS_InitCut(const CutInitDesc* desc, const void* conn4096, const void* gridEdges, const int* voxelOccupied, const int* cornerInside) {
-    (void)conn4096;
     resetCut();
     if (!desc) return -3000;
     if (desc->voxelCount <= 0 || desc->cornerCount <= 0) return -3001;
@@ -1088,6 +1113,9 @@ API int LCS_InitCut(const CutInitDesc* desc, const void* conn4096, const void* g
     S.prevCorner = S.pos;
     S.edgeWasExempt.assign(S.gridEdges.size(), 0); S.edgeDecay.assign(S.gridEdges.size(), 0);
     S.emitNcut = v3(0, 1, 0);
+    S.cutRec.assign((size_t)48 * S.N, Real(0));
+    S.conn.clear();
+    if (conn4096) S.conn.assign((const int*)conn4096, (const int*)conn4096 + 9 * 4096);
     float tau = desc->tearStretchRatio;
     S.tearLen2 = (tau >= 1.0f && tau == tau) ? (Real)((tau * desc->voxelL) * (tau * desc->voxelL)) : Real(0);
     S.cutReady = true;
@@ -1121,7 +1149,7 @@ API int LCS_DetectCut() {
             if (!h1 && !h2) continue;
             Real tr = (h1 && h2) ? std::fmin(t1, t2) : (h1 ? t1 : t2);
             tr = std::fmin(std::fmax(tr, Real(0)), Real(1));
-            markAndEmit(g, a, b, (float)tr);
+            markAndEmit(g, a, b, (float)tr, O + D * tr, fromA(c.ncut));
         }
     }
     severLinks();
@@ -1169,7 +1197,10 @@ static int ribbonTick() {
             Real u = dot(cross(wv, D), n2) / n2l, v = dot(cross(wv, e1), n2) / n2l;
             const Real EPS = Real(2e-2);
             if (u <= 0 || u > 1 || v < -EPS || v > Real(1) + EPS) continue;
-            markAndEmit(g, a, b, (float)u);
+            const V3 relV = (Pv + Qv) * Real(0.5f), nHit = cross(D, relV);
+            const Real nLen = len(nHit);
+            const V3 nEmit = nLen > Real(1e-8f) ? v3(nHit.x / nLen, nHit.y / nLen, nHit.z / nLen) : S.emitNcut;
+            markAndEmit(g, a, b, (float)u, a1 + (b1 - a1) * u, nEmit);
             break;
         }
     }
@@ -1192,7 +1223,8 @@ static int ribbonTick() {
             if (S.edgeWasExempt[e]) { S.edgeWasExempt[e] = 0; S.edgeDecay[e] = 0; }
             if (l2 <= tl2) continue;
             S.tearMarks++;
-            markAndEmit(g, a, b, 0.5f);
+            const Real l = std::sqrt(l2);
+            markAndEmit(g, a, b, 0.5f, S.pos[a] + d * Real(0.5f), v3(d.x / l, d.y / l, d.z / l));
         }
     }
     severLinks();

@@ -147,9 +147,94 @@ def test_skin_cut_severs_crossings(oracle_libs):
     assert all(np.isfinite(o["pos"]).all() and len(o["tri"]) > 0 for o in out)
 
 
+def rest_cut_run(lib, reference=False, sweeps=6):
+    """C1 block at rest: a vertical blade from above the top to mid-height sweeps across x in
+    `sweeps` rod-phase detections (LCS_SetTool, LCS_DetectCut, LCS_Finalize; no physics step), so
+    positions and particle frames stay at rest and every library sees the same cut.  Returns the
+    surface after each sweep and the final neighbour table."""
+    from genesis_tissue_simulation_gb300.native_backend import blade_sweep
+    g = c1_grid()
+    s = PlainTissue(g, dt=1 / 60, substeps=20, ks=1e6, young_pa=6000.0, poisson=0.25, strain_damping_s=0.04,
+                    dll_path=lib, reference=reference)
+    try:
+        xs = np.linspace(-2.3, 2.3, sweeps + 1)
+        z, top, low = 0.031, 1.3, 0.05
+        out = []
+        for k in range(sweeps):
+            s.set_blade(blade_sweep((xs[k], top, z), (xs[k], low, z), (xs[k + 1], top, z), (xs[k + 1], low, z)))
+            s.check("LCS_DetectCut")
+            s.check("LCS_Finalize")
+            out.append(s.surface())
+        return out, s.neighbors()
+    finally:
+        s.close()
+
+
+def directed_edges(tri):
+    t = tri.reshape(-1, 3).view(np.uint32).astype(np.uint64)
+    d = np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]])
+    return (d[:, 0] << np.uint64(32)) | d[:, 1], (d[:, 1] << np.uint64(32)) | d[:, 0]
+
+
+def test_cut_surface_walls(oracle_libs):
+    """After a blade has cut the block, the surface has wall triangles made of component feature
+    points (tag bits 31 and 30, aux flag 1); it stays consistently oriented (no directed edge twice)
+    and closed but for the crack front and rims where fewer than three component points exist
+    (1.5 % of the edges here); every component point lies in its voxel."""
+    out, nbr = rest_cut_run(oracle_libs[0])
+    surf = out[-1]
+    tags = surf["tri"].view(np.uint32)
+    wall = (tags & 0x40000000) != 0
+    assert wall.sum() > 30 and np.array_equal(surf["aux"][:, 3] == 1, wall)
+    assert np.all((tags[wall] & 0x80000000) != 0)
+    keys, rev = directed_edges(surf["tri"])
+    assert len(np.unique(keys)) == len(keys)
+    assert np.isin(keys, rev).mean() > 0.97
+    assert np.isfinite(surf["pos"]).all() and np.isfinite(surf["nrm"]).all()
+    g = c1_grid()
+    cut = (tags & 0x80000000) != 0
+    vox = (tags[cut] & 0x3FFFFFFF) >> 3
+    lo, hi = g.positions[g.corners[vox, 0]], g.positions[g.corners[vox, 6]]
+    assert np.all(surf["pos"][cut] >= lo - 1e-5) and np.all(surf["pos"][cut] <= hi + 1e-5)
+
+
 # ---------------------------------------------------------------------------------------------
 # GPU
 # ---------------------------------------------------------------------------------------------
+@pytest.mark.gpu
+def test_gpu_surface_bit_exact_rest_cut(gpu_lib, oracle_libs):
+    gpu, nbr_g = rest_cut_run(gpu_lib)
+    cpu, nbr_c = rest_cut_run(oracle_libs[0])
+    assert np.array_equal(nbr_g, nbr_c)
+    for a, b in zip(gpu, cpu):
+        assert_same_surface(a, b)
+
+
+@pytest.mark.gpu
+def test_cut_surface_against_reference_build(reference_lib, oracle_libs):
+    """The cut feature-point chain, the cut walls and the internal-face cancellation against the
+    reference's own build: the same rod-phase cuts of a block at rest give the same neighbour table
+    and the same triangles (multisets of vertex tags: voxel ids and component slots, wall marks
+    included), positions within 1e-5 of the diagonal (the reference sums cut points with float
+    atomics and contracts multiply-adds)."""
+    from conftest import results_dir
+    ref, nbr_r = rest_cut_run(reference_lib, reference=True)
+    orc, nbr_o = rest_cut_run(oracle_libs[0])
+    assert np.array_equal(nbr_r, nbr_o)
+    diag = W.bbox_diagonal(c1_grid())
+    rows = []
+    for a, b in zip(ref, orc):
+        ta, pa, _ = _by_triangle(a)
+        tb, pb, _ = _by_triangle(b)
+        assert np.array_equal(ta, tb)
+        rows.append({"triangles": int(len(ta)), "walls": int(((a["tri"].view(np.uint32) & 0x40000000) != 0).sum() // 3),
+                     "pos_err_over_diag": float(np.abs(pa - pb).max()) / diag})
+    with open(results_dir() / "reference_parity.jsonl", "a") as f:
+        f.write(json.dumps({"case": "cut surface at rest, c1 grid", "sweeps": rows}) + "\n")
+    assert rows[-1]["walls"] > 10
+    assert max(r["pos_err_over_diag"] for r in rows) < 1e-5, rows
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", [1, 2])
 def test_gpu_surface_bit_exact_skin_cut(gpu_lib, oracle_libs, mode):
@@ -196,7 +281,7 @@ def test_gpu_surface_bit_exact(gpu_lib, oracle_libs, name, steps, scale, mode):
 
 
 def _by_triangle(surface):
-    tri = triangles(surface)
+    tri = triangles(surface).view(np.uint32)
     order = np.lexsort(tri.T[::-1])
     return tri[order], surface["pos"].reshape(-1, 3, 3)[order], surface["nrm"].reshape(-1, 3, 3)[order]
 
