@@ -398,7 +398,25 @@ def finalize_measurement(lib, calls=50, warmup=3):
            "surface_voxels": int((w.grid.counts > 0).sum()), "surface_edges": int(len(w.grid.surface_edges)),
            "timing": f"wall clock around LCS_Finalize (two launches + stream sync), median of {calls}",
            "max_frame_orthonormality_error": gram_err}
-    for key, name in (("particle_frames", "ncu_particle_frames_c2"), ("surface", "ncu_surface_c2")):
+    # the same after 30 frames of the blade workload: cut voxels, walls, internal-face cancellation
+    wc = W.make("c3", steps=30)
+    s = wc.open(lib)
+    try:
+        wc.run(s, steps=30)
+        times = []
+        for k in range(max(calls // 2, 1) + warmup):
+            t0 = time.perf_counter()
+            s.check("LCS_Finalize")
+            if k >= warmup:
+                times.append(time.perf_counter() - t0)
+        surf = s.surface()
+    finally:
+        s.close()
+    tags = surf["tri"].view(np.uint32)
+    out["after_cut"] = {"workload": "c3 blade workload after 30 frames", "ms_per_finalize_wall": 1e3 * float(np.median(times)),
+                        "surface_triangles": int(len(tags) // 3), "wall_triangles": int(((tags & 0x40000000) != 0).sum() // 3),
+                        "component_vertices": int(((tags & 0x80000000) != 0).sum())}
+    for key, name in (("particle_frames", "ncu_particle_frames_c2"), ("surface", "ncu_surface_c2"), ("surface_after_cut", "ncu_surface_c3_cut")):
         path = ROOT / "profiles" / f"{name}.md"
         if not path.exists():
             continue
