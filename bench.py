@@ -142,6 +142,71 @@ def run_reference_arm(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def call_sequence_wall(name, steps, warmup, lib=None):
+    """Wall clock of the plugin call sequence per step (LCS_Step, the rod-phase LCS_DetectCut for the
+    blade, LCS_Finalize; both libraries synchronise before LCS_Step returns) on one workload.
+    `lib` None: the reference's own CUDA build (oracle/_ref, when it was built on this machine),
+    which also reports its own substep timeline (LCS_ProfileRead); the reference ABI has no per-tet
+    stiffness, so there the tets take the uniform (E, nu) bake (the arithmetic per step is the
+    same).  Otherwise this library, through the workload's own session."""
+    reference = lib is None
+    import ctypes
+
+    import torch
+
+    from genesis_tissue_simulation_gb300 import workloads as W
+    from genesis_tissue_simulation_gb300.native_backend import GraspParams, PlainTissue
+
+    if reference:
+        lib = ROOT / "oracle" / "_ref" / "libLiverCudaSim.so"
+        if not lib.exists():
+            return {"unavailable": "the reference build (oracle/_ref) is not present on this machine"}
+    w = W.make(name, steps=warmup + steps + 1)
+    p = w.params
+    if reference:
+        grasp = None
+        if p.get("instrument"):
+            g = dict(W.DEFAULT_GRASP)
+            g["ccd_velocity"] = p["instrument"]["ccd_velocity"]
+            grasp = GraspParams(**g)
+        m = p["tet_material"]
+        s = PlainTissue(w.grid, dt=p["dt"], substeps=p["substeps"], ks=1.0 / p["edge_compliance"], young_pa=m["young_pa"],
+                        poisson=m["poisson"], strain_damping_s=p["strain_damping_s"],
+                        tear_ratio=(p.get("blade") or {}).get("tear_ratio", 0.0), grasp_params=grasp, dll_path=lib, reference=True)
+    else:
+        s = w.open(lib)
+    try:
+        if reference:
+            s.set_gravity(*p["gravity"])
+            if w.initial_capsule is not None:
+                s.set_capsule(w.initial_capsule)
+        for k in range(warmup):
+            s.step(detect_cut=w.command(s, k))
+        torch.cuda.synchronize()
+        if reference:
+            s.functions["LCS_ProfileEnable"](1)
+        t0 = time.perf_counter()
+        for k in range(warmup, warmup + steps):
+            s.step(detect_cut=w.command(s, k))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        rc = -1
+        if reference:
+            substeps = int(p["substeps"])
+            ms = np.zeros(3, dtype=np.float32)
+            # its timeline is per substep and starts at the first profiled substep of the session
+            rc = s.functions["LCS_ProfileRead"](steps * substeps, ms.ctypes.data_as(ctypes.c_void_p))
+            s.functions["LCS_ProfileEnable"](0)
+    finally:
+        s.close()
+    out = {"workload": w.name, "wall_steps_per_s": steps / wall, "ms_per_step_wall": 1e3 * wall / steps, "steps": steps}
+    if reference:
+        out["material"] = "uniform (E, nu) bake (no per-tet stiffness in the reference ABI)"
+        if rc == 0:
+            out["substep_timeline_ms_per_step"] = float(ms.sum()) / steps
+    return out
+
+
 def workload_measurement(lib, name, steps, warmup, cpu_budget_s=6.0):
     """Steps/s of another plain-path workload through the C ABI: device time from the library's
     events around each frame (CUDA events), plus its CPU restatement on all host cores over a
@@ -552,6 +617,17 @@ def main():
     }
     if not args.no_workloads:
         line["workloads"] = {"c1": workload_measurement(lib, "c1", 100, 5), "c3": workload_measurement(lib, "c3", 30, 3)}
+        # the reference's own CUDA build on the same box and plugin call sequence, against ours
+        ref = {}
+        for key, name, steps in (("c1", "c1", 100), ("c2", args.workload, 30), ("c3", "c3", 30)):
+            r = call_sequence_wall(name, steps, 3)
+            if "wall_steps_per_s" in r:
+                ours = call_sequence_wall(name, steps, 3, lib=lib)
+                r["ours_wall_steps_per_s"] = ours["wall_steps_per_s"]
+                r["ours_over_reference"] = ours["wall_steps_per_s"] / r["wall_steps_per_s"]
+            ref[key] = r
+        line["reference_gpu"] = {"timing": "wall clock per step of LCS_Step (+ LCS_DetectCut for the blade) + LCS_Finalize, "
+                                           "both libraries on this GPU", **ref}
     if not args.no_adjoint:
         line["adjoint"] = adjoint_measurement(lib)
     if not args.no_workloads:
