@@ -286,9 +286,13 @@ def cpu_baseline_sample(workload_name, budget_s=15.0, max_steps=40):
             "sample": f"steps 2..{n + 1} of {w.name} (one warm-up step), CPU restatement FP32, OpenMP {threads} threads, {elapsed:.1f} s"}
 
 
-def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6):
+def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, rank=0, world=1):
     """Batched uneven instances: 256 grids with dims U{8..32} x U{4..16}(up) x U{8..32} cells from one
     seed, per-instance log-uniform compliance and capsule path, 10 substeps per frame.
+
+    On N GPUs (torchrun) the instances are split over the ranks by cost (longest processing time,
+    no exchange during a frame); each rank times its share, the slowest rank's time counts, and
+    the value is all 256 instances' steps over it (strong scaling).  Returns None on ranks > 0.
 
     Device rate: CUDA events around each graph-replayed frame launch (autotuned launch shape).  The
     packed state (~0.5 GB of node and element tables) exceeds L2, so no flush is added.  End to end:
@@ -304,11 +308,13 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6):
     from genesis_tissue_simulation_gb300 import workloads as W
     from genesis_tissue_simulation_gb300.native_backend import GraspParams, PlainTissue
 
-    w = BT.make_c4(steps=warmup + 2 * frames + 1)
+    full = BT.make_c4(steps=warmup + 2 * frames + 1)
+    shards = BT.shard_instances(BT.instance_costs(full), world)
+    w = full.subset(shards[rank]) if world > 1 else full
     grasp = dict(W.DEFAULT_GRASP, ccd_velocity=0.0)
     scale = w.stiffness_scale()
-    count = len(w.grids)
-    n_active = int(sum(int((g.active != 0).sum()) for g in w.grids))
+    count = len(full.grids)
+    n_active = int(sum(int((g.active != 0).sum()) for g in full.grids))
     with BT.TissueBatch(w.grids, dt=1 / 60, substeps=w.substeps, ks=1e6, strain_damping_s=w.strain_damping_s, stiffness_scale=scale,
                         grasp_params=GraspParams(**grasp), dll_path=lib) as b:
         info = b.info()
@@ -330,6 +336,17 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6):
             positions = b.positions()
         e2e_s = time.perf_counter() - e0
         assert np.isfinite(positions).all(), "non-finite batched state"
+    counts = torch.tensor([info["nodes"], info["edges"], info["tets"]], dtype=torch.float64, device="cuda")
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([device_s, e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(counts)
+        device_s, e2e_s = (float(x) for x in t.tolist())
+        if rank != 0:
+            return None
+    info = dict(info, nodes=int(counts[0]), edges=int(counts[1]), tets=int(counts[2]))
+    w = full
 
     # plain path on a size-spread sample of the same instances
     order = np.argsort([g.positions.shape[0] for g in w.grids])
@@ -362,7 +379,8 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6):
     bytes_per_substep = 64 * n_active + 4 * info["tets"]
     achieved = w.substeps * bytes_per_substep / (device_s / frames) / 1e9
     return {
-        "workload": "c4: 256 uneven instances, one launch per frame, CUDA graph",
+        "workload": "c4: 256 uneven instances, one launch per frame, CUDA graph"
+                    + (f", split over {world} GPUs by cost (slowest rank's time)" if world > 1 else ""),
         "value": value, "unit": "instance-steps/s", "ms_per_frame": 1e3 * device_s / frames, "frames": frames,
         "proj_per_s": value * w.substeps * (info["edges"] + info["tets"]) / count,
         "instances": count, "lattice_nodes": info["nodes"], "active_nodes": n_active, "tets": info["tets"],
@@ -586,6 +604,9 @@ def main():
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     device_s, e2e_s, wall = (float(x) for x in t.tolist())
+    batched = None
+    if not args.no_batched:   # every rank takes its share of the instances
+        batched = batched_measurement(lib, args.batched_frames, max(args.warmup, 3), rank=rank, world=world)
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -632,8 +653,7 @@ def main():
         line["adjoint"] = adjoint_measurement(lib)
     if not args.no_workloads:
         line["finalize"] = finalize_measurement(lib)
-    if not args.no_batched:
-        batched = batched_measurement(lib, args.batched_frames, max(args.warmup, 3))
+    if batched is not None:
         batched["roofline"].update(peak=peak, frac=batched["roofline"]["achieved"] / peak, peak_kind=peak_kind)
         line["batched"] = batched
     if not args.no_cpu_baseline:

@@ -162,6 +162,37 @@ class BatchWorkload:
     def capsules_at(self, step):
         return [path[min(step, len(path) - 1)] for path in self.capsule_paths]
 
+    def subset(self, indices):
+        """The instances `indices` (in that order) as a workload of their own."""
+        idx = [int(i) for i in indices]
+        return BatchWorkload([self.grids[i] for i in idx], self.compliance[idx], [self.capsule_paths[i] for i in idx],
+                             self.steps, self.substeps, self.strain_damping_s)
+
+
+def shard_instances(costs, world):
+    """Split instances over `world` GPUs with no exchange between them: longest-processing-time
+    assignment by cost (e.g. tets + edges per instance), ties to the lowest rank.  Returns one
+    ascending index list per rank; every instance lands on exactly one rank."""
+    costs = np.asarray(costs, dtype=np.float64)
+    if world < 1:
+        raise ValueError("world must be at least 1")
+    loads = np.zeros(world)
+    shards = [[] for _ in range(world)]
+    for i in np.argsort(-costs, kind="stable"):
+        r = int(np.argmin(loads))
+        shards[r].append(int(i))
+        loads[r] += costs[i]
+    return [sorted(s) for s in shards]
+
+
+def instance_costs(workload):
+    """Per-instance cost for sharding: lattice edges plus tets, from the grids alone."""
+    costs = []
+    for g in workload.grids:
+        cells = int(np.prod(g.dims))
+        costs.append(float(len(g.edges)) + 6.0 * cells)
+    return costs
+
 
 def make_c4(count=256, seed=4, steps=100, substeps=10, low=1e-7, high=1e-5, size_range=((8, 32), (4, 16), (8, 32))):
     """256 instances with cells x, y(up), z drawn uniformly from [8,32] x [4,16] x [8,32], one log-uniform
