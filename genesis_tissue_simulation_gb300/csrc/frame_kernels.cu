@@ -241,7 +241,7 @@ __device__ void tickEdge(const DeviceMesh& m, const CutParams& cu, int e, bool c
 // thread and read by all after a barrier, so every branch below is uniform.
 template <class Sync>
 __device__ bool guardFeasible(const DeviceMesh& m, const FrameCoeffs& fc, int substepIndex, Sync& sync) {
-    const int r = sync.rank(), R = sync.size();
+    const int r = sync.spreadRank(), R = sync.size();
     const int T = m.nTetColors > 0 ? m.tetRange[m.nTetColors - 1].y : 0;
     const int nodeEnd = m.nodeBase + m.nNodes;
     const float minimum = fc.minVolume;
@@ -312,7 +312,7 @@ __device__ __noinline__ void frictionPhase(const DeviceMesh& m, const FrameCoeff
 template <class Sync, bool Extended, bool Dsm = false, bool Rotations = false>
 __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
                          const ContactParams& cp, const CutParams& cu, unsigned* state, Sync& sync) {
-    const int r = sync.rank(), R = sync.size();
+    const int r = sync.spreadRank(), R = sync.size();
     const bool guarded = Extended && fc.guarded != 0;
     // state[0]: topology revision the liveness flags were derived at (~0u: never)
     unsigned derivedAt = *(volatile unsigned*)state;
@@ -539,6 +539,7 @@ __device__ __forceinline__ void runInstances(const DeviceMesh& m, const FrameCoe
 struct ClusterSync {
     int r, n; bool lead;
     __device__ int rank() const { return r; }
+    __device__ int spreadRank() const { return r; }
     __device__ int size() const { return n; }
     __device__ bool leader() const { return lead; }
     __device__ bool sync() { cooperative_groups::this_cluster().sync(); return true; }

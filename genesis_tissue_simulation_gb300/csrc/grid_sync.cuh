@@ -18,6 +18,12 @@ struct GridSync {
     long long budget;     // spin budget in SM clock cycles
     unsigned extra;       // arrivals awaited beyond the grid (non-zero only in the timeout test mode)
     __device__ int rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
+    // Element-to-thread map of the frame kernels: warp w of CTA b takes logical warp w * gridDim + b,
+    // so a phase with fewer elements than threads (a colour of a single mesh) spreads them over every
+    // SM instead of packing them into the first CTAs; a warp still takes 32 consecutive elements.
+    __device__ int spreadRank() const {
+        return (((int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x) << 5) | (int)(threadIdx.x & 31);
+    }
     __device__ int size() const { return gridDim.x * blockDim.x; }
     __device__ bool leader() const { return blockIdx.x == 0 && threadIdx.x == 0; }
     __device__ bool sync() {
@@ -46,6 +52,7 @@ struct GridSync {
 struct BlockSync {
     unsigned* status;
     __device__ int rank() const { return threadIdx.x; }
+    __device__ int spreadRank() const { return threadIdx.x; }
     __device__ int size() const { return blockDim.x; }
     __device__ bool sync() { __syncthreads(); return true; }
     __device__ bool leader() const { return threadIdx.x == 0; }
