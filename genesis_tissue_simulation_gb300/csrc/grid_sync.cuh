@@ -8,9 +8,11 @@
 namespace gbt {
 
 // Grid barrier on a monotonically increasing arrival counter (reset by the host before launch).
-// The arriving thread releases its block's writes with a gpu-scope fence, spins with a clock
-// budget, and acquires.  A barrier that times out records kSyncTimeout in the status word; every
-// block leaves at its next barrier, so the launch ends and the host reports the error.
+// After the block's __syncthreads, one thread arrives with a gpu-scope release add (cumulative: it
+// carries the block's writes), spins on gpu-scope acquire loads with a clock budget, and the
+// second __syncthreads hands the acquired view to the block.  A barrier that times out records
+// kSyncTimeout in the status word; every block leaves at its next barrier, so the launch ends and
+// the host reports the error.
 constexpr unsigned kSyncTimeout = 1u;
 
 struct GridSync {
@@ -31,8 +33,8 @@ struct GridSync {
         __syncthreads();
         target += nblocks;
         if (threadIdx.x == 0) {
-            __threadfence();
-            atomicAdd(counter, 1u);
+            unsigned old;
+            asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(counter) : "memory");
             long long start = clock64();
             while (true) {
                 unsigned now;
@@ -41,7 +43,6 @@ struct GridSync {
                 if (*(volatile unsigned*)status != 0u) break;
                 if (clock64() - start > budget) { atomicOr(status, kSyncTimeout); break; }
             }
-            __threadfence();
             ok = *(volatile unsigned*)status == 0u;
         }
         __syncthreads();
