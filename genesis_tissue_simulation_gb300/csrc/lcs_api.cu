@@ -102,6 +102,9 @@ struct Session {
     float tearLen2 = 0.f;
     // launch choice and profiling
     int launchMode = 0;                     // 0 automatic, 1 whole-GPU grid, 2 single CTA
+    // automatic mode on a mesh that fits one CTA: the session's 2nd and 3rd frames run one CTA and
+    // the whole GPU, timed; the faster shape is kept (both give the same results bit for bit)
+    int autoMode = 0, autoTrial = 0; float autoMs[2] = {0.f, 0.f}; cudaEvent_t autoEv[2] = {nullptr, nullptr};
     int clockKHz = 2000000;                 // SM clock, for the barrier spin budget
     int maxStageBytes = 0;                  // shared memory one CTA may stage the node state in
     int syncTestExtra = 0; float syncBudgetSeconds = 2.f;
@@ -133,6 +136,7 @@ void freePhysics() {
     S.fiberLambda.release(); S.feasTarget.release(); S.needed.release(); S.incOff.release(); S.incTet.release(); S.guardFlags.release();
     S.rotA.release(); S.rotB.release(); S.rotParity = 0;
     S.volumePasses = 0; S.minVolume = 0.f;
+    S.autoMode = 0; S.autoTrial = 0;
     S.physReady = false; S.toolArmed = false; S.E = S.B = S.T = 0; S.lastH = -1.f;
 }
 void freeAll() {
@@ -312,6 +316,15 @@ int launchFrame(const FrameCoeffs& fc, bool* followUp) {
     size_t stageBytes = (size_t)S.N * 2 * sizeof(float4);
     bool stage = stageBytes <= (size_t)S.maxStageBytes;
     bool single = S.launchMode == 2 || (S.launchMode == 0 && stage);
+    int timed = -1;   // automatic shape trial timed in this frame: 0 one CTA, 1 whole GPU
+    if (S.launchMode == 0 && stage) {
+        if (S.autoMode != 0) single = S.autoMode == 2;
+        else if (S.autoTrial >= 1) { timed = S.autoTrial - 1; single = timed == 0; }
+    }
+    if (timed >= 0) {
+        if (!S.autoEv[0]) { CK(cudaEventCreate(&S.autoEv[0])); CK(cudaEventCreate(&S.autoEv[1])); }
+        CK(cudaEventRecord(S.autoEv[0], S.stream));
+    }
     if (single) {
         FrameCoeffs f = fc;
         f.stageNodes = stage ? 1 : 0;
@@ -333,6 +346,15 @@ int launchFrame(const FrameCoeffs& fc, bool* followUp) {
         const bool ext = fc.guarded || fc.friction;
         CK(cudaLaunchCooperativeKernel(ext ? (const void*)frameKernelGridExt : (const void*)frameKernelGrid, dim3(ext ? S.gridBlocksExt : S.gridBlocks),
                                        dim3(kFrameThreads), args, 0, S.stream));
+    }
+    if (timed >= 0) CK(cudaEventRecord(S.autoEv[1], S.stream));
+    if (S.launchMode == 0 && stage && S.autoMode == 0) {   // after LCS_Step's synchronise: record the trial
+        S.autoTrial++;
+        if (timed >= 0) {
+            CK(cudaEventSynchronize(S.autoEv[1]));
+            CK(cudaEventElapsedTime(&S.autoMs[timed], S.autoEv[0], S.autoEv[1]));
+            if (timed == 1) S.autoMode = S.autoMs[0] <= S.autoMs[1] ? 2 : 1;
+        }
     }
     return 0;
 }
