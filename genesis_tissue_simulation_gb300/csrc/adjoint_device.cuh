@@ -155,17 +155,17 @@ __device__ __forceinline__ void tetVJP(const float* Bm, const float4 P[4], const
         vd += dot(gd[c], dx[c]);
         vh += dot(gh[c], dx[c]);
     }
-    float scale = 1.f + dampingOverH;
-    float eAd = ad / scale, eAh = ah / scale;
-    float A = dd + eAd, Bc = dh, gamma = Bc / A;
+    float scale = 1.f + dampingOverH, invScale = 1.f / scale;
+    float eAd = ad * invScale, eAh = ah * invScale;
+    float A = dd + eAd, invA = 1.f / A, Bc = dh, gamma = Bc * invA;
     float schur = eAh + eAd * gamma * gamma;
     f3 r[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) { r[c] = gh[c] - gd[c] * gamma; schur += w[c] * dot(r[c], r[c]); }
-    float rd = (-CD - dampingOverH * vd) / scale;
-    float rh = (-CH - (scale - 1.f) * vh) / scale;
+    float rd = (-CD - dampingOverH * vd) * invScale;
+    float rh = (-CH - (scale - 1.f) * vh) * invScale;
     if (!(A > 0.f) || !(schur > 0.f)) return;
-    float dlH = omega * (rh - gamma * rd) / schur, dlD = (omega * rd - Bc * dlH) / A;
+    float dlH = omega * (rh - gamma * rd) / schur, dlD = (omega * rd - Bc * dlH) * invA;
     if (!isfinite(dlD) || !isfinite(dlH)) return;
     // ---- reverse ----
     // o_c = p_c + (gd_c dlD + gh_c dlH) w_c

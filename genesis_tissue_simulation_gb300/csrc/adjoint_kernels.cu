@@ -21,6 +21,7 @@ __device__ __forceinline__ FrameCoeffs frameCoeffs(const DiffCoeffs& dc) {
     FrameCoeffs fc{};
     fc.alphaTilde = dc.alphaTilde; fc.betaGammaHS = dc.betaGammaHS; fc.omega = dc.omega;
     fc.dampingOverH = dc.dampingOverH; fc.fallback = 0; fc.fallbackInvEh2 = 0.f;
+    fc.invScale = 1.f / (1.f + fc.dampingOverH); fc.invBulkScale = fc.invScale;
     return fc;
 }
 

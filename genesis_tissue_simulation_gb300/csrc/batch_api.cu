@@ -166,6 +166,7 @@ FrameCoeffs frameCoeffs(float h) {
     fc.betaS = G.betaS;
     fc.omega = 1.f;
     fc.dampingOverH = fmaxf(0.f, G.strainDamping) / h;
+    fc.invScale = 1.f / (1.f + fc.dampingOverH); fc.invBulkScale = fc.invScale;
     fc.contact = G.armed ? 1 : 0;
     fc.contactAlphaH2 = G.cp.contactAlpha / (h * h);
     fc.spinBudget = (long long)(2.0 * 1e3 * G.clockKHz);

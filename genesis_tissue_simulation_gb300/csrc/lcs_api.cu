@@ -687,6 +687,7 @@ LCS_API int LCS_Step(float dt) {
     fc.volumePasses = S.volumePasses;
     fc.tensileStrength = S.tissueHardening;
     fc.bulkDampingOverH = S.bulkDampingSeconds / h;
+    fc.invScale = 1.f / (1.f + fc.dampingOverH); fc.invBulkScale = 1.f / (1.f + fc.bulkDampingOverH);
     fc.minVolume = S.minVolume;
     fc.contact = (S.toolArmed && S.contactModel == 0) ? 1 : 0;
     fc.friction = (S.toolArmed && S.contactModel == 1) ? 1 : 0;
@@ -965,6 +966,7 @@ LCS_API int LCS_StepNoAlloc(float dt) {
     fc.volumePasses = S.volumePasses;
     fc.tensileStrength = S.tissueHardening;
     fc.bulkDampingOverH = S.bulkDampingSeconds / h;
+    fc.invScale = 1.f / (1.f + fc.dampingOverH); fc.invBulkScale = 1.f / (1.f + fc.bulkDampingOverH);
     fc.minVolume = S.minVolume;
     fc.contact = (S.toolArmed && S.contactModel == 0) ? 1 : 0;
     fc.friction = (S.toolArmed && S.contactModel == 1) ? 1 : 0;

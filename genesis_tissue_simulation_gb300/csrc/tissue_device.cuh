@@ -78,6 +78,7 @@ struct FrameCoeffs {
     int doEdges, fallback, doBend, doStrain, perpDamp, contact, cut;
     float h, invH, invH2, alphaTilde, betaGammaHS, alphaB, betaGammaHB, velScale, betaS;
     float omega, dampingOverH, fallbackInvEh2, contactAlphaH2;
+    float invScale, invBulkScale;    // 1 / (1 + dampingOverH), 1 / (1 + bulkDampingOverH)
     int guarded, volumePasses;       // tissue guard: guarded tet form, tensile passes, feasibility chain
     float tensileStrength, bulkDampingOverH, minVolume;
     int friction;                    // contact model 1: tool SDFs, swept contact, Coulomb friction
@@ -162,10 +163,11 @@ GBT_HD ContactFrame contactFrame(const ToolPose& a, const ToolPose& b, float t, 
     return f;
 }
 
-// J^(-2/3): inverse cube root by four Newton steps in correction form y <- y + y(1 - J y^3)/3 from a
+// J^(-2/3): inverse cube root by four Newton steps in correction form y <- y + y(1 - J y^3)(1/3) from a
 // bit-level seed (the exponent trick of the fast inverse square root applied to the -1/3 power,
 // constant 0x54A23000 fitted on [0.05, 1e6]), squared.  <= 2.4 ulp from the exact power; the same
 // sequence of correctly rounded operations runs on the host, so both sides agree bit for bit.
+constexpr float kOneThird = 0.333333343f;   // 1/3 rounded to FP32
 __device__ __forceinline__ float powMinusTwoThirds(float J) {
     unsigned bits = 0x54A23000u - __float_as_uint(J) / 3u;
     float y = __uint_as_float(bits);
@@ -173,7 +175,7 @@ __device__ __forceinline__ float powMinusTwoThirds(float J) {
     for (int k = 0; k < 4; k++) {
         float y3 = (y * y) * y;
         float r = 1.f - J * y3;
-        y = y + (y * r) / 3.f;
+        y = y + (y * r) * kOneThird;
     }
     return y * y;
 }
@@ -331,16 +333,18 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
         vd += dot(gd[c], dx);
         vh += dot(gh[c], dx);
     }
-    float scale = 1.f + fc.dampingOverH, bulkScale = guarded ? 1.f + fc.bulkDampingOverH : scale;
-    float eAd = ad / scale, eAh = ah / bulkScale;
-    float A = dd + eAd, Bc = dh, gamma = Bc / A;
+    // 1 / (1 + D/h) is a frame constant; one reciprocal of A serves gamma and dlD
+    float bulkScale = guarded ? 1.f + fc.bulkDampingOverH : 1.f + fc.dampingOverH;
+    float invScale = fc.invScale, invBulk = guarded ? fc.invBulkScale : fc.invScale;
+    float eAd = ad * invScale, eAh = ah * invBulk;
+    float A = dd + eAd, invA = 1.f / A, Bc = dh, gamma = Bc * invA;
     float schur = eAh + eAd * gamma * gamma;
 #pragma unroll
     for (int c = 0; c < 4; c++) { f3 r = gh[c] - gd[c] * gamma; schur += w[c] * dot(r, r); }
-    float rd = (-CD - fc.dampingOverH * vd) / scale;
-    float rh = (-CH - (bulkScale - 1.f) * vh) / bulkScale;
+    float rd = (-CD - fc.dampingOverH * vd) * invScale;
+    float rh = (-CH - (bulkScale - 1.f) * vh) * invBulk;
     if (!(A > 0.f) || !(schur > 0.f)) return;
-    float dlH = fc.omega * (rh - gamma * rd) / schur, dlD = (fc.omega * rd - Bc * dlH) / A;
+    float dlH = fc.omega * (rh - gamma * rd) / schur, dlD = (fc.omega * rd - Bc * dlH) * invA;
     if (!isfinite(dlD) || !isfinite(dlH)) return;
     if (guarded) {
         float largest = 0.f;

@@ -104,7 +104,7 @@ static inline float powMinusTwoThirds(float J) {
     for (int k = 0; k < 4; k++) {
         float y3 = (y * y) * y;
         float r = 1.f - J * y3;
-        y = y + (y * r) / 3.f;
+        y = y + (y * r) * 0.333333343f;   // 1/3 rounded to FP32
     }
     return y * y;
 }
@@ -682,15 +682,17 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
         vd += dot(gd[k], dx); vh += dot(gh[k], dx);
     }
     (void)hh;
+    // the frame constant 1 / (1 + D/h) and one reciprocal of A (the library's form of the solve)
     Real scale = Real(1) + dampingOverH, bulkScale = guarded ? Real(1) + bulkDampingOverH : scale;
-    Real eAd = ad / scale, eAh = ah / bulkScale;
-    Real A = dd + eAd, Bc = dh, gamma = Bc / A;
+    Real invScale = Real(1) / scale, invBulk = Real(1) / bulkScale;
+    Real eAd = ad * invScale, eAh = ah * invBulk;
+    Real A = dd + eAd, invA = Real(1) / A, Bc = dh, gamma = Bc * invA;
     Real schur = eAh + eAd * gamma * gamma;
     for (int k = 0; k < 4; k++) { V3 r = gh[k] - gd[k] * gamma; schur += w[k] * dot(r, r); }
-    Real rd = (-CD - dampingOverH * vd) / scale;
-    Real rh = (-CH - (bulkScale - Real(1)) * vh) / bulkScale;
+    Real rd = (-CD - dampingOverH * vd) * invScale;
+    Real rh = (-CH - (bulkScale - Real(1)) * vh) * invBulk;
     if (!(A > 0) || !(schur > 0)) return;
-    Real dlH = S.omega * (rh - gamma * rd) / schur, dlD = (S.omega * rd - Bc * dlH) / A;
+    Real dlH = S.omega * (rh - gamma * rd) / schur, dlD = (S.omega * rd - Bc * dlH) * invA;
     if (!isFin(dlD) || !isFin(dlH)) return;
     if (guarded) {   // trust region on the update: no corner moves more than 0.15 of the shortest rest edge scale
         Real largest = 0;

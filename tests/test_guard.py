@@ -48,6 +48,18 @@ def guarded_run(lib, steps=12, minimum=0.9, passes=1, launch_mode=None, press=0.
         s.close()
 
 
+def test_pow_minus_two_thirds_accuracy(oracle_libs):
+    """J^(-2/3) of the Neo-Hookean deviatoric term (own Newton routine, identical on host and device)
+    against float64 pow: within 2.5 ulp on [0.05, 1e6]."""
+    dll = ctypes.CDLL(str(oracle_libs[0]))
+    dll.ORC_PowMinusTwoThirds.argtypes, dll.ORC_PowMinusTwoThirds.restype = (ctypes.c_double,), ctypes.c_double
+    xs = np.float32(np.concatenate([np.geomspace(0.05, 1e6, 8000), np.linspace(0.9, 1.1, 2001), [1.0, 0.05, 8.0, 27.0]]))
+    got = np.array([dll.ORC_PowMinusTwoThirds(float(x)) for x in xs], dtype=np.float32).astype(np.float64)
+    ref = xs.astype(np.float64) ** (-2.0 / 3.0)
+    err = np.abs(got - ref) / np.spacing(ref.astype(np.float32)).astype(np.float64)
+    assert err.max() <= 2.5, (float(err.max()), float(xs[err.argmax()]))
+
+
 def test_log_positive_accuracy(oracle_libs):
     """The FP32 logarithm of the guarded bulk strain (own routine, identical on host and device)
     against numpy's: within 2 ulp on [0.05, 1e4]."""
