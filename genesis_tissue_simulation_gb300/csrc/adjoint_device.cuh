@@ -180,7 +180,7 @@ __device__ __forceinline__ void tetVJP(const float* Bm, const float4 P[4], const
         gdlH += dot(gw, gh[c]);
     }
     // dlD = (omega rd - Bc dlH) / A
-    float t1 = gdlD / A;
+    float t1 = gdlD * invA;
     float grd = omega * t1;
     float gBc = -(dlH * t1);
     gdlH = gdlH - Bc * t1;
@@ -192,7 +192,7 @@ __device__ __forceinline__ void tetVJP(const float* Bm, const float4 P[4], const
     grd = grd - gamma * t2;
     float gschur = -(dlH * gdlH / schur);
     // rd = (-CD - D vd) / scale, rh = (-CH - (scale - 1) vh) / scale
-    float ud = grd / scale, uh = grh / scale;
+    float ud = grd * invScale, uh = grh * invScale;
     float gCD = -ud, gvd = -(dampingOverH * ud);
     float gCH = -uh, gvh = -((scale - 1.f) * uh);
     // schur = eAh + eAd gamma^2 + sum w_c |gh_c - gd_c gamma|^2
@@ -207,13 +207,13 @@ __device__ __forceinline__ void tetVJP(const float* Bm, const float4 P[4], const
         ggamma -= dot(gr, gd[c]);
     }
     // gamma = Bc / A, A = dd + eAd, Bc = dh
-    gBc += ggamma / A;
-    gA -= gamma * ggamma / A;
+    gBc += ggamma * invA;
+    gA -= gamma * ggamma * invA;
     float gdd = gA, gdh = gBc;
     geAd += gA;
     // eAd = ad / scale, eAh = ah / scale
-    out.gad = geAd / scale;
-    out.gah = geAh / scale;
+    out.gad = geAd * invScale;
+    out.gah = geAh * invScale;
     // dd, dh, vd, vh
 #pragma unroll
     for (int c = 0; c < 4; c++) {
