@@ -6,7 +6,7 @@
 // greedy colourings), so a batched instance evolves bit for bit as it would alone.  The packed
 // table stores colour c of every instance together (colour-major, instances in table order), which
 // gives two ways to run a frame, picked by GBT_BatchAutotune:
-//   lockstep   all instances advance colour by colour in one cooperative grid (frameKernelGrid);
+//   lockstep   all instances advance colour by colour in one cooperative grid (frameKernelLockstep);
 //   instances  one CTA per instance at a time, longest-processing-time packing over the CTAs, with
 //              only __syncthreads between colours (frameKernelInstances<256|512>).
 // GBT_BatchStepMany advances several frames with one CUDA graph launch: the instrument frames of all
@@ -103,7 +103,7 @@ int ensureDevice() {
     CK(cudaStreamCreateWithFlags(&G.stream, cudaStreamNonBlocking));
     CK(cudaMallocHost(&G.hostStatus, 4 * sizeof(unsigned)));
     int perSm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, frameKernelGrid, kFrameThreads, 0));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, frameKernelLockstep, kFrameThreads, 0));
     G.gridBlocks = std::max(1, perSm) * G.smCount;
     return 0;
 }
@@ -224,7 +224,7 @@ int launchFrame(const FrameCoeffs& fc, const ContactFrame* frames) {
         attr[0].id = cudaLaunchAttributeCooperative; attr[0].val.cooperative = 1;
         cfg.attrs = attr; cfg.numAttrs = 1;
         CK(cudaMemsetAsync(state + 1, 0, sizeof(unsigned), G.stream));
-        CK(cudaLaunchKernelEx(&cfg, frameKernelGrid, m, fc, none, none, cp, cu, state));
+        CK(cudaLaunchKernelEx(&cfg, frameKernelLockstep, m, fc, none, none, cp, cu, state));
     } else if (G.mode == 1) {
         InstanceTable it{G.nodeBaseD.p, G.nodeCountD.p, G.instEdge.p, G.instBend.p, G.instTet.p, G.order.p, G.ctaStart.p, G.derived.p};
         if (G.threads == 512) frameKernelInstances512<<<G.ctas, 512, 0, G.stream>>>(m, fc, G.cp, it);

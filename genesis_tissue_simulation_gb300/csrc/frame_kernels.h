@@ -11,6 +11,9 @@ __global__ void frameKernelGrid(DeviceMesh m, FrameCoeffs fc, ToolPose from, Too
                                 unsigned* state);
 __global__ void frameKernelBlock(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to, ContactParams cp, CutParams cu,
                                  unsigned* state);
+// the frame of batched instances in lockstep (two CTAs per SM)
+__global__ void frameKernelLockstep(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to, ContactParams cp, CutParams cu,
+                                    unsigned* state);
 // the same frames with the tissue guard and contact model 1 compiled in
 __global__ void frameKernelGridExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to, ContactParams cp, CutParams cu,
                                 unsigned* state);

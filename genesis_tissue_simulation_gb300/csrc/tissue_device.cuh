@@ -218,18 +218,17 @@ __device__ __forceinline__ EdgeRecord loadEdge(const DeviceMesh& m, int e, const
 
 // Lattice-edge distance constraint, k_solve_edges (xpbd_solver.cu:484-524).  Multipliers restart
 // at zero every substep and each edge is projected once, so the lambda term vanishes.
-template <bool Dsm = false>
-__device__ __forceinline__ void applyEdge(const DeviceMesh& m, const EdgeRecord& r, const FrameCoeffs& fc) {
-    if (r.live == 0) return;
+// The projection of edge r from its end positions pi, pj: false when the edge is dead, has no
+// mobile end or no length (nothing is written), else the new end positions.
+__device__ __forceinline__ bool solveEdge(const EdgeRecord& r, const FrameCoeffs& fc, float4 pi, float4 pj, float4& oi, float4& oj) {
+    if (r.live == 0) return false;
     float alphaTilde = fc.alphaTilde;
     if (fc.fallback) alphaTilde = fc.fallbackInvEh2 / r.rest;
-    int2 ij = r.ij;
-    float4 pi = posRef<Dsm>(m, ij.x), pj = posRef<Dsm>(m, ij.y);
     float wi = pi.w, wj = pj.w, ws = wi + wj;
-    if (ws <= 0.f) return;
+    if (ws <= 0.f) return false;
     f3 d = xyz(pi) - xyz(pj);
     float L = len(d);
-    if (L < 1e-9f) return;
+    if (L < 1e-9f) return false;
     f3 n = d * (1.f / L);
     float C = L - r.rest;
     float gamma = fc.betaGammaHS;
@@ -238,8 +237,29 @@ __device__ __forceinline__ void applyEdge(const DeviceMesh& m, const EdgeRecord&
     float ap = fc.omega * dl;
     f3 a = xyz(pi) + n * (wi * ap);
     f3 b = xyz(pj) - n * (wj * ap);
-    posRef<Dsm>(m, ij.x) = make_float4(a.x, a.y, a.z, wi);
-    posRef<Dsm>(m, ij.y) = make_float4(b.x, b.y, b.z, wj);
+    oi = make_float4(a.x, a.y, a.z, wi);
+    oj = make_float4(b.x, b.y, b.z, wj);
+    return true;
+}
+template <bool Dsm = false>
+__device__ __forceinline__ void applyEdge(const DeviceMesh& m, const EdgeRecord& r, const FrameCoeffs& fc) {
+    if (r.live == 0) return;
+    float4 oi, oj;
+    if (solveEdge(r, fc, posRef<Dsm>(m, r.ij.x), posRef<Dsm>(m, r.ij.y), oi, oj)) {
+        posRef<Dsm>(m, r.ij.x) = oi;
+        posRef<Dsm>(m, r.ij.y) = oj;
+    }
+}
+// Two edges of one colour at once: members of a colour touch disjoint nodes, so both edges' ends
+// are loaded before either is written and the two projections overlap.
+template <bool Dsm = false>
+__device__ __forceinline__ void applyEdgePair(const DeviceMesh& m, const EdgeRecord& r0, const EdgeRecord& r1, const FrameCoeffs& fc) {
+    const float4 a0 = posRef<Dsm>(m, r0.ij.x), b0 = posRef<Dsm>(m, r0.ij.y);
+    const float4 a1 = posRef<Dsm>(m, r1.ij.x), b1 = posRef<Dsm>(m, r1.ij.y);
+    float4 oa0, ob0, oa1, ob1;
+    const bool k0 = solveEdge(r0, fc, a0, b0, oa0, ob0), k1 = solveEdge(r1, fc, a1, b1, oa1, ob1);
+    if (k0) { posRef<Dsm>(m, r0.ij.x) = oa0; posRef<Dsm>(m, r0.ij.y) = ob0; }
+    if (k1) { posRef<Dsm>(m, r1.ij.x) = oa1; posRef<Dsm>(m, r1.ij.y) = ob1; }
 }
 
 // Bending angle constraint, k_solve_bending (xpbd_solver.cu:534-573); off unless kb > 0.
