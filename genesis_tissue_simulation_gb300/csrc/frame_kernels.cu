@@ -607,7 +607,7 @@ __global__ void __launch_bounds__(kFrameThreads, 1) frameKernelGrid(DeviceMesh m
 // table holds several elements per thread.
 __global__ void __launch_bounds__(kFrameThreads, 2) frameKernelLockstep(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                      ContactParams cp, CutParams cu, unsigned* state) {
-    gridFrame<false, false>(m, fc, from, to, cp, cu, state);
+    gridFrame<false, true>(m, fc, from, to, cp, cu, state);
 }
 __global__ void __launch_bounds__(kFrameThreads, 1) frameKernelGridExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                      ContactParams cp, CutParams cu, unsigned* state) {
