@@ -309,9 +309,9 @@ __device__ __noinline__ void frictionPhase(const DeviceMesh& m, const FrameCoeff
 // plain path's register allocation (the extended kernel launches only when either is armed).
 // Dsm: node positions live in the cluster's distributed shared memory (cluster batch kernel).
 // Rotations: the session kernels, which also compute the particle frames (batched instances do not).
-// Pairs: a thread takes its edges of a colour two at a time (the whole-GPU single-mesh kernels,
-// where the registers allow it).
-template <class Sync, bool Extended, bool Dsm = false, bool Rotations = false, bool Pairs = false>
+// EdgeGroup: a thread takes its edges of a colour this many at a time (2 in the whole-GPU kernels;
+// four at a time measured slower on the batch: the extra registers spill).
+template <class Sync, bool Extended, bool Dsm = false, bool Rotations = false, int EdgeGroup = 1>
 __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
                          const ContactParams& cp, const CutParams& cu, unsigned* state, Sync& sync) {
     const int r = sync.spreadRank(), R = sync.size();
@@ -389,7 +389,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         if (fc.doEdges)
             for (int c = 0; c < m.nEdgeColors; c++) {
                 int2 rg = m.edgeRange[c];
-                if (Pairs) {
+                if (EdgeGroup == 2) {
                     for (int e = rg.x + r; e < rg.y; e += 2 * R) {
                         if (e + R < rg.y) applyEdgePair<Dsm>(m, loadEdge(m, e, fc), loadEdge(m, e + R, fc), fc);
                         else applyEdge<Dsm>(m, loadEdge(m, e, fc), fc);
@@ -591,27 +591,27 @@ __global__ void __launch_bounds__(512) frameKernelInstances512(DeviceMesh m, Fra
     runInstances(m, fc, cp, it);
 }
 
-template <bool Extended, bool Pairs>
+template <bool Extended, int EdgeGroup>
 __device__ __forceinline__ void gridFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
                                           const ContactParams& cp, const CutParams& cu, unsigned* state) {
     GridSync g{state + 1, state + 2, gridDim.x, 0u, fc.spinBudget, (unsigned)fc.syncTestExtra};
-    runFrame<GridSync, Extended, false, true, Pairs>(m, fc, from, to, cp, cu, state, g);
+    runFrame<GridSync, Extended, false, true, EdgeGroup>(m, fc, from, to, cp, cu, state, g);
 }
 // A single mesh: one CTA per SM, so the tet projection keeps its registers without spilling (a
 // colour of ~19 k tets still finds a warp for every scheduler).
 __global__ void __launch_bounds__(kFrameThreads, 1) frameKernelGrid(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                   ContactParams cp, CutParams cu, unsigned* state) {
-    gridFrame<false, true>(m, fc, from, to, cp, cu, state);
+    gridFrame<false, 2>(m, fc, from, to, cp, cu, state);
 }
 // Batched instances in lockstep: two CTAs per SM (128 registers), since every colour of the packed
 // table holds several elements per thread.
 __global__ void __launch_bounds__(kFrameThreads, 2) frameKernelLockstep(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                      ContactParams cp, CutParams cu, unsigned* state) {
-    gridFrame<false, true>(m, fc, from, to, cp, cu, state);
+    gridFrame<false, 2>(m, fc, from, to, cp, cu, state);
 }
 __global__ void __launch_bounds__(kFrameThreads, 1) frameKernelGridExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                      ContactParams cp, CutParams cu, unsigned* state) {
-    gridFrame<true, true>(m, fc, from, to, cp, cu, state);
+    gridFrame<true, 2>(m, fc, from, to, cp, cu, state);
 }
 
 // One CTA per mesh.  When fc.stageNodes is set the whole node state (positions and substep-start
