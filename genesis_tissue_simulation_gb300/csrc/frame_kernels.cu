@@ -143,9 +143,8 @@ __device__ void markEdge(const DeviceMesh& m, const CutParams& cu, const float* 
     }
 }
 
-__device__ void tickEdge(const DeviceMesh& m, const CutParams& cu, int e, bool ccd, const float* rot) {
-    int4 g = cu.gridEdges[e];          // (axis, x, y, z)
-    int axis = g.x;
+__device__ void tickEdgeAt(const DeviceMesh& m, const CutParams& cu, int4 g, bool ccd, const float* rot) {
+    int axis = g.x;                    // g = (axis, x, y, z) of the base node
     int a = nodeId(m, g.y, g.z, g.w);
     int b = nodeId(m, g.y + (axis == 0), g.z + (axis == 1), g.w + (axis == 2));
     int slotA = 6 * a + 2 * axis + 1;
@@ -233,6 +232,60 @@ __device__ void tickEdge(const DeviceMesh& m, const CutParams& cu, int e, bool c
 
 // ---------------------------------------------------------------------------------------------
 // tissue guard: the feasibility chain after contact (finishFeasible, xpbd_solver.cu:628-741)
+__device__ __forceinline__ void tickEdge(const DeviceMesh& m, const CutParams& cu, int e, bool ccd, const float* rot) {
+    tickEdgeAt(m, cu, cu.gridEdges[e], ccd, rot);
+}
+
+// Brick pre-cull of the ribbon tick: the lattice's base nodes in bricks of 4 x 4 x 4, each brick's
+// box over the current and substep-start positions of its nodes and of the +1 layer that its edges
+// reach.  An edge whose brick box misses the blade's padded box misses it too, so only the edges of
+// listed bricks run the crossing test; the rest of the tick (the sever of marked edges) has nothing
+// to do on the others: rod-phase marks are severed when made, tick marks are made on listed edges,
+// and the tear law (which visits every edge) keeps the full pass.
+constexpr int kBrick = 4, kBrickEdges = 3 * kBrick * kBrick * kBrick;
+__device__ void brickBounds(const DeviceMesh& m, const CutParams& cu, int b, int lane) {
+    const int nbx = (m.dx + kBrick - 1) / kBrick, nby = (m.dy + kBrick - 1) / kBrick;
+    const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+    const int x0 = bx * kBrick, y0 = by * kBrick, z0 = bz * kBrick;
+    const int x1 = min(x0 + kBrick, m.dx), y1 = min(y0 + kBrick, m.dy), z1 = min(z0 + kBrick, m.dz);
+    const int nx = x1 - x0 + 1, ny = y1 - y0 + 1, count = nx * ny * (z1 - z0 + 1);
+    f3 lo = mk(3.0e38f, 3.0e38f, 3.0e38f), hi = mk(-3.0e38f, -3.0e38f, -3.0e38f);
+    for (int k = lane; k < count; k += 32) {
+        const int id = nodeId(m, x0 + k % nx, y0 + (k / nx) % ny, z0 + k / (nx * ny));
+        const f3 p = xyz(m.pos[id]), q = xyz(m.prev[id]);
+        lo = mk(fminf(lo.x, fminf(p.x, q.x)), fminf(lo.y, fminf(p.y, q.y)), fminf(lo.z, fminf(p.z, q.z)));
+        hi = mk(fmaxf(hi.x, fmaxf(p.x, q.x)), fmaxf(hi.y, fmaxf(p.y, q.y)), fmaxf(hi.z, fmaxf(p.z, q.z)));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = mk(fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o)), fminf(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, o)),
+                fminf(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, o)));
+        hi = mk(fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, o)), fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, o)),
+                fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, o)));
+    }
+    if (lane != 0) return;
+    const float pad = cu.voxelL;
+    const bool miss = hi.x < fminf(cu.sx, cu.ex) - pad || lo.x > fmaxf(cu.sx, cu.ex) + pad ||
+                      hi.y < fminf(cu.sy, cu.ey) - pad || lo.y > fmaxf(cu.sy, cu.ey) + pad ||
+                      hi.z < fminf(cu.sz, cu.ez) - pad || lo.z > fmaxf(cu.sz, cu.ez) + pad;
+    if (!miss) {
+        const unsigned slot = atomicAdd(cu.brickCount, 1u);
+        if (slot < (unsigned)cu.nBricks) cu.brickList[slot] = b;
+    }
+}
+// Edge `l` (0 .. kBrickEdges-1) of a listed brick as (axis, base node), or false when the lattice has
+// no such interior edge (one whose four incident voxels exist, as the host's edge list holds).
+__device__ __forceinline__ bool brickEdge(const DeviceMesh& m, int b, int l, int4& g) {
+    const int nbx = (m.dx + kBrick - 1) / kBrick, nby = (m.dy + kBrick - 1) / kBrick;
+    const int axis = l / (kBrick * kBrick * kBrick), o = l % (kBrick * kBrick * kBrick);
+    const int x = (b % nbx) * kBrick + o % kBrick, y = ((b / nbx) % nby) * kBrick + (o / kBrick) % kBrick,
+              z = (b / (nbx * nby)) * kBrick + o / (kBrick * kBrick);
+    const int c[3] = {x, y, z}, d[3] = {m.dx, m.dy, m.dz};
+    for (int a = 0; a < 3; a++)
+        if (a == axis ? c[a] >= d[a] : (c[a] < 1 || c[a] >= d[a])) return false;
+    g = make_int4(axis, x, y, z);
+    return true;
+}
+
 // ---------------------------------------------------------------------------------------------
 // If a live tet is below the minimum relative volume: two colour sweeps of a linearised repair; if
 // one still is: every vertex of a tet whose substep motion may pass below the minimum restarts from
@@ -492,8 +545,20 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 const unsigned pointsBefore = rotations ? *(volatile unsigned*)(cu.counters + 1) : 0u;
                 if (!sync.sync()) return;
                 const float* rot = rotations ? m.particleRot[rotParity] : nullptr;
-                for (int e = r; e < cu.nGridEdges; e += R) tickEdge(m, cu, e, true, rot);
+                if (cu.brickList && cu.tearLen2 <= 0.f) {   // only the bricks near the blade
+                    const int nb = ((m.dx + kBrick - 1) / kBrick) * ((m.dy + kBrick - 1) / kBrick) * ((m.dz + kBrick - 1) / kBrick);
+                    for (int b = r >> 5; b < nb; b += R >> 5) brickBounds(m, cu, b, r & 31);
+                    if (!sync.sync()) return;
+                    const int listed = min((int)*(volatile unsigned*)cu.brickCount, nb);
+                    for (int j = r; j < listed * kBrickEdges; j += R) {
+                        int4 g;
+                        if (brickEdge(m, cu.brickList[j / kBrickEdges], j % kBrickEdges, g)) tickEdgeAt(m, cu, g, true, rot);
+                    }
+                } else {
+                    for (int e = r; e < cu.nGridEdges; e += R) tickEdge(m, cu, e, true, rot);
+                }
                 if (!sync.sync()) return;
+                if (sync.leader() && cu.brickCount) *cu.brickCount = 0u;   // every reader has passed the barrier above
                 mark(s, kPhaseTick);
                 // a tick that emitted cut points is followed by fresh frames before the next substep
                 // (V/physics.cu:368-379)

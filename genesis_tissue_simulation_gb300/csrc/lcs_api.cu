@@ -97,6 +97,7 @@ struct Session {
     DBuf<int4> gridEdges; DBuf<unsigned> occupied, cutMask, counters; DBuf<int> inside; DBuf<float> skinTD, edgeCutT;
     DBuf<int> conn;                         // [4096 x 9] components of the voxel corners per 12-bit cut mask
     DBuf<float4> cutRec;                    // [2 x 6N] cut points per directed lattice slot
+    DBuf<int> brickList; DBuf<unsigned> brickCount; int nBricks = 0;   // ribbon-tick brick pre-cull
     float emitNcut[3] = {0.f, 1.f, 0.f};    // last valid world cut normal of the blade
     bool toolSet = false, havePrev = false, pressure = false; CutToolDesc cutTool{};
     float tearLen2 = 0.f;
@@ -120,7 +121,7 @@ int cudaStatus(cudaError_t e) { return e == cudaSuccess ? 0 : -(int)e; }
 
 void freeCut() {
     S.gridEdges.release(); S.occupied.release(); S.cutMask.release(); S.counters.release(); S.inside.release();
-    S.conn.release(); S.cutRec.release();
+    S.conn.release(); S.cutRec.release(); S.brickList.release(); S.brickCount.release(); S.nBricks = 0;
     S.cutFP.release(); S.cutNrmFixed.release(); S.rawTri.release(); S.faces.release(); S.faceCap = 0;
     S.emitNcut[0] = 0.f; S.emitNcut[1] = 1.f; S.emitNcut[2] = 0.f;
     S.skinTD.release(); S.edgeCutT.release();
@@ -302,6 +303,7 @@ CutParams cutParams() {
     c.ex = S.cutTool.t1v2[0]; c.ey = S.cutTool.t1v2[1]; c.ez = S.cutTool.t1v2[2];
     c.voxelL = S.cd.voxelL; c.tearLen2 = S.tearLen2; c.havePrev = S.havePrev ? 1 : 0;
     c.cutRec = S.cutRec.p; c.toolD = S.cutTool.d; c.ncx = S.emitNcut[0]; c.ncy = S.emitNcut[1]; c.ncz = S.emitNcut[2];
+    c.brickList = S.brickList.p; c.brickCount = S.brickCount.p; c.nBricks = S.nBricks;
     return c;
 }
 
@@ -313,6 +315,7 @@ int launchFrame(const FrameCoeffs& fc, bool* followUp) {
     CutParams cu = cutParams();
     unsigned* state = S.state.p;
     CK(cudaMemsetAsync(state + 1, 0, 2 * sizeof(unsigned), S.stream));
+    if (S.brickCount.p) CK(cudaMemsetAsync(S.brickCount.p, 0, sizeof(unsigned), S.stream));
     size_t stageBytes = (size_t)S.N * 2 * sizeof(float4);
     bool stage = stageBytes <= (size_t)S.maxStageBytes;
     bool single = S.launchMode == 2 || (S.launchMode == 0 && stage);
@@ -614,6 +617,31 @@ LCS_API int LCS_InitCut(const CutInitDesc* desc, const void* conn4096, const voi
     }
     CK(S.cutRec.alloc((size_t)12 * S.N));
     CK(cudaMemsetAsync(S.cutRec.p, 0, (size_t)12 * S.N * sizeof(float4), S.stream));
+    {   // the ribbon tick may enumerate edges by lattice bricks only if the edge list is the full
+        // interior set (every edge whose four incident voxels exist), each once
+        const int d[3] = {S.dx, S.dy, S.dz};
+        long long expected = 0;
+        for (int a = 0; a < 3; a++) expected += (long long)d[a] * (d[(a + 1) % 3] - 1) * (d[(a + 2) % 3] - 1);
+        bool full = expected == desc->gridEdgeCount;
+        std::vector<unsigned char> seen(full ? (size_t)3 * S.N : 0, 0);
+        const int* g = (const int*)gridEdges;
+        for (int e = 0; full && e < desc->gridEdgeCount; e++) {
+            const int axis = g[4 * e], c[3] = {g[4 * e + 1], g[4 * e + 2], g[4 * e + 3]};
+            if (axis < 0 || axis > 2) { full = false; break; }
+            for (int a = 0; a < 3; a++)
+                if (a == axis ? (c[a] < 0 || c[a] >= d[a]) : (c[a] < 1 || c[a] >= d[a])) full = false;
+            if (!full) break;
+            const size_t slot = 3 * ((size_t)c[0] + (S.dx + 1) * ((size_t)c[1] + (S.dy + 1) * (size_t)c[2])) + axis;
+            if (seen[slot]) full = false;
+            seen[slot] = 1;
+        }
+        if (full) {
+            const int k = 4;
+            S.nBricks = ((S.dx + k - 1) / k) * ((S.dy + k - 1) / k) * ((S.dz + k - 1) / k);
+            CK(S.brickList.alloc(S.nBricks)); CK(S.brickCount.alloc(1));
+            CK(cudaMemsetAsync(S.brickCount.p, 0, sizeof(unsigned), S.stream));
+        }
+    }
     if (S.surfaceReady && S.conn.p) {   // the cut voxels' share of the surface: component points, walls
         CK(S.cutFP.alloc((size_t)8 * S.nVox)); CK(S.cutNrmFixed.alloc((size_t)24 * S.nVox));
         CK(cudaMemsetAsync(S.cutFP.p, 0, (size_t)8 * S.nVox * sizeof(float4), S.stream));
@@ -982,6 +1010,7 @@ LCS_API int LCS_StepNoAlloc(float dt) {
     // written again for this session's tets.
     CK(cudaMemsetAsync(state, 0xFF, sizeof(unsigned), S.stream));
     CK(cudaMemsetAsync(state + 1, 0, 3 * sizeof(unsigned), S.stream));
+    if (S.brickCount.p) CK(cudaMemsetAsync(S.brickCount.p, 0, sizeof(unsigned), S.stream));
     if (fc.doStrain) {
         tetAlphaKernel<<<(S.T + 255) / 256, 256, 0, S.stream>>>(S.T, fc.invH2, S.tetStiff.p, alpha);
         CK(cudaGetLastError());

@@ -113,6 +113,9 @@ struct CutParams {
     float4* cutRec;
     float toolD;          // blade thickness D
     float ncx, ncy, ncz;  // last valid world cut normal of the blade
+    // brick pre-cull of the ribbon tick (null: every edge): listed bricks and their count, which
+    // the tick leaves at zero
+    int* brickList; unsigned* brickCount; int nBricks;
     float sx, sy, sz, ex, ey, ez;     // current blade segment S -> E
     float voxelL, tearLen2;
     int havePrev;
