@@ -217,6 +217,10 @@ __device__ void tickEdgeAt(const DeviceMesh& m, const CutParams& cu, int4 g, boo
     for (int s = 0; s < 4; s++)
         valid = valid && voxIn(m, g.y + kStencilOff[axis][s][0], g.z + kStencilOff[axis][s][1], g.w + kStencilOff[axis][s][2]);
     if (!valid || !edgeIsCut(m, cu, g)) return;
+    // When every live bend pair's links exist (checked when the physics is set up, and kept: a
+    // sever kills the pairs of the link it removes), an edge whose link is already gone has no live
+    // pair left, and the pass below would change nothing.
+    if (cu.skipSevered && m.nbr[slotA] < 0) return;
     if (m.nbr[slotA] >= 0) atomicAdd(cu.counters + 0, 1u);
     m.nbr[slotA] = -1;
     m.nbr[6 * b + 2 * axis] = -1;
@@ -549,6 +553,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                     const int nb = ((m.dx + kBrick - 1) / kBrick) * ((m.dy + kBrick - 1) / kBrick) * ((m.dz + kBrick - 1) / kBrick);
                     for (int b = r >> 5; b < nb; b += R >> 5) brickBounds(m, cu, b, r & 31);
                     if (!sync.sync()) return;
+                    mark(s, kPhaseTickBricks);
                     const int listed = min((int)*(volatile unsigned*)cu.brickCount, nb);
                     for (int j = r; j < listed * kBrickEdges; j += R) {
                         int4 g;

@@ -98,6 +98,7 @@ struct Session {
     DBuf<int> conn;                         // [4096 x 9] components of the voxel corners per 12-bit cut mask
     DBuf<float4> cutRec;                    // [2 x 6N] cut points per directed lattice slot
     DBuf<int> brickList; DBuf<unsigned> brickCount; int nBricks = 0;   // ribbon-tick brick pre-cull
+    bool bendsFollowLinks = false;          // every live bend pair (i; j, k) has the links i-j and i-k
     float emitNcut[3] = {0.f, 1.f, 0.f};    // last valid world cut normal of the blade
     bool toolSet = false, havePrev = false, pressure = false; CutToolDesc cutTool{};
     float tearLen2 = 0.f;
@@ -304,6 +305,7 @@ CutParams cutParams() {
     c.voxelL = S.cd.voxelL; c.tearLen2 = S.tearLen2; c.havePrev = S.havePrev ? 1 : 0;
     c.cutRec = S.cutRec.p; c.toolD = S.cutTool.d; c.ncx = S.emitNcut[0]; c.ncy = S.emitNcut[1]; c.ncz = S.emitNcut[2];
     c.brickList = S.brickList.p; c.brickCount = S.brickCount.p; c.nBricks = S.nBricks;
+    c.skipSevered = S.bendsFollowLinks ? 1 : 0;
     return c;
 }
 
@@ -432,6 +434,15 @@ LCS_API int LCS_InitPhysics(const PhysicsInitDesc* desc, const float* mass, cons
     std::memcpy(S.typeB, hm.typeB, sizeof(S.typeB));
     S.E = E; S.B = B; S.T = T;
     const BendRecord* bp = (const BendRecord*)bendPairs;
+    S.bendsFollowLinks = true;
+    for (int q = 0; q < bpc && S.bendsFollowLinks; q++) {
+        if (bp[q].alive == 0) continue;
+        const int i = bp[q].i;
+        bool hj = false, hk = false;
+        if (i >= 0 && i < cc)
+            for (int t = 0; t < 6; t++) { hj = hj || nbrIdx[6 * (size_t)i + t] == bp[q].j; hk = hk || nbrIdx[6 * (size_t)i + t] == bp[q].k; }
+        S.bendsFollowLinks = hj && hk && bp[q].j >= 0 && bp[q].k >= 0;
+    }
     std::vector<float4> zero4(cc, make_float4(0, 0, 0, 0));
     CK(S.pos.upload(hm.pos.data(), cc, S.stream));
     CK(S.prev.upload(hm.pos.data(), cc, S.stream));
@@ -915,9 +926,9 @@ LCS_API void LCS_ProfileSections(int enabled) {
 }
 LCS_API int LCS_ProfileSectionsRead(char* text, int capacity) {
     static const char* names[8] = {"frame start", "liveness and predict", "edge colours", "bend colours", "tet colours",
-                                   "contact and velocity", "ribbon tick", ""};
+                                   "contact and velocity", "ribbon tick", "ribbon tick bricks"};
     std::string out;
-    for (int k = 1; k < 7; k++) {
+    for (int k = 1; k < 8; k++) {
         if (!S.sectionCount[k]) continue;
         char line[160];
         snprintf(line, sizeof line, "%s=%.4f count=%lld\n", names[k], S.sectionMs[k], S.sectionCount[k]);

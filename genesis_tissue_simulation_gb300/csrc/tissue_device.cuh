@@ -94,7 +94,7 @@ struct FrameCoeffs {
 
 // Phase tags of the section profiler; one 64-bit record per phase end: (tag << 56) | nanoseconds.
 enum PhaseTag : unsigned { kPhaseFrameStart = 0, kPhasePredict = 1, kPhaseEdges = 2, kPhaseBends = 3, kPhaseTets = 4,
-                           kPhaseVelocity = 5, kPhaseTick = 6 };
+                           kPhaseVelocity = 5, kPhaseTick = 6, kPhaseTickBricks = 7 };
 constexpr int kPhaseRecordsPerSubstep = 128;
 
 // Shaft capsule + jaw slab of contact model 0 (XpbdToolState, xpbd_solver.h:223-229).
@@ -116,6 +116,7 @@ struct CutParams {
     // brick pre-cull of the ribbon tick (null: every edge): listed bricks and their count, which
     // the tick leaves at zero
     int* brickList; unsigned* brickCount; int nBricks;
+    int skipSevered;      // every live bend pair's two links exist (see the sever in the tick)
     float sx, sy, sz, ex, ey, ez;     // current blade segment S -> E
     float voxelL, tearLen2;
     int havePrev;
