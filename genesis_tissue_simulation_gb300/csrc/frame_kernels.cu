@@ -252,11 +252,23 @@ __device__ void brickBounds(const DeviceMesh& m, const CutParams& cu, int b, int
     const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
     const int x0 = bx * kBrick, y0 = by * kBrick, z0 = bz * kBrick;
     const int x1 = min(x0 + kBrick, m.dx), y1 = min(y0 + kBrick, m.dy), z1 = min(z0 + kBrick, m.dz);
-    const int nx = x1 - x0 + 1, ny = y1 - y0 + 1, count = nx * ny * (z1 - z0 + 1);
+    // the (kBrick + 1)^3 = 125 node slots of the brick, four per lane (constant divisors), all loads
+    // issued before any use; slots past the lattice's last layer are skipped
+    constexpr int kSide = kBrick + 1;
     f3 lo = mk(3.0e38f, 3.0e38f, 3.0e38f), hi = mk(-3.0e38f, -3.0e38f, -3.0e38f);
-    for (int k = lane; k < count; k += 32) {
-        const int id = nodeId(m, x0 + k % nx, y0 + (k / nx) % ny, z0 + k / (nx * ny));
-        const f3 p = xyz(m.pos[id]), q = xyz(m.prev[id]);
+    float4 P[4], Q[4];
+    bool in[4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        const int k = lane + 32 * t;
+        const int x = x0 + k % kSide, y = y0 + (k / kSide) % kSide, z = z0 + k / (kSide * kSide);
+        in[t] = k < kSide * kSide * kSide && x <= x1 && y <= y1 && z <= z1;
+        if (in[t]) { const int id = nodeId(m, x, y, z); P[t] = m.pos[id]; Q[t] = m.prev[id]; }
+    }
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        if (!in[t]) continue;
+        const f3 p = xyz(P[t]), q = xyz(Q[t]);
         lo = mk(fminf(lo.x, fminf(p.x, q.x)), fminf(lo.y, fminf(p.y, q.y)), fminf(lo.z, fminf(p.z, q.z)));
         hi = mk(fmaxf(hi.x, fmaxf(p.x, q.x)), fmaxf(hi.y, fmaxf(p.y, q.y)), fmaxf(hi.z, fmaxf(p.z, q.z)));
     }
