@@ -24,13 +24,8 @@ namespace gbt {
 // ---------------------------------------------------------------------------------------------
 // The substep's instrument frame (contactFrame) lives in tissue_device.cuh: batches evaluate it on
 // the host, single meshes on the device, with the same operations.
-template <bool Dsm = false>
-__device__ __forceinline__ void contactNode(const DeviceMesh& m, int c, const ContactFrame& f, const ContactParams& cp) {
-    float4 P = posRef<Dsm>(m, c);
-    float wc = P.w;
-    if (wc <= 0.f) return;
-    f3 p = xyz(P);
-    f3 v = xyz(m.vel[c]);
+// The contact of one mobile node (wc > 0) at p moving with the substep's predicted velocity v.
+__device__ __forceinline__ f3 contactPoint(f3 p, float wc, f3 v, const ContactFrame& f, const ContactParams& cp) {
     {
         f3 ab = f.sb - f.sa;
         float ab2 = dot(ab, ab);
@@ -67,7 +62,29 @@ __device__ __forceinline__ void contactNode(const DeviceMesh& m, int c, const Co
             }
         }
     }
-    posRef<Dsm>(m, c) = make_float4(p.x, p.y, p.z, wc);
+    return p;
+}
+template <bool Dsm = false>
+__device__ __forceinline__ void contactNode(const DeviceMesh& m, int c, const ContactFrame& f, const ContactParams& cp) {
+    const float4 P = posRef<Dsm>(m, c);
+    if (P.w <= 0.f) return;
+    const f3 p = contactPoint(xyz(P), P.w, xyz(m.vel[c]), f, cp);
+    posRef<Dsm>(m, c) = make_float4(p.x, p.y, p.z, P.w);
+}
+
+// k_predict on one node whose position P (w = inverse mass), velocity V and external force F are
+// in registers: x_prev = x; v += h f w; x += h v.
+template <bool Dsm = false>
+__device__ __forceinline__ void predictNode(const DeviceMesh& m, int i, float4 P, f3 V, float4 F, float h) {
+    m.prev[i] = make_float4(P.x, P.y, P.z, 0.f);
+    if (P.w > 0.f) {
+        f3 a = mk(F.x, F.y, F.z) * P.w;
+        f3 v = V + a * h;
+        m.vel[i] = make_float4(v.x, v.y, v.z, 0.f);
+        f3 x = xyz(P) + v * h;
+        P = make_float4(x.x, x.y, x.z, P.w);
+    }
+    posRef<Dsm>(m, i) = P;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -380,7 +397,10 @@ __device__ __noinline__ void frictionPhase(const DeviceMesh& m, const FrameCoeff
 // Rotations: the session kernels, which also compute the particle frames (batched instances do not).
 // EdgeGroup: a thread takes its edges of a colour this many at a time (2 in the whole-GPU kernels;
 // four at a time measured slower on the batch: the extra registers spill).
-template <class Sync, bool Extended, bool Dsm = false, bool Rotations = false, int EdgeGroup = 1>
+// Ahead (only where registers allow: the one-CTA-per-SM kernels): with edge pairs, the thread's
+// first pair of colour c+1 is loaded before colour c's edges are projected, and the node passes
+// take two nodes at a time.
+template <class Sync, bool Extended, bool Dsm = false, bool Rotations = false, int EdgeGroup = 1, bool Ahead = false>
 __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
                          const ContactParams& cp, const CutParams& cu, unsigned* state, Sync& sync) {
     const int r = sync.spreadRank(), R = sync.size();
@@ -403,6 +423,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
     // Session kernels only, where positions are plain memory (Dsm is false).
     const bool rotations = Rotations && fc.rotations != 0;
     int rotParity = fc.rotParity;
+    bool predicted = false;   // the substep's predict already ran in the previous substep's velocity pass
     auto framePass = [&]() {
         const float* prevRot = m.particleRot[rotParity];
         float* rot = m.particleRot[rotParity ^ 1];
@@ -433,21 +454,21 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
             derivedAt = revision;
         }
         const int nodeEnd = m.nodeBase + m.nNodes;
-        // -- predict (k_predict) --
-        for (int i = m.nodeBase + r; i < nodeEnd; i += R) {
-            float4 P = posRef<Dsm>(m, i);
-            if (stale) P.w = nodeInvMass(m, i);
-            m.prev[i] = make_float4(P.x, P.y, P.z, 0.f);
-            if (P.w > 0.f) {
-                float4 F = m.ext[i], V = m.vel[i];
-                f3 a = mk(F.x, F.y, F.z) * P.w;
-                f3 v = xyz(V) + a * fc.h;
-                m.vel[i] = make_float4(v.x, v.y, v.z, 0.f);
-                f3 x = xyz(P) + v * fc.h;
-                P = make_float4(x.x, x.y, x.z, P.w);
+        // -- predict (k_predict), unless the previous substep's velocity pass already did it --
+        // With Ahead a thread takes its nodes two at a time, both nodes' loads ahead of either's stores.
+        if (!predicted)
+            for (int i = m.nodeBase + r; i < nodeEnd; i += (Ahead ? 2 : 1) * R) {
+                const int j = Ahead ? i + R : nodeEnd;
+                float4 Pi = posRef<Dsm>(m, i), Vi = m.vel[i], Fi = m.ext[i], Pj, Vj, Fj;
+                if (j < nodeEnd) { Pj = posRef<Dsm>(m, j); Vj = m.vel[j]; Fj = m.ext[j]; }
+                if (stale) Pi.w = nodeInvMass(m, i);
+                predictNode<Dsm>(m, i, Pi, xyz(Vi), Fi, fc.h);
+                if (j < nodeEnd) {
+                    if (stale) Pj.w = nodeInvMass(m, j);
+                    predictNode<Dsm>(m, j, Pj, xyz(Vj), Fj, fc.h);
+                }
             }
-            posRef<Dsm>(m, i) = P;
-        }
+        predicted = false;
         if (!sync.sync()) return;
         mark(s, kPhasePredict);
         // -- coloured Gauss-Seidel sweeps --
@@ -455,20 +476,49 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         // substep-start positions, none of which the sweep writes) before the barrier that closes
         // colour c, so only the gathers of current positions follow the barrier.  (Loading further
         // ahead inside a colour costs more in registers, hence occupancy, than it saves; measured.)
-        if (fc.doEdges)
+        // the thread's first tet of colour 0 (loaded before the last edge barrier with Ahead)
+        TetRecord next;
+        bool hasNext = false, tetLoaded = false;
+        auto loadFirstTet = [&]() {
+            const int2 first = m.nTetColors > 0 ? m.tetRange[0] : make_int2(0, 0);
+            hasNext = first.x + r < first.y;
+            if (hasNext) next = loadTet(m, first.x + r);
+            tetLoaded = true;
+        };
+        if (fc.doEdges) {
+            EdgeRecord n0, n1;
+            bool h0 = false, h1 = false;
+            if (Ahead && EdgeGroup == 2 && m.nEdgeColors > 0) {
+                const int2 g0 = m.edgeRange[0];
+                h0 = g0.x + r < g0.y; h1 = g0.x + r + R < g0.y;
+                if (h0) n0 = loadEdge(m, g0.x + r, fc);
+                if (h1) n1 = loadEdge(m, g0.x + r + R, fc);
+            }
             for (int c = 0; c < m.nEdgeColors; c++) {
                 int2 rg = m.edgeRange[c];
-                if (EdgeGroup == 2) {
-                    for (int e = rg.x + r; e < rg.y; e += 2 * R) {
+                if (Ahead && EdgeGroup == 2) {
+                    const EdgeRecord c0 = n0, c1 = n1;
+                    const bool k0 = h0, k1 = h1;
+                    if (c + 1 < m.nEdgeColors) {
+                        const int2 ng = m.edgeRange[c + 1];
+                        h0 = ng.x + r < ng.y; h1 = ng.x + r + R < ng.y;
+                        if (h0) n0 = loadEdge(m, ng.x + r, fc);
+                        if (h1) n1 = loadEdge(m, ng.x + r + R, fc);
+                    }
+                    if (k1) applyEdgePair<Dsm>(m, c0, c1, fc);
+                    else if (k0) applyEdge<Dsm>(m, c0, fc);
+                    for (int e = rg.x + r + 2 * R; e < rg.y; e += 2 * R) {
                         if (e + R < rg.y) applyEdgePair<Dsm>(m, loadEdge(m, e, fc), loadEdge(m, e + R, fc), fc);
                         else applyEdge<Dsm>(m, loadEdge(m, e, fc), fc);
                     }
                 } else {
                     for (int e = rg.x + r; e < rg.y; e += R) applyEdge<Dsm>(m, loadEdge(m, e, fc), fc);
                 }
+                if (Ahead && c + 1 == m.nEdgeColors && fc.doStrain && !fc.doBend) loadFirstTet();
                 if (!sync.sync()) return;
                 mark(s, kPhaseEdges);
             }
+        }
         if (fc.doBend)
             for (int c = 0; c < m.nBendColors; c++) {
                 int2 rg = m.bendRange[c];
@@ -477,10 +527,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 mark(s, kPhaseBends);
             }
         if (fc.doStrain) {
-            TetRecord next;
-            int2 first = m.nTetColors > 0 ? m.tetRange[0] : make_int2(0, 0);
-            bool hasNext = first.x + r < first.y;
-            if (hasNext) next = loadTet(m, first.x + r);
+            if (!tetLoaded) loadFirstTet();
             for (int c = 0; c < m.nTetColors; c++) {
                 int2 rg = m.tetRange[c];
                 TetRecord cur = next;
@@ -512,19 +559,40 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 for (int i = m.nodeBase + r; i < nodeEnd; i += R) contactNode(m, i, cf, cp);
             if (!guardFeasible(m, fc, fc.firstSubstep + s + 1, sync)) return;
         }
-        for (int i = m.nodeBase + r; i < nodeEnd; i += R) {
-            if (fc.contact && !guarded) {
-                if (m.nodeInstance) {   // batched instances: each node meets its own instance's tool
-                    const ContactFrame& own = m.contactFrames[(size_t)(fc.firstSubstep + s) * m.nInstances + m.nodeInstance[i]];
-                    contactNode<Dsm>(m, i, own, cp);
-                } else {
-                    contactNode<Dsm>(m, i, cf, cp);
-                }
+        // Without ⟂ damping or a blade the next substep's predict needs nothing but the node's own
+        // state, so it follows each node's velocity update here, in registers (no barrier lies
+        // between them anyway).  With Ahead a thread takes its nodes two at a time, loads ahead of
+        // stores.
+        predicted = s + 1 < fc.substeps && !fc.perpDamp && !fc.cut;
+        const bool touch = fc.contact && !guarded;
+        auto velocityNode = [&](int i, float4 P, float4 Q, float4 V, float4 F) {
+            if (touch && P.w > 0.f) {
+                const ContactFrame* own = &cf;   // batched instances: each node meets its own instance's tool
+                if (m.nodeInstance) own = &m.contactFrames[(size_t)(fc.firstSubstep + s) * m.nInstances + m.nodeInstance[i]];
+                const f3 p = contactPoint(xyz(P), P.w, xyz(V), *own, cp);
+                P = make_float4(p.x, p.y, p.z, P.w);
             }
-            float4 P = posRef<Dsm>(m, i), Q = m.prev[i];
             f3 v = P.w > 0.f ? (xyz(P) - xyz(Q)) * fc.invH : mk(0.f, 0.f, 0.f);
             if (!fc.perpDamp) v = P.w > 0.f ? v * fc.velScale : mk(0.f, 0.f, 0.f);
+            if (predicted && P.w > 0.f) {
+                predictNode<Dsm>(m, i, P, v, F, fc.h);
+                return;
+            }
             m.vel[i] = make_float4(v.x, v.y, v.z, 0.f);
+            if (predicted) predictNode<Dsm>(m, i, P, v, F, fc.h);
+            else if (touch) posRef<Dsm>(m, i) = P;
+        };
+        for (int i = m.nodeBase + r; i < nodeEnd; i += (Ahead ? 2 : 1) * R) {
+            const int j = Ahead ? i + R : nodeEnd;
+            const float4 Pi = posRef<Dsm>(m, i), Qi = m.prev[i];
+            const float4 Vi = touch ? m.vel[i] : make_float4(0.f, 0.f, 0.f, 0.f), Fi = predicted ? m.ext[i] : Vi;
+            float4 Pj, Qj, Vj, Fj;
+            if (j < nodeEnd) {
+                Pj = posRef<Dsm>(m, j); Qj = m.prev[j];
+                Vj = touch ? m.vel[j] : make_float4(0.f, 0.f, 0.f, 0.f); Fj = predicted ? m.ext[j] : Vj;
+            }
+            velocityNode(i, Pi, Qi, Vi, Fi);
+            if (j < nodeEnd) velocityNode(j, Pj, Qj, Vj, Fj);
         }
         if (fc.perpDamp) {   // k_perp_damp_edges between the raw velocity write and the Rayleigh scale
             if (!sync.sync()) return;
@@ -673,27 +741,27 @@ __global__ void __launch_bounds__(512) frameKernelInstances512(DeviceMesh m, Fra
     runInstances(m, fc, cp, it);
 }
 
-template <bool Extended, int EdgeGroup>
+template <bool Extended, int EdgeGroup, bool Ahead>
 __device__ __forceinline__ void gridFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
                                           const ContactParams& cp, const CutParams& cu, unsigned* state) {
     GridSync g{state + 1, state + 2, gridDim.x, 0u, fc.spinBudget, (unsigned)fc.syncTestExtra};
-    runFrame<GridSync, Extended, false, true, EdgeGroup>(m, fc, from, to, cp, cu, state, g);
+    runFrame<GridSync, Extended, false, true, EdgeGroup, Ahead>(m, fc, from, to, cp, cu, state, g);
 }
 // A single mesh: one CTA per SM, so the tet projection keeps its registers without spilling (a
 // colour of ~19 k tets still finds a warp for every scheduler).
 __global__ void __launch_bounds__(kFrameThreads, 1) frameKernelGrid(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                   ContactParams cp, CutParams cu, unsigned* state) {
-    gridFrame<false, 2>(m, fc, from, to, cp, cu, state);
+    gridFrame<false, 2, true>(m, fc, from, to, cp, cu, state);
 }
 // Batched instances in lockstep: two CTAs per SM (128 registers), since every colour of the packed
 // table holds several elements per thread.
 __global__ void __launch_bounds__(kFrameThreads, 2) frameKernelLockstep(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                      ContactParams cp, CutParams cu, unsigned* state) {
-    gridFrame<false, 2>(m, fc, from, to, cp, cu, state);
+    gridFrame<false, 2, false>(m, fc, from, to, cp, cu, state);
 }
 __global__ void __launch_bounds__(kFrameThreads, 1) frameKernelGridExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                      ContactParams cp, CutParams cu, unsigned* state) {
-    gridFrame<true, 2>(m, fc, from, to, cp, cu, state);
+    gridFrame<true, 2, false>(m, fc, from, to, cp, cu, state);
 }
 
 // One CTA per mesh.  When fc.stageNodes is set the whole node state (positions and substep-start
