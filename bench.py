@@ -52,28 +52,37 @@ def ncu_traffic_per_launch(name):
 
 
 class ClockSampler:
-    """nvidia-smi clock and throttle-reason samples every 200 ms while running."""
+    """nvidia-smi clock and throttle-reason samples every 50 ms.  The sampler is started, and its
+    first sample awaited, before the timed region opens, so nvidia-smi's start-up (which briefly
+    holds the driver) falls outside it; the summary keeps the samples taken inside the region (the
+    last one before it when the region is shorter than the sampling period)."""
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device_index):
         self.device = device_index
         self.lines, self.proc = [], None
+        self.t0 = self.t1 = None
+        self.first = threading.Event()
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                          "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
+            self.first.wait(timeout=10.0)
         except OSError:
             self.proc = None
+        self.t0 = time.perf_counter()
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+            self.first.set()
 
     def __exit__(self, *exc):
+        self.t1 = time.perf_counter()
         if self.proc:
             self.proc.terminate()
             try:
@@ -82,9 +91,12 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        inside = [l for t, l in self.lines if self.t0 is not None and self.t0 <= t <= (self.t1 or t)]
+        before = [l for t, l in self.lines if self.t0 is not None and t < self.t0]
+        use = inside or before[-1:]
         sm, mx, reasons = [], None, set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for line in self.lines:
+        for line in use:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -97,7 +109,7 @@ class ClockSampler:
                 if flag.lower().startswith("active"):
                     reasons.add(name)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(inside), "sampled": "inside the timed region" if inside else "just before the timed region"}
 
 
 def dist_setup():
