@@ -342,10 +342,11 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, ra
         torch.cuda.synchronize()
         device_s = b.profile_read() / 1e3
         b.profile(0)
+        positions = np.empty((b.total_nodes, 3), dtype=np.float32)
         e0 = time.perf_counter()
         for k in range(warmup + frames, warmup + 2 * frames):
             b.step_many([w.capsules_at(k + 1)], use_graph=True)
-            positions = b.positions()
+            b.positions(out=positions)
         e2e_s = time.perf_counter() - e0
         assert np.isfinite(positions).all(), "non-finite batched state"
     counts = torch.tensor([info["nodes"], info["edges"], info["tets"]], dtype=torch.float64, device="cuda")
@@ -402,7 +403,7 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, ra
                                                                   f"{plain_frames} frames each after 2 warm-up frames",
         "batched_over_plain": value / plain_rate,
         "e2e": {"value": count * frames / e2e_s, "unit": "instance-steps/s", "h2d_bytes_per_step": 92 * count,
-                "d2h_bytes_per_step": 16 * info["nodes"]},
+                "d2h_bytes_per_step": 12 * info["nodes"]},
         "l2": "state larger than L2 (no flush)",
         "roofline": {"bound": "hbm", "achieved": achieved, "unit": "GB/s", "algorithmic_bytes_per_launch": w.substeps * bytes_per_substep,
                      "traffic": ncu_traffic_per_launch("ncu_batch_frame_c4")},

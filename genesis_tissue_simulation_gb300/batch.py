@@ -117,8 +117,12 @@ class TissueBatch:
         self.check("GBT_BatchAutotune", self.dt, trial_steps, ct.byref(mode), ct.byref(threads), ms)
         return {"mode": mode.value, "threads": threads.value, "ms_per_frame": [float(v) for v in ms]}
 
-    def positions(self):
-        out = np.empty((self.total_nodes, 3), dtype=np.float32)
+    def positions(self, out=None):
+        """Every instance's node positions [total_nodes, 3]; into `out` when given (float32, C order)."""
+        if out is None:
+            out = np.empty((self.total_nodes, 3), dtype=np.float32)
+        elif out.shape != (self.total_nodes, 3) or out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise ValueError("positions: out must be a C-ordered float32 array of shape (total_nodes, 3)")
         self.check("GBT_BatchGetPositions", pointer(out))
         return out
 

@@ -59,7 +59,7 @@ struct Batch {
     Buf<ContactFrame> frames;
     unsigned* hostStatus = nullptr;
     ContactFrame* framesHost = nullptr; size_t framesHostCap = 0;
-    float4* posHost = nullptr; size_t posHostCap = 0;   // pinned staging for GBT_BatchGetPositions
+    Buf<float> packedXyz;                             // GBT_BatchGetPositions: xyz packed on the device (3N)
     // instruments
     std::vector<ToolPose> toolFrom, tool;
     bool armed = false;
@@ -87,8 +87,7 @@ void releaseAll() {
     G.derived.release(); G.state.release(); G.frames.release();
     if (G.framesHost) cudaFreeHost(G.framesHost);
     G.framesHost = nullptr; G.framesHostCap = 0;
-    if (G.posHost) cudaFreeHost(G.posHost);
-    G.posHost = nullptr; G.posHostCap = 0;
+    G.packedXyz.release();
     for (cudaEvent_t e : G.events) cudaEventDestroy(e);
     G.events.clear();
     G.ready = false; G.armed = false; G.lastH = -1.f;
@@ -468,6 +467,7 @@ LCS_API int GBT_BatchInit(int count, const GbtInstanceDesc* inst, const GbtBatch
     std::vector<unsigned> derived(count, ~0u), state(4, 0u);
     state[0] = ~0u;
     CK(G.pos.upload(pos.data(), G.N, G.stream)); CK(G.prev.upload(pos.data(), G.N, G.stream));
+    CK(G.packedXyz.alloc((size_t)3 * G.N));
     CK(G.vel.upload(zero4.data(), G.N, G.stream)); CK(G.ext.upload(ext.data(), G.N, G.stream));
     CK(G.pinned.upload(pinned.data(), G.N, G.stream)); CK(G.active.upload(active.data(), G.N, G.stream));
     CK(G.nbr.upload(nbr.data(), nbr.size(), G.stream)); CK(G.nodeInstance.upload(nodeInst.data(), G.N, G.stream));
@@ -522,18 +522,15 @@ LCS_API int GBT_BatchStepMany(float dt, int steps, const void* tools, int useGra
     return stepFrames(dt, steps, (const ToolPose*)tools, useGraph != 0);
 }
 
+// Every instance's node positions (3N floats, packed-table order): packed by a kernel, then one
+// copy straight into the caller's buffer (no host repacking).
 LCS_API int GBT_BatchGetPositions(float* out3N) {
     if (!G.ready || !out3N) return XPBD_ERR_BAD_ARG;
-    if (G.posHostCap < (size_t)G.N) {
-        if (G.posHost) cudaFreeHost(G.posHost);
-        G.posHost = nullptr; G.posHostCap = 0;
-        CK(cudaMallocHost(&G.posHost, G.N * sizeof(float4)));
-        G.posHostCap = G.N;
-    }
-    const float4* p = G.posHost;
-    CK(cudaMemcpyAsync(G.posHost, G.pos.p, G.N * sizeof(float4), cudaMemcpyDeviceToHost, G.stream));
+    if (G.packedXyz.n < (size_t)3 * G.N) CK(G.packedXyz.alloc((size_t)3 * G.N));
+    packXyzKernel<<<(G.N + 255) / 256, 256, 0, G.stream>>>(G.N, G.pos.p, G.packedXyz.p);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out3N, G.packedXyz.p, (size_t)3 * G.N * sizeof(float), cudaMemcpyDeviceToHost, G.stream));
     CK(cudaStreamSynchronize(G.stream));
-    for (int i = 0; i < G.N; i++) { out3N[3 * i] = p[i].x; out3N[3 * i + 1] = p[i].y; out3N[3 * i + 2] = p[i].z; }
     return 0;
 }
 

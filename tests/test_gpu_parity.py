@@ -24,7 +24,7 @@ def trajectory(workload, lib, steps, every, launch_mode=None, topology=False):
 
         def observe(k, s):
             if (k + 1) % every == 0:
-                rec = {"pos": s.positions()}
+                rec = {"pos": s.positions(), "vel": s.velocities()}
                 if topology:
                     rec.update(nbr=s.neighbors(), rev=s.topology_revision(), mask=s.voxel_cut_mask(),
                                frac=s.cut_edge_fractions(), bends=s.bend_alive(), dbg=s.cut_debug()[15:17].copy())
@@ -78,6 +78,7 @@ def test_c2_capsule_small_matches_oracle(gpu_lib, oracle_libs):
     cpu = trajectory(w, oracle_libs[0], 40, 10)
     for a, b in zip(gpu, cpu):
         assert np.array_equal(a["pos"], b["pos"]), float(np.abs(a["pos"] - b["pos"]).max())
+        assert np.array_equal(a["vel"], b["vel"]), float(np.abs(a["vel"] - b["vel"]).max())
 
 
 def test_c3_cut_small_topology_bit_exact(gpu_lib, oracle_libs):
@@ -87,7 +88,7 @@ def test_c3_cut_small_topology_bit_exact(gpu_lib, oracle_libs):
     assert cpu[-1]["rev"] > 0, "the blade never crossed the tissue"
     for a, b in zip(gpu, cpu):
         assert a["rev"] == b["rev"]
-        for key in ("nbr", "mask", "frac", "bends", "dbg", "pos"):
+        for key in ("nbr", "mask", "frac", "bends", "dbg", "pos", "vel"):
             assert np.array_equal(a[key], b[key]), key
 
 
