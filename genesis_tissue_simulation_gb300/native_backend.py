@@ -526,6 +526,13 @@ def _device_floats(address, count):
     return torch.as_tensor(_View(), device="cuda").cpu().numpy()
 
 
+def severed_edges(baseline, current):
+    """Lattice links cut since `baseline` (scenario.py:392-394): both are neighbour tables [N, 6]
+    (slot 2a: -axis a, 2a+1: +axis a); each undirected link is counted once, on its +axis slot."""
+    before, after = np.asarray(baseline)[:, 1::2], np.asarray(current)[:, 1::2]
+    return int(np.count_nonzero((before >= 0) & (after < 0)))
+
+
 def blade_sweep(prev_start, prev_end, start, end, thickness=0.02):
     """Swept blade quad as the two triangles T1=(Sprev,Eprev,E), T2=(Sprev,E,S) of a ``CutTool`` (V/cut.h:29-38).
 

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from genesis_tissue_simulation_gb300 import workloads as W
-from genesis_tissue_simulation_gb300.native_backend import XPBD_ERR_BAD_DT, LCS_ERR_DEVICE_TIMEOUT
+from genesis_tissue_simulation_gb300.native_backend import XPBD_ERR_BAD_DT, LCS_ERR_DEVICE_TIMEOUT, severed_edges
 
 pytestmark = pytest.mark.gpu
 
@@ -88,6 +88,8 @@ def test_c3_cut_small_topology_bit_exact(gpu_lib, oracle_libs):
     assert cpu[-1]["rev"] > 0, "the blade never crossed the tissue"
     for a, b in zip(gpu, cpu):
         assert a["rev"] == b["rev"]
+        # the revision counts links severed, each once (V/cut.cu:719-746)
+        assert a["rev"] == severed_edges(w.grid.neighbors, a["nbr"])
         for key in ("nbr", "mask", "frac", "bends", "dbg", "pos", "vel"):
             assert np.array_equal(a[key], b[key]), key
 

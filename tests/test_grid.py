@@ -115,3 +115,21 @@ def test_invalid_spacing_rejected():
         build_grid(0.05)
     with pytest.raises(ValueError):
         build_grid(0.2, vertical_spacing=0.3)
+
+
+def test_severed_edges_counts_each_link_once():
+    """Known answer of the reference's undirected cut count (test_core.py:233-236): one link between
+    nodes 0 and 1, seen from both ends, cut once."""
+    from genesis_tissue_simulation_gb300.native_backend import severed_edges
+    baseline = np.full((2, 6), -1, dtype=np.int32)
+    baseline[0, 1], baseline[1, 0] = 1, 0
+    assert severed_edges(baseline, np.full_like(baseline, -1)) == 1
+    assert severed_edges(baseline, baseline) == 0
+    g = build_grid(0.5, size=(2.0, 1.0, 1.5))
+    cut = g.neighbors.copy()
+    live = np.argwhere(cut[:, 1::2] >= 0)
+    i, a = live[len(live) // 2]
+    j = cut[i, 2 * a + 1]
+    cut[i, 2 * a + 1] = cut[j, 2 * a] = -1
+    assert severed_edges(g.neighbors, cut) == 1
+
