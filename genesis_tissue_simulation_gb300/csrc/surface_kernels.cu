@@ -514,7 +514,14 @@ __global__ void __launch_bounds__(kSurfaceThreads) surfaceKernel(SurfaceMesh s, 
         while (fcap < 2 * T) fcap <<= 1;
         for (int k = r; k < fcap; k += R) s.faces[k] = make_int4(-1, 0, 0x7fffffff, 0x7fffffff);
         if (!g.sync()) return;
+        // A triangle whose three vertices are all intact feature points (no cut tag) is never repeated:
+        // its three voxels lie around exactly one surface edge, and its key differs from every key
+        // holding a cut point.  Only triangles with a cut point enter the table; the others stay.
+        auto intact = [&](int i) {
+            return (((unsigned)s.raw[3 * i] | (unsigned)s.raw[3 * i + 1] | (unsigned)s.raw[3 * i + 2]) & kCutTag) == 0u;
+        };
         for (int i = r; i < T; i += R) {
+            if (intact(i)) continue;
             unsigned key[3]; bool odd;
             faceKey(s.raw + 3 * i, key, &odd);
             const unsigned h = faceHash(key, fcap);
@@ -529,6 +536,7 @@ __global__ void __launch_bounds__(kSurfaceThreads) surfaceKernel(SurfaceMesh s, 
         if (!g.sync()) return;
         const int ct = (T + G - 1) / G, t0 = min(T, b * ct), t1 = min(T, t0 + ct);
         auto keep = [&](int i) {
+            if (intact(i)) return true;
             unsigned key[3]; bool odd;
             faceKey(s.raw + 3 * i, key, &odd);
             const unsigned h = faceHash(key, fcap);
