@@ -84,7 +84,7 @@ struct Session {
     DBuf<int> voxelCorner, isectOff, isectCnt, surfVox, tri, nrmFixed, blockTotal;
     DBuf<IsectRec> isect; DBuf<int4> surfEdges; DBuf<float4> fp, fpRest, outAux; DBuf<float> outPos, outNrm;
     DBuf<unsigned> surfSync, triCount;
-    DBuf<float4> cutFP; DBuf<int> cutNrmFixed, rawTri; DBuf<int4> faces; int faceCap = 0;   // cut voxels' surface
+    DBuf<float4> cutFP; DBuf<int> cutNrmFixed, rawTri, wallCount; DBuf<int4> faces; int faceCap = 0;   // cut voxels' surface
     unsigned* hostState = nullptr;          // pinned mirror of state + cut counters
     DBuf<float> packedXyz;                  // node getters: xyz packed on the device (3N floats)
     // tool / contact
@@ -124,7 +124,7 @@ int cudaStatus(cudaError_t e) { return e == cudaSuccess ? 0 : -(int)e; }
 void freeCut() {
     S.gridEdges.release(); S.occupied.release(); S.cutMask.release(); S.counters.release(); S.inside.release();
     S.conn.release(); S.cutRec.release(); S.brickList.release(); S.brickCount.release(); S.nBricks = 0;
-    S.cutFP.release(); S.cutNrmFixed.release(); S.rawTri.release(); S.faces.release(); S.faceCap = 0;
+    S.cutFP.release(); S.cutNrmFixed.release(); S.rawTri.release(); S.wallCount.release(); S.faces.release(); S.faceCap = 0;
     S.emitNcut[0] = 0.f; S.emitNcut[1] = 1.f; S.emitNcut[2] = 0.f;
     S.skinTD.release(); S.edgeCutT.release();
     S.cutReady = false; S.toolSet = false; S.havePrev = false;
@@ -195,7 +195,7 @@ int buildSurface() {
         m.nbr = S.nbr.p; m.rot = S.rotParity ? S.rotB.p : S.rotA.p; m.cutT = S.edgeCutT.p; m.cutMask = S.cutMask.p;
         m.conn = S.conn.p; m.occupied = S.occupied.p; m.inside = S.inside.p; m.skinT = S.skinTD.p; m.active = S.active.p;
         m.cutRec = S.cutRec.p; m.cutFP = S.cutFP.p; m.cutNrmFixed = S.cutNrmFixed.p; m.raw = S.rawTri.p;
-        m.faces = S.faces.p; m.faceCap = S.faceCap;
+        m.faces = S.faces.p; m.faceCap = S.faceCap; m.wallCount = S.wallCount.p;
     }
     m.fp = S.fp.p; m.fpRest = S.fpRest.p; m.nrmFixed = S.nrmFixed.p;
     m.tri = S.tri.p; m.triCount = S.triCount.p; m.blockTotal = S.blockTotal.p;
@@ -656,7 +656,7 @@ LCS_API int LCS_InitCut(const CutInitDesc* desc, const void* conn4096, const voi
         }
     }
     if (S.surfaceReady && S.conn.p) {   // the cut voxels' share of the surface: component points, walls
-        CK(S.cutFP.alloc((size_t)8 * S.nVox)); CK(S.cutNrmFixed.alloc((size_t)24 * S.nVox));
+        CK(S.cutFP.alloc((size_t)8 * S.nVox)); CK(S.cutNrmFixed.alloc((size_t)24 * S.nVox)); CK(S.wallCount.alloc((size_t)S.nVox));
         CK(cudaMemsetAsync(S.cutFP.p, 0, (size_t)8 * S.nVox * sizeof(float4), S.stream));
         CK(S.rawTri.alloc((size_t)3 * S.triCapacity));
         int cap = 1;

@@ -35,6 +35,7 @@ struct SurfaceMesh {
     int* cutNrmFixed;                   // [3 x 8V] their fixed-point normal sums
     int* raw;                           // [3 cap] triangles before internal faces cancel
     int4* faces; int faceCap;           // hash table of triangle keys (power of two entries)
+    int* wallCount;                     // [V] wall faces of a cut voxel, then the index of its first face (-1: none)
     float* outPos; float* outNrm; float4* outAux;   // [3 cap] vertex soup: xyz, xyz, rest anchor + wall flag
 };
 

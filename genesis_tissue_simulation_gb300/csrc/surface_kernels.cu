@@ -151,102 +151,130 @@ __device__ __forceinline__ bool cutHitsMaterial(float t, float skin, int ia, int
 // that box, and projected onto the plane of its cut points.  The cut points of v are those of its
 // 12 edges, gathered here in a fixed order (edge, then the low owner before the high one), so the
 // sums do not depend on scheduling (the reference adds them with float atomics).
-__device__ void componentPoints(const SurfaceMesh& s, int v) {
+// The 32 lanes of a warp work on one cut voxel (all lanes call with the same v): lane j < 24 gathers
+// half-edge j's cut point (edge j / 2, low owner first) and lane k < 12 skin crossing k, all at
+// once; every sum then runs in that fixed order through shuffles, and lane c < 8 finishes component
+// c.  A few dependent round trips per voxel instead of one per half-edge.
+__device__ __forceinline__ f3 shfl3(f3 a, int src) {
+    return mk(__shfl_sync(0xffffffffu, a.x, src), __shfl_sync(0xffffffffu, a.y, src), __shfl_sync(0xffffffffu, a.z, src));
+}
+__device__ void componentPointsWarp(const SurfaceMesh& s, int v, int lane) {
     const unsigned mask = s.cutMask[v] & 0xFFFu;
     const int vx = v % s.dx, vy = (v / s.dx) % s.dy, vz = v / (s.dx * s.dy);
     const int* c = s.voxelCorner + 8 * (size_t)v;
     const int compCount = s.conn[9 * mask];
-    f3 acc[8]; int cnt[8], nx[8], ny[8], nz[8];
-    for (int k = 0; k < 8; k++) { acc[k] = mk(0.f, 0.f, 0.f); cnt[k] = 0; nx[k] = ny[k] = nz[k] = 0; }
-    for (int le = 0; le < 12; le++) {
-        const int ca = kEdgeCorners[le][0], cb = kEdgeCorners[le][1];
-        const int axis = kCorner[ca][0] != kCorner[cb][0] ? 0 : (kCorner[ca][1] != kCorner[cb][1] ? 1 : 2);
-        const bool aLow = kCorner[ca][axis] < kCorner[cb][axis];
-        const int lcs[2] = {aLow ? ca : cb, aLow ? cb : ca};   // low end, high end
-        for (int h = 0; h < 2; h++) {
-            const int owner = c[lcs[h]];
-            const size_t slot = 6 * (size_t)owner + 2 * axis + (h == 0 ? 1 : 0);
-            const float4 L = s.cutRec[2 * slot];
-            if (L.w == 0.f || s.active[owner] == 0) continue;
+    // corners: lane r < 8 holds corner r's id, deformed position and component
+    const int cid = lane < 8 ? c[lane] : 0;
+    const f3 cpos = lane < 8 ? xyz(s.pos[cid]) : mk(0.f, 0.f, 0.f);
+    const int ccomp = lane < 8 ? compOf(s, mask, lane) : -1;
+    // half-edge j = lane
+    const int le = lane < 24 ? lane >> 1 : 0, h = lane & 1;
+    const int ca = kEdgeCorners[le][0], cb = kEdgeCorners[le][1];
+    const int axis = kCorner[ca][0] != kCorner[cb][0] ? 0 : (kCorner[ca][1] != kCorner[cb][1] ? 1 : 2);
+    const bool aLow = kCorner[ca][axis] < kCorner[cb][axis];
+    const int lcOwn = h == 0 ? (aLow ? ca : cb) : (aLow ? cb : ca);
+    const int owner = __shfl_sync(0xffffffffu, cid, lcOwn);
+    const int comp = __shfl_sync(0xffffffffu, ccomp, lcOwn);
+    int root = 8;
+    for (int q = 7; q >= 0; q--) if (__shfl_sync(0xffffffffu, ccomp, q) == comp) root = q;
+    const f3 origin = shfl3(cpos, root < 8 ? root : 0);
+    bool valid = false;
+    f3 local = mk(0.f, 0.f, 0.f);
+    int fx = 0, fy = 0, fz = 0;
+    if (lane < 24) {
+        const size_t slot = 6 * (size_t)owner + 2 * axis + (h == 0 ? 1 : 0);
+        const float4 L = s.cutRec[2 * slot];
+        if (L.w != 0.f && s.active[owner] != 0) {
+            valid = true;
             const float4 Mn = s.cutRec[2 * slot + 1];
-            const int comp = compOf(s, mask, lcs[h]);
-            int root = 0;
-            while (root < 8 && compOf(s, mask, root) != comp) root++;
-            const f3 origin = xyz(s.pos[c[root]]);
             const float* q = s.rot + 9 * (size_t)owner;
             const f3 r0 = mk(q[0], q[1], q[2]), r1 = mk(q[3], q[4], q[5]), r2 = mk(q[6], q[7], q[8]);
             const f3 lo = mk(L.x, L.y, L.z), mn = mk(Mn.x, Mn.y, Mn.z);
-            const f3 local = (xyz(s.pos[owner]) - origin) + mk(dot(r0, lo), dot(r1, lo), dot(r2, lo));
+            local = (xyz(s.pos[owner]) - origin) + mk(dot(r0, lo), dot(r1, lo), dot(r2, lo));
             const f3 nw = mk(dot(r0, mn), dot(r1, mn), dot(r2, mn));
-            acc[comp] = acc[comp] + local;
-            cnt[comp]++;
-            nx[comp] += (int)rintf(nw.x * kPosScale); ny[comp] += (int)rintf(nw.y * kPosScale); nz[comp] += (int)rintf(nw.z * kPosScale);
+            fx = (int)rintf(nw.x * kPosScale); fy = (int)rintf(nw.y * kPosScale); fz = (int)rintf(nw.z * kPosScale);
         }
     }
-    // the voxel's skin crossings and the corner owning each after the cut
-    const int off = s.isectOff[v], ncross = s.isectCnt[v];
-    f3 world[12]; int owner[12];
-    for (int k = 0; k < ncross && k < 12; k++) {
-        const IsectRec& it = s.isect[off + k];
-        world[k] = crossingWorld(s, it);
+    // lane `lane` (< 8) accumulates component `lane` in half-edge order
+    f3 acc = mk(0.f, 0.f, 0.f);
+    int cnt = 0, nx = 0, ny = 0, nz = 0;
+    for (int j = 0; j < 24; j++) {
+        const bool vj = __shfl_sync(0xffffffffu, valid, j);
+        const int cj = __shfl_sync(0xffffffffu, comp, j);
+        const f3 lj = shfl3(local, j);
+        const int xj = __shfl_sync(0xffffffffu, fx, j), yj = __shfl_sync(0xffffffffu, fy, j), zj = __shfl_sync(0xffffffffu, fz, j);
+        if (vj && cj == lane) { acc = acc + lj; cnt++; nx += xj; ny += yj; nz += zj; }
+    }
+    // skin crossings: lane k < ncross
+    const int off = s.isectOff[v], ncross = min(s.isectCnt[v], 12);
+    f3 wk = mk(0.f, 0.f, 0.f), nk = mk(0.f, 0.f, 0.f);
+    int ok = -1;
+    if (lane < ncross) {
+        const IsectRec& it = s.isect[off + lane];
+        wk = crossingWorld(s, it);
+        nk = mk(it.nx, it.ny, it.nz);
         const float cT = s.cutT ? s.cutT[directedSlot(s, it.a, it.b)] : -1.f;
         const int in = skinOwnerA(it.t, cT, it.insideA) ? it.a : it.b;
         const int nxn = s.dx + 1, nyn = s.dy + 1;
         const int lc = localCorner(in % nxn - vx, (in / nxn) % nyn - vy, in / (nxn * nyn) - vz);
-        owner[k] = lc < 0 ? -1 : compOf(s, mask, lc);
+        ok = lc < 0 ? -1 : compOf(s, mask, lc);
     }
     f3 half = xyz(s.rest[c[6]]) - xyz(s.rest[c[0]]);
     half = mk(fabsf(half.x) * .5f, fabsf(half.y) * .5f, fabsf(half.z) * .5f);
-    for (int comp = 0; comp < 8; comp++) {
-        const size_t slot = 8 * (size_t)v + comp;
-        s.cutNrmFixed[3 * slot] = 0; s.cutNrmFixed[3 * slot + 1] = 0; s.cutNrmFixed[3 * slot + 2] = 0;
-        if (comp >= compCount) { s.cutFP[slot] = make_float4(0.f, 0.f, 0.f, 0.f); continue; }
-        f3 bc = mk(0.f, 0.f, 0.f), origin = mk(0.f, 0.f, 0.f);
-        int nCorn = 0;
-        for (int lc = 0; lc < 8; lc++) {
-            if (compOf(s, mask, lc) != comp) continue;
-            const f3 p = xyz(s.pos[c[lc]]);
-            if (nCorn == 0) origin = p;
-            bc = bc + p;
-            nCorn++;
-        }
-        if (nCorn > 0) bc = mk(bc.x / (float)nCorn, bc.y / (float)nCorn, bc.z / (float)nCorn);
-        f3 sum = mk(0.f, 0.f, 0.f);
-        int nIncl = 0;
-        for (int k = 0; k < ncross && k < 12; k++) if (owner[k] == comp) { sum = sum + world[k]; nIncl++; }
-        const int ccnt = cnt[comp];
-        if (ccnt > 0) sum = (sum + acc[comp]) + origin * (float)ccnt;
-        const int total = nIncl + ccnt;
-        if (total == 0) { s.cutFP[slot] = make_float4(0.f, 0.f, 0.f, 0.f); continue; }
-        f3 x = mk(sum.x / (float)total, sum.y / (float)total, sum.z / (float)total);
-        if (nIncl > 0) {
-            for (int it = 0; it < s.qefIters; it++) {
-                f3 F = mk(0.f, 0.f, 0.f);
-                for (int k = 0; k < ncross && k < 12; k++) {
-                    if (owner[k] != comp) continue;
-                    const IsectRec& rec = s.isect[off + k];
-                    const f3 n = mk(rec.nx, rec.ny, rec.nz);
-                    F = F + n * dot(n, world[k] - x);
-                }
-                const float a = 0.1f * (1.0f - (float)it / (float)s.qefIters);
-                const f3 xn = x + F * a;
-                if (fabsf(xn.x - bc.x) >= half.x || fabsf(xn.y - bc.y) >= half.y || fabsf(xn.z - bc.z) >= half.z) break;
-                x = xn;
-            }
-        }
-        x = mk(fminf(fmaxf(x.x, bc.x - half.x), bc.x + half.x), fminf(fmaxf(x.y, bc.y - half.y), bc.y + half.y),
-               fminf(fmaxf(x.z, bc.z - half.z), bc.z + half.z));
-        if (ccnt > 0) {   // onto the plane of the component's own cut points
-            const f3 nAcc = mk((float)nx[comp] / kPosScale, (float)ny[comp] / kPosScale, (float)nz[comp] / kPosScale);
-            const float nLen = len(nAcc);
-            if (nLen > 1e-6f && nLen > 0.25f * (float)ccnt) {
-                const f3 nbar = mk(nAcc.x / nLen, nAcc.y / nLen, nAcc.z / nLen);
-                const f3 cutC = mk(acc[comp].x / (float)ccnt, acc[comp].y / (float)ccnt, acc[comp].z / (float)ccnt) + origin;
-                x = x - nbar * dot(nbar, x - cutC);
-            }
-        }
-        s.cutFP[slot] = make_float4(x.x, x.y, x.z, 1.f);
+    // component `lane`
+    const int me = lane;
+    f3 bc = mk(0.f, 0.f, 0.f), corigin = mk(0.f, 0.f, 0.f);
+    int nCorn = 0;
+    for (int q = 0; q < 8; q++) {
+        const int cq = __shfl_sync(0xffffffffu, ccomp, q);
+        const f3 pq = shfl3(cpos, q);
+        if (cq != me) continue;
+        if (nCorn == 0) corigin = pq;
+        bc = bc + pq;
+        nCorn++;
     }
+    if (nCorn > 0) bc = mk(bc.x / (float)nCorn, bc.y / (float)nCorn, bc.z / (float)nCorn);
+    f3 sum = mk(0.f, 0.f, 0.f);
+    int nIncl = 0;
+    for (int k = 0; k < ncross; k++) {
+        const int ow = __shfl_sync(0xffffffffu, ok, k);
+        const f3 w = shfl3(wk, k);
+        if (ow == me) { sum = sum + w; nIncl++; }
+    }
+    if (cnt > 0) sum = (sum + acc) + corigin * (float)cnt;
+    const int total = nIncl + cnt;
+    f3 x = total > 0 ? mk(sum.x / (float)total, sum.y / (float)total, sum.z / (float)total) : mk(0.f, 0.f, 0.f);
+    bool walking = nIncl > 0 && total > 0;
+    for (int it = 0; it < s.qefIters; it++) {   // every lane runs every iteration (the shuffles)
+        f3 F = mk(0.f, 0.f, 0.f);
+        for (int k = 0; k < ncross; k++) {
+            const int ow = __shfl_sync(0xffffffffu, ok, k);
+            const f3 w = shfl3(wk, k), n = shfl3(nk, k);
+            if (ow == me) F = F + n * dot(n, w - x);
+        }
+        if (walking) {
+            const float a = 0.1f * (1.0f - (float)it / (float)s.qefIters);
+            const f3 xn = x + F * a;
+            if (fabsf(xn.x - bc.x) >= half.x || fabsf(xn.y - bc.y) >= half.y || fabsf(xn.z - bc.z) >= half.z) walking = false;
+            else x = xn;
+        }
+    }
+    if (lane >= 8) return;
+    const size_t slot = 8 * (size_t)v + me;
+    s.cutNrmFixed[3 * slot] = 0; s.cutNrmFixed[3 * slot + 1] = 0; s.cutNrmFixed[3 * slot + 2] = 0;
+    if (me >= compCount || total == 0) { s.cutFP[slot] = make_float4(0.f, 0.f, 0.f, 0.f); return; }
+    x = mk(fminf(fmaxf(x.x, bc.x - half.x), bc.x + half.x), fminf(fmaxf(x.y, bc.y - half.y), bc.y + half.y),
+           fminf(fmaxf(x.z, bc.z - half.z), bc.z + half.z));
+    if (cnt > 0) {
+        const f3 nAcc = mk((float)nx / kPosScale, (float)ny / kPosScale, (float)nz / kPosScale);
+        const float nLen = len(nAcc);
+        if (nLen > 1e-6f && nLen > 0.25f * (float)cnt) {
+            const f3 nbar = mk(nAcc.x / nLen, nAcc.y / nLen, nAcc.z / nLen);
+            const f3 cutC = mk(acc.x / (float)cnt, acc.y / (float)cnt, acc.z / (float)cnt) + corigin;
+            x = x - nbar * dot(nbar, x - cutC);
+        }
+    }
+    s.cutFP[slot] = make_float4(x.x, x.y, x.z, 1.f);
 }
 
 // Vertex of a skin quad (StitchVertId, V/dc_recon.cu:213-226): a cut, occupied voxel resolves to
@@ -294,78 +322,91 @@ __device__ void stitchEdge(const SurfaceMesh& s, bool cutChain, int e, int ids[6
 // edges whose first marked stencil voxel is v: from each end p of the edge, the component points
 // of p's component in the four voxels around the edge, fanned (through the separated corners when
 // two opposite corners are shared), wound by the rest stencil and flipped for the far end; faces
-// made of shared points only, or of zero area, are dropped.  Writes up to 48 triangles from
-// out[3 * base] on (those at or beyond `cap` are skipped) and returns how many there are.
-__device__ int wallsOfVoxel(const SurfaceMesh& s, int v, int* out, int base, int cap) {
-    const unsigned mask = s.cutMask[v] & 0xFFFu;
-    if (mask == 0u || s.occupied[v] == 0u) return 0;
+// made of shared points only, or of zero area, are dropped.  A voxel's faces come item by item,
+// item j = (edge j / 2, end j % 2), in item order.  wallItem gives item j's faces: it writes them
+// from out[3 * base] on (those at or beyond `cap` are skipped; none when out is null) and returns
+// how many there are (at most 2).
+__device__ int wallItem(const SurfaceMesh& s, int v, unsigned mask, int j, int* out, int base, int cap) {
+    const int le = j >> 1, end = j & 1;
+    if (((mask >> le) & 1u) == 0u) return 0;
     const int vx = v % s.dx, vy = (v / s.dx) % s.dy, vz = v / (s.dx * s.dy);
+    const int ca = kEdgeCorners[le][0], cb = kEdgeCorners[le][1];
+    const int axis = kCorner[ca][0] != kCorner[cb][0] ? 0 : (kCorner[ca][1] != kCorner[cb][1] ? 1 : 2);
+    const int bx = vx + min(kCorner[ca][0], kCorner[cb][0]), by = vy + min(kCorner[ca][1], kCorner[cb][1]),
+              bz = vz + min(kCorner[ca][2], kCorner[cb][2]);
+    bool valid = true, canonical = true, seen = false;
+    for (int st = 0; st < 4; st++) {
+        const int x = bx + kStencil[axis][st][0], y = by + kStencil[axis][st][1], z = bz + kStencil[axis][st][2];
+        if (!voxIn(s, x, y, z)) { valid = false; continue; }
+        if (x == vx && y == vy && z == vz) seen = true;
+        else if (!seen && ((s.cutMask[voxId(s, x, y, z)] >> kStencilEdge[axis][st]) & 1u)) canonical = false;
+    }
+    if (!valid || !canonical) return 0;
+    const int ax = axis == 0, ay = axis == 1, az = axis == 2;
+    const int A = nodeOf(s, bx, by, bz), B = nodeOf(s, bx + ax, by + ay, bz + az);
+    const bool basedHere = end == 0;
+    const int p = basedHere ? A : B, other = basedHere ? B : A;
+    const int px = bx + (basedHere ? 0 : ax), py = by + (basedHere ? 0 : ay), pz = bz + (basedHere ? 0 : az);
+    const int qx = bx + (basedHere ? ax : 0), qy = by + (basedHere ? ay : 0), qz = bz + (basedHere ? az : 0);
+    const int slot = 6 * p + 2 * axis + (basedHere ? 1 : 0);
+    if (!cutHitsMaterial(s.cutT[slot], s.skinT[slot], s.inside[p], s.inside[other])) return 0;
+    int tag[4]; bool ok[4], shared[4]; int n = 0;
+    for (int st = 0; st < 4; st++) {
+        ok[st] = false; shared[st] = false; tag[st] = 0;
+        const int x = bx + kStencil[axis][st][0], y = by + kStencil[axis][st][1], z = bz + kStencil[axis][st][2];
+        const int w = voxId(s, x, y, z);
+        if (s.occupied[w] == 0u) continue;
+        const unsigned m2 = s.cutMask[w] & 0xFFFu;
+        if (m2 == 0u) continue;
+        const int lc = localCorner(px - x, py - y, pz - z);
+        if (lc < 0) continue;
+        const int comp = compOf(s, m2, lc);
+        const int lq = localCorner(qx - x, qy - y, qz - z);
+        shared[st] = lq >= 0 && comp == compOf(s, m2, lq);
+        const int fs = 8 * w + comp;
+        if (s.cutFP[fs].w < .5f) continue;
+        tag[st] = (int)(kCutTag | kWallTag | (unsigned)fs);
+        ok[st] = true;
+        n++;
+    }
+    if (n < 3) return 0;
+    int ord[4], m = 0;
+    for (int st = 0; st < 4; st++) if (ok[st]) ord[m++] = st;
+    if (m == 4 && shared[ord[0]] && shared[ord[2]] && !shared[ord[1]] && !shared[ord[3]]) {
+        const int first = ord[0]; ord[0] = ord[1]; ord[1] = ord[2]; ord[2] = ord[3]; ord[3] = first;
+    }
+    f3 q[4];
+    for (int k = 0; k < m; k++) q[k] = tagPos(s, tag[ord[k]]);
     int count = 0;
-    for (int le = 0; le < 12; le++) {
-        if (((mask >> le) & 1u) == 0u) continue;
-        const int ca = kEdgeCorners[le][0], cb = kEdgeCorners[le][1];
-        const int axis = kCorner[ca][0] != kCorner[cb][0] ? 0 : (kCorner[ca][1] != kCorner[cb][1] ? 1 : 2);
-        const int bx = vx + min(kCorner[ca][0], kCorner[cb][0]), by = vy + min(kCorner[ca][1], kCorner[cb][1]),
-                  bz = vz + min(kCorner[ca][2], kCorner[cb][2]);
-        bool valid = true, canonical = true, seen = false;
-        for (int st = 0; st < 4; st++) {
-            const int x = bx + kStencil[axis][st][0], y = by + kStencil[axis][st][1], z = bz + kStencil[axis][st][2];
-            if (!voxIn(s, x, y, z)) { valid = false; continue; }
-            if (x == vx && y == vy && z == vz) seen = true;
-            else if (!seen && ((s.cutMask[voxId(s, x, y, z)] >> kStencilEdge[axis][st]) & 1u)) canonical = false;
+    for (int k = 1; k < m - 1; k++) {
+        if (shared[ord[0]] && shared[ord[k]] && shared[ord[k + 1]]) continue;
+        const f3 nrm = cross(q[k] - q[0], q[k + 1] - q[0]);
+        if (dot(nrm, nrm) < 1e-16f) continue;
+        const int t = base + count;
+        if (out && t < cap) {
+            out[3 * t] = tag[ord[0]];
+            out[3 * t + 1] = tag[ord[basedHere ? k : k + 1]];
+            out[3 * t + 2] = tag[ord[basedHere ? k + 1 : k]];
         }
-        if (!valid || !canonical) continue;
-        const int ax = axis == 0, ay = axis == 1, az = axis == 2;
-        const int A = nodeOf(s, bx, by, bz), B = nodeOf(s, bx + ax, by + ay, bz + az);
-        for (int end = 0; end < 2; end++) {
-            const bool basedHere = end == 0;
-            const int p = basedHere ? A : B, other = basedHere ? B : A;
-            const int px = bx + (basedHere ? 0 : ax), py = by + (basedHere ? 0 : ay), pz = bz + (basedHere ? 0 : az);
-            const int qx = bx + (basedHere ? ax : 0), qy = by + (basedHere ? ay : 0), qz = bz + (basedHere ? az : 0);
-            const int slot = 6 * p + 2 * axis + (basedHere ? 1 : 0);
-            if (!cutHitsMaterial(s.cutT[slot], s.skinT[slot], s.inside[p], s.inside[other])) continue;
-            int tag[4]; bool ok[4], shared[4]; int n = 0;
-            for (int st = 0; st < 4; st++) {
-                ok[st] = false; shared[st] = false; tag[st] = 0;
-                const int x = bx + kStencil[axis][st][0], y = by + kStencil[axis][st][1], z = bz + kStencil[axis][st][2];
-                const int w = voxId(s, x, y, z);
-                if (s.occupied[w] == 0u) continue;
-                const unsigned m2 = s.cutMask[w] & 0xFFFu;
-                if (m2 == 0u) continue;
-                const int lc = localCorner(px - x, py - y, pz - z);
-                if (lc < 0) continue;
-                const int comp = compOf(s, m2, lc);
-                const int lq = localCorner(qx - x, qy - y, qz - z);
-                shared[st] = lq >= 0 && comp == compOf(s, m2, lq);
-                const int fs = 8 * w + comp;
-                if (s.cutFP[fs].w < .5f) continue;
-                tag[st] = (int)(kCutTag | kWallTag | (unsigned)fs);
-                ok[st] = true;
-                n++;
-            }
-            if (n < 3) continue;
-            int ord[4], m = 0;
-            for (int st = 0; st < 4; st++) if (ok[st]) ord[m++] = st;
-            if (m == 4 && shared[ord[0]] && shared[ord[2]] && !shared[ord[1]] && !shared[ord[3]]) {
-                const int first = ord[0]; ord[0] = ord[1]; ord[1] = ord[2]; ord[2] = ord[3]; ord[3] = first;
-            }
-            f3 q[4];
-            for (int k = 0; k < m; k++) q[k] = tagPos(s, tag[ord[k]]);
-            for (int k = 1; k < m - 1; k++) {
-                if (shared[ord[0]] && shared[ord[k]] && shared[ord[k + 1]]) continue;
-                const f3 nrm = cross(q[k] - q[0], q[k + 1] - q[0]);
-                if (dot(nrm, nrm) < 1e-16f) continue;
-                const int t = base + count;
-                if (out && t < cap) {
-                    out[3 * t] = tag[ord[0]];
-                    out[3 * t + 1] = tag[ord[basedHere ? k : k + 1]];
-                    out[3 * t + 2] = tag[ord[basedHere ? k + 1 : k]];
-                }
-                count++;
-            }
-        }
+        count++;
     }
     return count;
+}
+// A warp on cut voxel v (all lanes call with the same v): lane j < 24 takes item j; returns the
+// voxel's face count (every lane), writing the faces from out[3 * base] on in item order when out
+// is given.
+__device__ int wallsOfVoxelWarp(const SurfaceMesh& s, int v, int lane, int* out, int base, int cap) {
+    const unsigned mask = s.cutMask[v] & 0xFFFu;
+    const int mine = lane < 24 ? wallItem(s, v, mask, lane, nullptr, 0, 0) : 0;
+    int before = mine;   // inclusive scan over lanes
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, before, d);
+        if (lane >= d) before += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, before, 31);
+    if (out && mine > 0) wallItem(s, v, mask, lane, out, base + before - mine, cap);
+    return total;
 }
 
 // Triangle key for the internal-face cancellation (V/surface_cleanup.cuh): the three vertex tags
@@ -449,22 +490,41 @@ __global__ void __launch_bounds__(kSurfaceThreads) surfaceKernel(SurfaceMesh s, 
         featurePoint(s, v);
         s.nrmFixed[3 * v] = 0; s.nrmFixed[3 * v + 1] = 0; s.nrmFixed[3 * v + 2] = 0;
     }
-    if (cutChain)
-        for (int v = r; v < s.nVox; v += R)
-            if ((s.cutMask[v] & 0xFFFu) != 0u && s.occupied[v] != 0u) componentPoints(s, v);
+    // Cut voxels go a warp each, warp w taking the voxels v = w (mod warps), so a blade's
+    // neighbouring cut voxels spread over the GPU.
+    const int lane = (int)(threadIdx.x & 31u), W = R >> 5, wid = r >> 5;
+    auto forCutVoxels = [&](auto&& work) {
+        for (int k0 = 0; wid + k0 * W < s.nVox; k0 += 32) {
+            const int v = wid + (k0 + lane) * W;
+            const bool cut = v < s.nVox && (s.cutMask[v] & 0xFFFu) != 0u && s.occupied[v] != 0u;
+            for (unsigned bits = __ballot_sync(0xffffffffu, cut); bits != 0u; bits &= bits - 1u)
+                work(wid + (k0 + __ffs((int)bits) - 1) * W);
+        }
+    };
+    if (cutChain) {
+        forCutVoxels([&](int v) { componentPointsWarp(s, v, lane); });
+        if (threadIdx.x == 0) s.blockTotal[G + b] = 0;   // wall faces of this CTA's voxel range, summed in 2.
+    }
     if (!g.sync()) return;
     // 2. count: skin quads of this CTA's surface-edge range, cut walls of its voxel range
     const int ce = (s.nEdges + G - 1) / G, e0 = min(s.nEdges, b * ce), e1 = min(s.nEdges, e0 + ce);
     const int cv = cutChain ? (s.nVox + G - 1) / G : 0, v0 = min(s.nVox, b * cv), v1 = cutChain ? min(s.nVox, v0 + cv) : v0;
-    int mine = 0, walls = 0;
+    int mine = 0;
     for (int e = e0 + (int)threadIdx.x; e < e1; e += blockDim.x) {
         int ids[6]; bool ok[2];
         stitchEdge(s, cutChain, e, ids, ok);
         mine += (ok[0] ? 1 : 0) + (ok[1] ? 1 : 0);
     }
-    for (int v = v0 + (int)threadIdx.x; v < v1; v += blockDim.x) walls += wallsOfVoxel(s, v, nullptr, 0, 0);
-    const int ownSkin = blockSum(mine), ownWalls = blockSum(walls);
-    if (threadIdx.x == 0) { s.blockTotal[b] = ownSkin; s.blockTotal[G + b] = ownWalls; }
+    if (cutChain)   // each cut voxel's wall faces, added to the total of the CTA whose range holds it
+        forCutVoxels([&](int v) {
+            const int n = wallsOfVoxelWarp(s, v, lane, nullptr, 0, 0);
+            if (lane == 0) {
+                s.wallCount[v] = n;
+                if (n > 0) atomicAdd(s.blockTotal + G + v / cv, n);
+            }
+        });
+    const int ownSkin = blockSum(mine);
+    if (threadIdx.x == 0) { s.blockTotal[b] = ownSkin; if (!cutChain) s.blockTotal[G + b] = 0; }
     if (!g.sync()) return;
     // write at the prefix: the skin in surface-edge order, then the walls in voxel order
     int skinBefore = 0, skinAll = 0, wallBefore = 0, wallAll = 0;
@@ -497,17 +557,24 @@ __global__ void __launch_bounds__(kSurfaceThreads) surfaceKernel(SurfaceMesh s, 
         }
         running += roundTotal;
     }
-    running = skinAll + wallBefore;
+    running = skinAll + wallBefore;   // the walls' first faces, in voxel order
     for (int base = v0; base < v1; base += blockDim.x) {
         const int v = base + (int)threadIdx.x;
-        const int c = v < v1 ? wallsOfVoxel(s, v, nullptr, 0, 0) : 0;
+        const bool cut = v < v1 && (s.cutMask[v] & 0xFFFu) != 0u && s.occupied[v] != 0u;
+        const int c = cut ? s.wallCount[v] : 0;
         int roundTotal = 0;
         const int t = running + blockExclusive(c, &roundTotal);
-        if (c > 0) wallsOfVoxel(s, v, out, t, s.triCapacity);
+        if (cut) s.wallCount[v] = c > 0 ? t : -1;
         running += roundTotal;
     }
     if (!g.sync()) return;
     if (cancel) {
+        // the walls at their places, a warp per cut voxel that has any
+        forCutVoxels([&](int v) {
+            const int first = s.wallCount[v];
+            if (first >= 0) wallsOfVoxelWarp(s, v, lane, out, first, s.triCapacity);
+        });
+        if (!g.sync()) return;
         // internal faces (V/surface_cleanup.cuh): triangles with the same vertex set cancel in
         // opposite orientation; of a surplus the first in list order stays.  Survivors keep list order.
         int fcap = 1;
