@@ -734,6 +734,30 @@ __global__ void __launch_bounds__(kClusterThreads) frameKernelCluster(DeviceMesh
     cluster.sync();   // no CTA leaves while another may still read its shared memory
 }
 
+// A single mesh on one thread-block cluster of 2^logK CTAs x kSessionClusterThreads: its positions in the
+// cluster's distributed shared memory for the frame (as above), every phase closed by the hardware
+// cluster barrier instead of a grid barrier.  Plain frames only (no blade tick, guard or friction;
+// cu only supplies the topology revision);
+// the closing particle-frame pass follows as its own launch, reading the parity word state[3].
+__global__ void __launch_bounds__(kSessionClusterThreads, 1) frameKernelSessionCluster(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
+                                                                              ContactParams cp, CutParams cu, unsigned* state, int logK) {
+    extern __shared__ float4 clusterSlots[];
+    __shared__ float4* bases[8];
+    cooperative_groups::cluster_group cluster = cooperative_groups::this_cluster();
+    const int K = 1 << logK, rank = (int)cluster.block_rank();
+    if ((int)threadIdx.x < K) bases[threadIdx.x] = cluster.map_shared_rank(clusterSlots, (int)threadIdx.x);
+    __syncthreads();
+    ClusterSync sync{rank * kSessionClusterThreads + (int)threadIdx.x, K * kSessionClusterThreads, rank == 0 && threadIdx.x == 0};
+    DeviceMesh v = m;
+    v.dsm = bases; v.dsmLogB = kSessionClusterLogThreads; v.dsmLogK = logK;
+    for (int n = sync.r; n < v.nNodes; n += sync.n) posRef<true>(v, v.nodeBase + n) = m.pos[v.nodeBase + n];
+    cluster.sync();
+    runFrame<ClusterSync, false, true, true>(v, fc, from, to, cp, cu, state, sync);   // fc.cut is 0: no tick
+    cluster.sync();
+    for (int n = sync.r; n < v.nNodes; n += sync.n) m.pos[v.nodeBase + n] = posRef<true>(v, v.nodeBase + n);
+    cluster.sync();   // no CTA leaves while another may still read its shared memory
+}
+
 __global__ void __launch_bounds__(256) frameKernelInstances256(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it) {
     runInstances(m, fc, cp, it);
 }

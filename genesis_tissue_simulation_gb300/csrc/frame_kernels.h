@@ -34,6 +34,12 @@ __global__ void frameKernelInstances256(DeviceMesh m, FrameCoeffs fc, ContactPar
 constexpr int kClusterThreads = 512, kClusterLogThreads = 9;
 __global__ void frameKernelCluster(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it, int logK);
 __global__ void frameKernelInstances512(DeviceMesh m, FrameCoeffs fc, ContactParams cp, InstanceTable it);
+// A single mesh on one cluster of 2^logK CTAs x kSessionClusterThreads, positions in distributed
+// shared memory (plain frames: no blade tick, guard or friction; particle frames by a following
+// launch).  256 threads a CTA, so the tet projection keeps its registers.
+constexpr int kSessionClusterThreads = 256, kSessionClusterLogThreads = 8;
+__global__ void frameKernelSessionCluster(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to, ContactParams cp,
+                                          CutParams cu, unsigned* state, int logK);
 
 __global__ void particleRotKernel(DeviceMesh m, const unsigned* parityWord, int parity);
 __global__ void tetAlphaKernel(int n, float invH2, const float2* stiff, float2* alpha);

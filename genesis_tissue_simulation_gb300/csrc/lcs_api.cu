@@ -104,12 +104,14 @@ struct Session {
     bool toolSet = false, havePrev = false, pressure = false; CutToolDesc cutTool{};
     float tearLen2 = 0.f;
     // launch choice and profiling
-    int launchMode = 0;                     // 0 automatic, 1 whole-GPU grid, 2 single CTA
-    // automatic mode on a mesh that fits one CTA: the session's 2nd and 3rd frames run one CTA and
-    // the whole GPU, timed; the faster shape is kept (both give the same results bit for bit)
-    int autoMode = 0, autoTrial = 0; float autoMs[2] = {0.f, 0.f}; cudaEvent_t autoEv[2] = {nullptr, nullptr};
+    int launchMode = 0;                     // 0 automatic, 1 whole-GPU grid, 2 single CTA, 3 one cluster
+    // automatic mode on a mesh that fits one CTA or one cluster: after the session's first frame,
+    // one frame in each candidate shape (one CTA, whole GPU, one cluster) is timed and the fastest
+    // kept (all give the same results bit for bit).  autoShape: -1 undecided, else kShape*.
+    int autoShape = -1, autoTrial = 0; float autoMs[3] = {-1.f, -1.f, -1.f}; cudaEvent_t autoEv[2] = {nullptr, nullptr};
     int clockKHz = 2000000;                 // SM clock, for the barrier spin budget
     int maxStageBytes = 0;                  // shared memory one CTA may stage the node state in
+    int maxClusterBytes = 0;                // dynamic shared memory of a session-cluster CTA
     int syncTestExtra = 0; float syncBudgetSeconds = 2.f;
     bool profile = false; std::vector<cudaEvent_t> events; int profiledSteps = 0;
     // section profiler (xpbd_profile_sections, xpbd_solver.cu:30-60): device time per phase kind
@@ -139,7 +141,7 @@ void freePhysics() {
     S.fiberLambda.release(); S.feasTarget.release(); S.needed.release(); S.incOff.release(); S.incTet.release(); S.guardFlags.release();
     S.rotA.release(); S.rotB.release(); S.rotParity = 0;
     S.volumePasses = 0; S.minVolume = 0.f;
-    S.autoMode = 0; S.autoTrial = 0;
+    S.autoShape = -1; S.autoTrial = 0; S.autoMs[0] = S.autoMs[1] = S.autoMs[2] = -1.f;
     S.physReady = false; S.toolArmed = false; S.E = S.B = S.T = 0; S.lastH = -1.f;
 }
 void freeAll() {
@@ -166,6 +168,10 @@ int ensureStream() {
     S.maxStageBytes = optin;
     CK(cudaFuncSetAttribute((const void*)frameKernelBlock, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     CK(cudaFuncSetAttribute((const void*)frameKernelBlockExt, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    cudaFuncAttributes ca{};
+    CK(cudaFuncGetAttributes(&ca, (const void*)frameKernelSessionCluster));
+    S.maxClusterBytes = optin - (int)ca.sharedSizeBytes;   // dynamic bytes left beside its static shared memory
+    CK(cudaFuncSetAttribute((const void*)frameKernelSessionCluster, cudaFuncAttributeMaxDynamicSharedMemorySize, S.maxClusterBytes));
     int khz = 0;
     if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, S.device) == cudaSuccess && khz > 0) S.clockKHz = khz;
     S.gridBlocks = std::max(1, perSm) * S.smCount;
@@ -312,6 +318,14 @@ CutParams cutParams() {
 
 // The frame kernel; when it runs on one CTA, the closing frame pass follows as a whole-GPU launch
 // (*followUp set), so the host flips the parity the kernel leaves in state[3].
+// Launch shapes of a frame: one CTA, the whole GPU, one thread-block cluster.
+constexpr int kShapeBlock = 0, kShapeGrid = 1, kShapeCluster = 2;
+constexpr int kSessionLogK = 3;   // 8 CTAs, the portable cluster size
+size_t clusterBytes() {
+    const size_t perCluster = (size_t)kSessionClusterThreads << kSessionLogK;
+    return (((size_t)S.N + perCluster - 1) / perCluster) * kSessionClusterThreads * sizeof(float4);
+}
+
 int launchFrame(const FrameCoeffs& fc, bool* followUp) {
     *followUp = false;
     DeviceMesh m = deviceMesh();
@@ -319,30 +333,56 @@ int launchFrame(const FrameCoeffs& fc, bool* followUp) {
     unsigned* state = S.state.p;
     CK(cudaMemsetAsync(state + 1, 0, 2 * sizeof(unsigned), S.stream));
     if (S.brickCount.p) CK(cudaMemsetAsync(S.brickCount.p, 0, sizeof(unsigned), S.stream));
-    size_t stageBytes = (size_t)S.N * 2 * sizeof(float4);
-    bool stage = stageBytes <= (size_t)S.maxStageBytes;
-    bool single = S.launchMode == 2 || (S.launchMode == 0 && stage);
-    int timed = -1;   // automatic shape trial timed in this frame: 0 one CTA, 1 whole GPU
-    if (S.launchMode == 0 && stage) {
-        if (S.autoMode != 0) single = S.autoMode == 2;
-        else if (S.autoTrial >= 1) { timed = S.autoTrial - 1; single = timed == 0; }
+    const size_t stageBytes = (size_t)S.N * 2 * sizeof(float4);
+    const bool stage = stageBytes <= (size_t)S.maxStageBytes;
+    const bool clusterFits = clusterBytes() <= (size_t)S.maxClusterBytes;
+    const bool plain = !fc.guarded && !fc.friction && !fc.cut;   // what the cluster shape runs
+    const bool usable[3] = {stage, true, clusterFits && plain};
+    int shape = S.launchMode == 2 ? kShapeBlock : S.launchMode == 3 && usable[kShapeCluster] ? kShapeCluster : kShapeGrid;
+    int timed = -1;   // the automatic trial shape timed in this frame
+    if (S.launchMode == 0) {
+        shape = kShapeGrid;
+        if (stage || clusterFits) {
+            if (S.autoShape >= 0) {
+                shape = S.autoShape;
+                if (!usable[shape]) {   // e.g. a cluster choice on a frame with a blade: the faster usable other
+                    shape = kShapeGrid;
+                    if (usable[kShapeBlock] && S.autoMs[kShapeBlock] >= 0.f && S.autoMs[kShapeBlock] <= S.autoMs[kShapeGrid]) shape = kShapeBlock;
+                }
+            } else if (S.autoTrial >= 1 && S.autoTrial <= 3) {
+                timed = S.autoTrial - 1;   // 0 one CTA, 1 whole GPU, 2 cluster
+                if (usable[timed]) shape = timed;
+                else timed = -1;
+            } else if (S.autoTrial == 0 && stage) {
+                shape = kShapeBlock;
+            }
+        }
     }
     if (timed >= 0) {
         if (!S.autoEv[0]) { CK(cudaEventCreate(&S.autoEv[0])); CK(cudaEventCreate(&S.autoEv[1])); }
         CK(cudaEventRecord(S.autoEv[0], S.stream));
     }
-    if (single) {
+    if (shape == kShapeBlock) {
         FrameCoeffs f = fc;
         f.stageNodes = stage ? 1 : 0;
         f.closingPass = 0;
         const bool ext = fc.guarded || fc.friction;
         (ext ? frameKernelBlockExt : frameKernelBlock)<<<1, kBlockThreads, stage ? stageBytes : 0, S.stream>>>(m, f, S.toolFrom, S.tool, S.cp, cu, state);
         CK(cudaGetLastError());
-        if (fc.rotations) {
-            particleRotKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(m, state + 3, 0);
-            CK(cudaGetLastError());
-            *followUp = true;
-        }
+    } else if (shape == kShapeCluster) {
+        FrameCoeffs f = fc;
+        f.closingPass = 0;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(1u << kSessionLogK); cfg.blockDim = dim3(kSessionClusterThreads); cfg.stream = S.stream;
+        cfg.dynamicSmemBytes = clusterBytes();
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 1u << kSessionLogK; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr; cfg.numAttrs = 1;
+        ToolPose from = S.toolFrom, to = S.tool;
+        ContactParams cp = S.cp;
+        int logK = kSessionLogK;
+        CK(cudaLaunchKernelEx(&cfg, frameKernelSessionCluster, m, f, from, to, cp, cu, state, logK));
     } else {
         ToolPose from = S.toolFrom, to = S.tool;
         ContactParams cp = S.cp;
@@ -353,13 +393,23 @@ int launchFrame(const FrameCoeffs& fc, bool* followUp) {
         CK(cudaLaunchCooperativeKernel(ext ? (const void*)frameKernelGridExt : (const void*)frameKernelGrid, dim3(ext ? S.gridBlocksExt : S.gridBlocks),
                                        dim3(kFrameThreads), args, 0, S.stream));
     }
+    if (shape != kShapeGrid && fc.rotations) {   // the closing particle-frame pass, on the whole GPU
+        particleRotKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(m, state + 3, 0);
+        CK(cudaGetLastError());
+        *followUp = true;
+    }
     if (timed >= 0) CK(cudaEventRecord(S.autoEv[1], S.stream));
-    if (S.launchMode == 0 && stage && S.autoMode == 0) {   // after LCS_Step's synchronise: record the trial
+    if (S.launchMode == 0 && (stage || clusterFits) && S.autoShape < 0) {   // record the trial
         S.autoTrial++;
         if (timed >= 0) {
             CK(cudaEventSynchronize(S.autoEv[1]));
             CK(cudaEventElapsedTime(&S.autoMs[timed], S.autoEv[0], S.autoEv[1]));
-            if (timed == 1) S.autoMode = S.autoMs[0] <= S.autoMs[1] ? 2 : 1;
+        }
+        if (S.autoTrial > 3) {   // every candidate had its frame: keep the fastest measured
+            int best = kShapeGrid;
+            for (int k = 0; k < 3; k++)
+                if (S.autoMs[k] >= 0.f && (S.autoMs[best] < 0.f || S.autoMs[k] < S.autoMs[best])) best = k;
+            S.autoShape = best;
         }
     }
     return 0;
@@ -944,7 +994,7 @@ LCS_API int LCS_ProfileSectionsRead(char* text, int capacity) {
 }
 
 LCS_API int LCS_SetLaunchMode(int mode) {
-    if (mode < 0 || mode > 2) return XPBD_ERR_BAD_ARG;
+    if (mode < 0 || mode > 3) return XPBD_ERR_BAD_ARG;
     S.launchMode = mode;
     return 0;
 }

@@ -128,7 +128,7 @@ LCS_API int LCS_GetTetColors(int* outT);         /* greedy colour of each tet, s
 LCS_API int LCS_GetEdgeColors(int* out6N);       /* colour of each lattice edge at its owner slot, else -1 */
 LCS_API int LCS_GetBendPairs(void* out);         /* the live 32-byte bend records */
 LCS_API int LCS_GetVoxelCutMask(unsigned* outV); /* cumulative 12-bit cut mask per voxel */
-LCS_API int LCS_SetLaunchMode(int mode);         /* 0 automatic, 1 whole-GPU cooperative grid, 2 one CTA */
+LCS_API int LCS_SetLaunchMode(int mode);         /* 0 automatic, 1 whole-GPU cooperative grid, 2 one CTA, 3 one thread-block cluster (plain frames) */
 /* Failure-detection test mode of the grid barrier: every barrier awaits `extraArrivals` arrivals that
  * never come and gives up after `budgetSeconds` (normal budget 2 s); LCS_Step then returns -4002 and
  * the context stays usable.  (0, 2.0) restores normal operation. */

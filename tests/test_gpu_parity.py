@@ -58,7 +58,7 @@ def test_c1_plain_step_matches_oracle(gpu_lib, oracle_libs):
           f"({fp64_err / W.bbox_diagonal(w.grid):.3e} of the diagonal)")
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 def test_launch_modes_agree(gpu_lib, oracle_libs, mode):
     import ctypes
     w = W.make("c1", steps=20)
@@ -119,3 +119,23 @@ def test_bad_dt_and_barrier_timeout_status(gpu_lib):
         session.dll.LCS_SetLaunchMode(0)
         session.dll.LCS_SetBarrierTest(0, ctypes.c_float(2.0))
         session.close()
+
+
+@pytest.mark.parametrize("mode", [3, 0])
+def test_c2_small_cluster_and_automatic_shapes(gpu_lib, oracle_libs, mode):
+    """The 24 x 12 x 20 capsule block on one thread-block cluster (positions in distributed shared
+    memory), and in automatic mode, which times one CTA, the whole GPU and the cluster on its 2nd to
+    4th frames: bit-identical to the oracle either way."""
+    import ctypes
+    w = W.make("c2", steps=12, scale=SMALL)
+    dll = ctypes.CDLL(str(gpu_lib))
+    dll.LCS_SetLaunchMode(mode)
+    try:
+        gpu = trajectory(w, gpu_lib, 12, 4)
+    finally:
+        dll.LCS_SetLaunchMode(0)
+    cpu = trajectory(w, oracle_libs[0], 12, 4)
+    for a, b in zip(gpu, cpu):
+        assert np.array_equal(a["pos"], b["pos"])
+        assert np.array_equal(a["vel"], b["vel"])
+

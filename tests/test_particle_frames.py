@@ -231,7 +231,7 @@ def frames_run(workload, lib, steps, every, launch_mode=None):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 def test_gpu_frames_bit_exact_c1(gpu_lib, oracle_libs, mode):
     w = W.make("c1", steps=30)
     gpu = frames_run(w, gpu_lib, 30, 10, launch_mode=mode)

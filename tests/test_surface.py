@@ -236,7 +236,7 @@ def test_cut_surface_against_reference_build(reference_lib, oracle_libs):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 def test_gpu_surface_bit_exact_skin_cut(gpu_lib, oracle_libs, mode):
     gpu, severed = skin_cut_run(gpu_lib, launch_mode=mode)
     cpu, _ = skin_cut_run(oracle_libs[0])
