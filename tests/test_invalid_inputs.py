@@ -1,0 +1,70 @@
+"""Invalid and empty inputs through the C ABI: every entry point refuses them with the reference's
+status codes (recon -1000/-1001 as V/dc_recon's init, -1 before initialisation, XPBD_ERR_BAD_ARG)
+and nothing is touched; a valid session opened afterwards works.  The oracle answers on the CPU;
+the CUDA library's answers are the GPU test (its initialisation opens a CUDA stream)."""
+import ctypes as ct
+
+import numpy as np
+import pytest
+
+from genesis_tissue_simulation_gb300 import workloads as W
+from genesis_tissue_simulation_gb300.grid import build_grid
+from genesis_tissue_simulation_gb300.native_backend import ReconDesc, XPBD_ERR_BAD_ARG, pointer
+
+
+def _refusals(lib_path):
+    dll = ct.CDLL(str(lib_path))
+    dll.LCS_Step.argtypes = [ct.c_float]
+    g = build_grid(0.5, size=(2.0, 1.0, 1.5))
+    n, v = len(g.positions), len(g.corners)
+    good = dict(voxels=v, corners=n, dims=g.dims)
+
+    def init(voxels, corners, dims, cap=1024, positions=g.positions, corner_ids=g.corners):
+        rd = ReconDesc(voxels, corners, len(g.intersections), len(g.surface_edges), cap, *dims, g.spacing, 8)
+        return dll.LCS_Init(ct.byref(rd), pointer(positions), pointer(corner_ids), pointer(g.offsets),
+                            pointer(g.counts), pointer(g.intersections), pointer(g.surface_edges))
+
+    out = {}
+    out["null desc"] = dll.LCS_Init(None, None, None, None, None, None, None)
+    out["no voxels"] = init(0, n, g.dims)
+    out["no corners"] = init(v, 0, g.dims)
+    out["no triangle capacity"] = init(v, n, g.dims, cap=0)
+    out["dims disagree with corners"] = init(v, n, (g.dims[0] + 1, g.dims[1], g.dims[2]))
+    bad = g.corners.copy()
+    bad.flat[5] = n + 7
+    out["corner id out of range"] = init(v, n, g.dims, corner_ids=bad)
+    out["step before physics"] = dll.LCS_Step(ct.c_float(1 / 60))
+    out["positions into null"] = dll.LCS_GetCornerPos(None)
+    out["launch mode 9"] = dll.LCS_SetLaunchMode(9) if hasattr(dll, "LCS_SetLaunchMode") else XPBD_ERR_BAD_ARG
+    dll.LCS_Shutdown()
+    return out
+
+
+EXPECTED = {"null desc": -1000, "no voxels": -1001, "no corners": -1001, "no triangle capacity": -1001,
+            "dims disagree with corners": -1001, "corner id out of range": -1001, "step before physics": -1,
+            "positions into null": -1, "launch mode 9": XPBD_ERR_BAD_ARG}
+
+
+def _then_a_valid_session_runs(lib_path):
+    w = W.make("c1", steps=2)
+    s = w.open(lib_path)
+    try:
+        w.run(s, steps=2)
+        assert np.isfinite(s.positions()).all()
+    finally:
+        s.close()
+
+
+def test_oracle_refuses_invalid_inputs(oracle_libs):
+    got = _refusals(oracle_libs[0])
+    for k, want in EXPECTED.items():
+        if k != "launch mode 9":           # a launch shape is the CUDA library's own notion
+            assert got[k] == want, (k, got[k])
+    _then_a_valid_session_runs(oracle_libs[0])
+
+
+@pytest.mark.gpu
+def test_cuda_library_refuses_invalid_inputs(gpu_lib):
+    got = _refusals(gpu_lib)
+    assert got == EXPECTED, got
+    _then_a_valid_session_runs(gpu_lib)
