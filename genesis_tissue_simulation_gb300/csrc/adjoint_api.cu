@@ -63,7 +63,7 @@ int blocksFor(const void* kernel, const SessionView& v) {
     return std::max(1, perSm) * v.smCount;
 }
 
-bool useGrid(const SessionView& v) {
+bool useGrid(const SessionView& v) {   // launch modes 0 (automatic) and 3 (cluster, no adjoint form): by size
     if (v.launchMode == 1) return true;
     if (v.launchMode == 2) return false;
     return !(v.T < 16384 && v.N < 32768);
