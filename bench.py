@@ -373,11 +373,11 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, ra
             s.set_tet_stiffness(mu * scale[i], kappa * scale[i])
             s.set_gravity(0.0, -981.0, 0.0)
             s.set_capsule(w.capsule_paths[i][0])
-            for k in range(2):
+            for k in range(4):   # past the automatic launch-shape trials (frames 2-4)
                 s.set_capsule(w.capsule_paths[i][k + 1])
                 s.step()
             s.functions["LCS_ProfileEnable"](1)
-            for k in range(2, 2 + plain_frames):
+            for k in range(4, 4 + plain_frames):
                 s.set_capsule(w.capsule_paths[i][k + 1])
                 s.step()
             ms = np.zeros(3, dtype=np.float32)
@@ -400,7 +400,7 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, ra
         "edges": info["edges"], "substeps": w.substeps, "launch": {"mode": tune["mode"], "threads": tune["threads"],
                                                                     "autotune_ms_per_frame": tune["ms_per_frame"]},
         "plain_instance_steps_per_s": plain_rate, "plain_sample": f"{len(picks)} instances spread over the size order, "
-                                                                  f"{plain_frames} frames each after 2 warm-up frames",
+                                                                  f"{plain_frames} frames each after 4 warm-up frames (past the automatic launch-shape trials)",
         "batched_over_plain": value / plain_rate,
         "e2e": {"value": count * frames / e2e_s, "unit": "instance-steps/s", "h2d_bytes_per_step": 92 * count,
                 "d2h_bytes_per_step": 12 * info["nodes"]},
@@ -654,9 +654,9 @@ def main():
         # the reference's own CUDA build on the same box and plugin call sequence, against ours
         ref = {}
         for key, name, steps in (("c1", "c1", 100), ("c2", args.workload, 30), ("c3", "c3", 30)):
-            r = call_sequence_wall(name, steps, 3)
+            r = call_sequence_wall(name, steps, 4)   # 4 warm-up frames: past our launch-shape trials
             if "wall_steps_per_s" in r:
-                ours = call_sequence_wall(name, steps, 3, lib=lib)
+                ours = call_sequence_wall(name, steps, 4, lib=lib)
                 r["ours_wall_steps_per_s"] = ours["wall_steps_per_s"]
                 r["ours_over_reference"] = ours["wall_steps_per_s"] / r["wall_steps_per_s"]
             ref[key] = r
