@@ -334,18 +334,18 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, ra
         b.set_capsules(w.capsules_at(0))
         tune = b.autotune(trial_steps=2)
         for k in range(warmup):
-            b.step_many([w.capsules_at(k + 1)], use_graph=True)
+            b.step_many(w.capsule_array_at(k + 1)[None], use_graph=True)
         torch.cuda.synchronize()
         b.profile(1)
         for k in range(warmup, warmup + frames):
-            b.step_many([w.capsules_at(k + 1)], use_graph=True)
+            b.step_many(w.capsule_array_at(k + 1)[None], use_graph=True)
         torch.cuda.synchronize()
         device_s = b.profile_read() / 1e3
         b.profile(0)
         positions = np.empty((b.total_nodes, 3), dtype=np.float32)
         e0 = time.perf_counter()
         for k in range(warmup + frames, warmup + 2 * frames):
-            b.step_many([w.capsules_at(k + 1)], use_graph=True)
+            b.step_many(w.capsule_array_at(k + 1)[None], use_graph=True)
             b.positions(out=positions)
         e2e_s = time.perf_counter() - e0
         assert np.isfinite(positions).all(), "non-finite batched state"

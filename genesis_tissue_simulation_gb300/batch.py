@@ -42,6 +42,20 @@ def capsule_tool(c: Capsule) -> Grasper:
     return Grasper(V3(*c.a), V3(*c.b), c.radius, V3(*far), V3(0, 0, 1), V3(*far), V3(1, 0, 0), 0.0, 0.0, 0.0, 0.0)
 
 
+def tool_array(capsules) -> np.ndarray:
+    """The same XpbdToolState records (23 float32, 92 B each) for capsules given as an array
+    [..., 7] = (a xyz, b xyz, radius): one numpy fill instead of one ctypes record per instance."""
+    c = np.asarray(capsules, dtype=np.float32)
+    if c.shape[-1] != 7:
+        raise ValueError("tool_array: capsules must be [..., 7] = (a xyz, b xyz, radius)")
+    out = np.zeros(c.shape[:-1] + (23,), dtype=np.float32)
+    out[..., :7] = c
+    out[..., 8] = out[..., 14] = 1.0e4      # hinge and jaw centre parked at (0, 1e4, 0)
+    out[..., 12] = 1.0                      # jaw axis (0, 0, 1)
+    out[..., 16] = 1.0                      # jaw normal (1, 0, 0)
+    return out
+
+
 class TissueBatch:
     """Many tissue instances advanced together.  ``tet_stiffness[i]`` = (mu*V, kappa*V) per tet in storage
     order, or None for the (E, nu) bake; ``stiffness_scale[i]`` multiplies an instance's stiffnesses."""
@@ -101,8 +115,14 @@ class TissueBatch:
         self.check("GBT_BatchStep", self.dt)
 
     def step_many(self, capsules_per_step=None, steps=None, use_graph=True):
-        """Advance ``steps`` frames (or ``len(capsules_per_step)``), one capsule per instance per frame."""
-        if capsules_per_step is not None:
+        """Advance ``steps`` frames (or ``len(capsules_per_step)``), one capsule per instance per frame:
+        lists of Capsule per frame, or an array [frames, instances, 7] (a xyz, b xyz, radius)."""
+        if isinstance(capsules_per_step, np.ndarray):
+            if capsules_per_step.ndim != 3 or capsules_per_step.shape[1] != len(self.grids):
+                raise ValueError("step_many: capsule array must be [frames, instances, 7]")
+            tools = np.ascontiguousarray(tool_array(capsules_per_step))
+            self.check("GBT_BatchStepMany", self.dt, int(tools.shape[0]), tools.ctypes.data_as(ct.c_void_p), int(use_graph))
+        elif capsules_per_step is not None:
             steps = len(capsules_per_step)
             tools = (Grasper * (steps * len(self.grids)))(*(capsule_tool(c) for frame in capsules_per_step for c in frame))
             self.check("GBT_BatchStepMany", self.dt, steps, ct.byref(tools), int(use_graph))
@@ -165,6 +185,14 @@ class BatchWorkload:
 
     def capsules_at(self, step):
         return [path[min(step, len(path) - 1)] for path in self.capsule_paths]
+
+    def capsule_array_at(self, step):
+        """capsules_at(step) as an array [instances, 7] = (a xyz, b xyz, radius)."""
+        if getattr(self, "_capsule_table", None) is None:
+            longest = max(len(p) for p in self.capsule_paths)
+            self._capsule_table = np.array([[(*p[min(k, len(p) - 1)].a, *p[min(k, len(p) - 1)].b, p[min(k, len(p) - 1)].radius)
+                                             for k in range(longest)] for p in self.capsule_paths], dtype=np.float32)
+        return self._capsule_table[:, min(step, self._capsule_table.shape[1] - 1)]
 
     def subset(self, indices):
         """The instances `indices` (in that order) as a workload of their own."""

@@ -68,3 +68,16 @@ def test_two_ranks_split_and_combine():
     w = BT.make_c4(count=10, steps=2)
     costs = BT.instance_costs(w)
     assert s0 == pytest.approx(1e-6 * max(sum(costs[i] for i in a), sum(costs[i] for i in b)))
+
+
+def test_tool_array_matches_ctypes_records():
+    """The vectorised XpbdToolState fill gives the bytes of the per-capsule ctypes records."""
+    import ctypes as ct
+    from genesis_tissue_simulation_gb300.native_backend import Grasper
+    w = BT.make_c4(count=12, steps=3)
+    for step in (0, 2, 9):
+        caps = w.capsules_at(step)
+        records = (Grasper * len(caps))(*(BT.capsule_tool(c) for c in caps))
+        arr = BT.tool_array(w.capsule_array_at(step))
+        assert arr.shape == (12, 23) and ct.sizeof(Grasper) == 92
+        assert bytes(records) == arr.tobytes()
