@@ -45,7 +45,7 @@ __device__ __forceinline__ float4 f4(f3 v, float w) { return make_float4(v.x, v.
 template <class Sync>
 __device__ bool substepForward(const DeviceMesh& m, const DiffCoeffs& dc, const ContactParams& cp, const DiffBuffers& b, int g, int N,
                                bool record, int j, Sync& sync) {
-    const int r = sync.rank(), R = sync.size();
+    const int r = sync.spreadRank(), R = sync.size();   // spread: a phase smaller than the grid reaches every SM
     const FrameCoeffs fc = frameCoeffs(dc);
     const int nodes = m.nNodes;
     for (int i = r; i < nodes; i += R) {
@@ -108,7 +108,7 @@ __device__ bool substepForward(const DeviceMesh& m, const DiffCoeffs& dc, const 
 
 template <class Sync>
 __device__ void rolloutForward(const DeviceMesh& m, const DiffCoeffs& dc, const ContactParams& cp, const DiffBuffers& b, int N, Sync& sync) {
-    const int r = sync.rank(), R = sync.size();
+    const int r = sync.spreadRank(), R = sync.size();   // spread: a phase smaller than the grid reaches every SM
     // liveness of the current topology, per-tet compliance, origin state with inverse masses
     for (int c = 0; c < m.nEdgeColors; c++)
         for (int e = m.edgeRange[c].x + r; e < m.edgeRange[c].y; e += R) refreshEdge(m, e);
@@ -156,7 +156,7 @@ __device__ void blockSum6(float v[6], float* out) {
 
 template <class Sync>
 __device__ void rolloutBackward(const DeviceMesh& m, const DiffCoeffs& dc, const ContactParams& cp, const DiffBuffers& b, int N, Sync& sync) {
-    const int r = sync.rank(), R = sync.size();
+    const int r = sync.spreadRank(), R = sync.size();   // spread: a phase smaller than the grid reaches every SM
     const int nodes = m.nNodes;
     const int E = m.nEdgeColors > 0 ? m.edgeRange[m.nEdgeColors - 1].y : 0;
     const int T = m.nTetColors > 0 ? m.tetRange[m.nTetColors - 1].y : 0;
@@ -211,15 +211,20 @@ __device__ void rolloutBackward(const DeviceMesh& m, const DiffCoeffs& dc, const
 #pragma unroll
                         for (int n = 0; n < 4; n++) { q[n] = xyz(tq[id[n]]); go[n] = xyz(b.gx[id[n]]); }
                         float2 a = m.tetAlpha[k];
+                        // what the writes below add to, read before the VJP so its latency overlaps
+                        f3 gq0[4];
+#pragma unroll
+                        for (int n = 0; n < 4; n++) gq0[n] = xyz(b.gq[id[n]]);
+                        const int st = b.slotStorage[k];
+                        const float th0 = b.gTheta[st];
                         TetAdjoint adj;
                         tetVJP(m.typeB[meta & 7], P, q, a.x, a.y, dc.dampingOverH, dc.omega, go, b.gB != nullptr, adj);
 #pragma unroll
                         for (int n = 0; n < 4; n++) {
                             b.gx[id[n]] = f4(adj.gp[n], 0.f);
-                            b.gq[id[n]] = f4(xyz(b.gq[id[n]]) + adj.gq[n], 0.f);
+                            b.gq[id[n]] = f4(gq0[n] + adj.gq[n], 0.f);
                         }
-                        int st = b.slotStorage[k];
-                        b.gTheta[st] += adj.gad * a.x + adj.gah * a.y;
+                        b.gTheta[st] = th0 + (adj.gad * a.x + adj.gah * a.y);
                         if (b.gB) {
                             float* gb = b.gB + (size_t)9 * k;
 #pragma unroll
