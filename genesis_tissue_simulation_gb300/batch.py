@@ -104,6 +104,10 @@ class TissueBatch:
         keys = ("instances", "nodes", "edges", "tets", "edge_colours", "tet_colours", "mode", "threads")
         return dict(zip(keys, (int(v) for v in out)))
 
+    def set_grasp_params(self, grasp_params: GraspParams):
+        """Contact parameters of every instance (XpbdGraspParams); a captured CUDA graph is recaptured."""
+        self.f["GBT_BatchSetGraspParams"](ct.byref(grasp_params))
+
     def set_gravity(self, gx, gy, gz):
         self.check("GBT_BatchSetGravity", gx, gy, gz)
 

@@ -501,10 +501,15 @@ LCS_API int GBT_BatchSetGravity(float gx, float gy, float gz) {
     return 0;
 }
 
+// The contact parameters are frame-kernel arguments, so a CUDA graph captured with the previous ones
+// is dropped (the next graph step captures again).
 LCS_API void GBT_BatchSetGraspParams(const GraspParamsAbi* p) {
     if (!p) return;
-    G.cp.jawGapClosed = p->jawGapClosed; G.cp.contactAlpha = p->contactAlpha; G.cp.ccdVelThresh = p->ccdVelThresh;
-    G.cp.ccdMaxDisp = p->ccdMaxDisp; G.cp.ccdOmega = p->ccdOmega;
+    ContactParams c = G.cp;
+    c.jawGapClosed = p->jawGapClosed; c.contactAlpha = p->contactAlpha; c.ccdVelThresh = p->ccdVelThresh;
+    c.ccdMaxDisp = p->ccdMaxDisp; c.ccdOmega = p->ccdOmega;
+    if (std::memcmp(&c, &G.cp, sizeof(c)) != 0) dropGraph();
+    G.cp = c;
 }
 
 LCS_API int GBT_BatchSetTools(const void* tools) {

@@ -836,13 +836,19 @@ __global__ void tetAlphaKernel(int n, float invH2, const float2* stiff, float2* 
     if (k < n) { float2 s = stiff[k]; alpha[k] = make_float2(invH2 / s.x, invH2 / s.y); }
 }
 
-// Body force = acceleration * mass, k_SetGravity (V/physics.cu:317-321).  ext.w holds the mass.
 __global__ void packXyzKernel(int n, const float4* in, float* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 v = in[i];
     out[3 * i] = v.x; out[3 * i + 1] = v.y; out[3 * i + 2] = v.z;
 }
+__global__ void unpackXyzKernel(int n, const float* in, float4* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v = out[i];
+    out[i] = make_float4(in[3 * i], in[3 * i + 1], in[3 * i + 2], v.w);
+}
+// Body force = acceleration * mass, k_SetGravity (V/physics.cu:317-321).  ext.w holds the mass.
 __global__ void gravityKernel(int n, float gx, float gy, float gz, float4* ext) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) { float mass = ext[i].w; ext[i] = make_float4(gx * mass, gy * mass, gz * mass, mass); }

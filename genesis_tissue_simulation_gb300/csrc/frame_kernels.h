@@ -46,6 +46,8 @@ __global__ void tetAlphaKernel(int n, float invH2, const float2* stiff, float2* 
 __global__ void gravityKernel(int n, float gx, float gy, float gz, float4* ext);
 // xyz of n float4 records, packed as 3n floats (the getters' host layout)
 __global__ void packXyzKernel(int n, const float4* in, float* out);
+// 3n packed floats into the xyz of n float4 records, keeping each record's w (inverse mass, mass)
+__global__ void unpackXyzKernel(int n, const float* in, float4* out);
 
 struct QuadTool { f3 t1[3], t2[3], lo, hi, ncut; int valid; };
 __global__ void detectQuadKernel(DeviceMesh m, CutParams cu, QuadTool tool, const float* rot);

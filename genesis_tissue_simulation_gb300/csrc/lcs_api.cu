@@ -117,8 +117,15 @@ struct Session {
     // section profiler (xpbd_profile_sections, xpbd_solver.cu:30-60): device time per phase kind
     bool sections = false; DBuf<unsigned long long> phaseClock; std::vector<unsigned long long> phaseHost;
     double sectionMs[8] = {}; long long sectionCount[8] = {};
+    // changes whenever the liveness flags must be derived again from scratch (a new mesh, a restored
+    // state); LCS_StepNoAlloc keeps its liveness record only for the generation that wrote it
+    unsigned long long generation = 0;
 };
 Session S;
+unsigned long long g_sessionGeneration = 0;
+}  // namespace
+void forgetStepScratch();   // LCS_StepNoAlloc's cached scratch address (below)
+namespace {
 
 int cudaStatus(cudaError_t e) { return e == cudaSuccess ? 0 : -(int)e; }
 #define CK(call) do { cudaError_t _e = (call); if (_e != cudaSuccess) return -(int)_e; } while (0)
@@ -262,7 +269,6 @@ int uploadSurface(const ReconInitDescAbi* d, const int* voxelCorner, const int* 
     return 0;
 }
 
-int nodeIndex(int x, int y, int z) { return x + (S.dx + 1) * (y + (S.dy + 1) * z); }
 int directedSlot(int a, int b) {
     int d = b - a, ad = d < 0 ? -d : d;
     int axis = ad == 1 ? 0 : (ad == S.dx + 1 ? 1 : 2);
@@ -326,48 +332,48 @@ size_t clusterBytes() {
     return (((size_t)S.N + perCluster - 1) / perCluster) * kSessionClusterThreads * sizeof(float4);
 }
 
-int launchFrame(const FrameCoeffs& fc, bool* followUp) {
-    *followUp = false;
-    DeviceMesh m = deviceMesh();
-    CutParams cu = cutParams();
-    unsigned* state = S.state.p;
-    CK(cudaMemsetAsync(state + 1, 0, 2 * sizeof(unsigned), S.stream));
-    if (S.brickCount.p) CK(cudaMemsetAsync(S.brickCount.p, 0, sizeof(unsigned), S.stream));
-    const size_t stageBytes = (size_t)S.N * 2 * sizeof(float4);
-    const bool stage = stageBytes <= (size_t)S.maxStageBytes;
-    const bool clusterFits = clusterBytes() <= (size_t)S.maxClusterBytes;
+// Which shapes can run this frame: one CTA only when the node state can be staged in its shared
+// memory, the cluster only on plain frames whose positions fit its distributed shared memory.
+struct Shapes { bool stage, clusterFits, usable[3]; size_t stageBytes; };
+Shapes usableShapes(const FrameCoeffs& fc) {
+    Shapes u{};
+    u.stageBytes = (size_t)S.N * 2 * sizeof(float4);
+    u.stage = u.stageBytes <= (size_t)S.maxStageBytes;
+    u.clusterFits = clusterBytes() <= (size_t)S.maxClusterBytes;
     const bool plain = !fc.guarded && !fc.friction && !fc.cut;   // what the cluster shape runs
-    const bool usable[3] = {stage, true, clusterFits && plain};
-    int shape = S.launchMode == 2 ? kShapeBlock : S.launchMode == 3 && usable[kShapeCluster] ? kShapeCluster : kShapeGrid;
-    int timed = -1;   // the automatic trial shape timed in this frame
-    if (S.launchMode == 0) {
-        shape = kShapeGrid;
-        if (stage || clusterFits) {
-            if (S.autoShape >= 0) {
-                shape = S.autoShape;
-                if (!usable[shape]) {   // e.g. a cluster choice on a frame with a blade: the faster usable other
-                    shape = kShapeGrid;
-                    if (usable[kShapeBlock] && S.autoMs[kShapeBlock] >= 0.f && S.autoMs[kShapeBlock] <= S.autoMs[kShapeGrid]) shape = kShapeBlock;
-                }
-            } else if (S.autoTrial >= 1 && S.autoTrial <= 3) {
-                timed = S.autoTrial - 1;   // 0 one CTA, 1 whole GPU, 2 cluster
-                if (usable[timed]) shape = timed;
-                else timed = -1;
-            } else if (S.autoTrial == 0 && stage) {
-                shape = kShapeBlock;
-            }
-        }
+    u.usable[kShapeBlock] = u.stage; u.usable[kShapeGrid] = true; u.usable[kShapeCluster] = u.clusterFits && plain;
+    return u;
+}
+// The shape the launch mode asks for; in automatic mode the kept trial winner, else (before the
+// trials have decided) one CTA where the nodes stage, the whole GPU otherwise.
+int requestedShape(const Shapes& u) {
+    if (S.launchMode == 2) return kShapeBlock;
+    if (S.launchMode == 3) return u.usable[kShapeCluster] ? kShapeCluster : kShapeGrid;
+    if (S.launchMode == 1 || !(u.stage || u.clusterFits)) return kShapeGrid;
+    if (S.autoShape >= 0) {
+        if (u.usable[S.autoShape]) return S.autoShape;
+        // e.g. a cluster choice on a frame with a blade: the faster usable other
+        if (u.usable[kShapeBlock] && S.autoMs[kShapeBlock] >= 0.f && S.autoMs[kShapeBlock] <= S.autoMs[kShapeGrid]) return kShapeBlock;
+        return kShapeGrid;
     }
-    if (timed >= 0) {
-        if (!S.autoEv[0]) { CK(cudaEventCreate(&S.autoEv[0])); CK(cudaEventCreate(&S.autoEv[1])); }
-        CK(cudaEventRecord(S.autoEv[0], S.stream));
-    }
+    return u.stage ? kShapeBlock : kShapeGrid;
+}
+
+// One frame in `shape` on the session's stream, with `state` as its state words (the counter and
+// status at [1], [2] must be zero) and m.tetAlpha as its compliances.  When the frame ran on one CTA
+// or one cluster, the closing particle-frame pass follows as a whole-GPU launch (*followUp set), so
+// the host flips the parity the kernel leaves in state[3].
+int launchShape(int shape, const Shapes& u, const FrameCoeffs& fc, const DeviceMesh& m, unsigned* state, bool* followUp) {
+    *followUp = false;
+    CutParams cu = cutParams();
+    ToolPose from = S.toolFrom, to = S.tool;
+    ContactParams cp = S.cp;
+    const bool ext = fc.guarded || fc.friction;
     if (shape == kShapeBlock) {
         FrameCoeffs f = fc;
-        f.stageNodes = stage ? 1 : 0;
+        f.stageNodes = u.stage ? 1 : 0;
         f.closingPass = 0;
-        const bool ext = fc.guarded || fc.friction;
-        (ext ? frameKernelBlockExt : frameKernelBlock)<<<1, kBlockThreads, stage ? stageBytes : 0, S.stream>>>(m, f, S.toolFrom, S.tool, S.cp, cu, state);
+        (ext ? frameKernelBlockExt : frameKernelBlock)<<<1, kBlockThreads, u.stage ? u.stageBytes : 0, S.stream>>>(m, f, from, to, cp, cu, state);
         CK(cudaGetLastError());
     } else if (shape == kShapeCluster) {
         FrameCoeffs f = fc;
@@ -379,17 +385,13 @@ int launchFrame(const FrameCoeffs& fc, bool* followUp) {
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = 1u << kSessionLogK; attr[0].val.clusterDim.y = 1; attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr; cfg.numAttrs = 1;
-        ToolPose from = S.toolFrom, to = S.tool;
-        ContactParams cp = S.cp;
         int logK = kSessionLogK;
         CK(cudaLaunchKernelEx(&cfg, frameKernelSessionCluster, m, f, from, to, cp, cu, state, logK));
     } else {
-        ToolPose from = S.toolFrom, to = S.tool;
-        ContactParams cp = S.cp;
+        DeviceMesh mm = m;
         FrameCoeffs f = fc;
         f.closingPass = 1;
-        void* args[] = {&m, (void*)&f, &from, &to, &cp, &cu, &state};
-        const bool ext = fc.guarded || fc.friction;
+        void* args[] = {&mm, (void*)&f, &from, &to, &cp, &cu, &state};
         CK(cudaLaunchCooperativeKernel(ext ? (const void*)frameKernelGridExt : (const void*)frameKernelGrid, dim3(ext ? S.gridBlocksExt : S.gridBlocks),
                                        dim3(kFrameThreads), args, 0, S.stream));
     }
@@ -398,8 +400,72 @@ int launchFrame(const FrameCoeffs& fc, bool* followUp) {
         CK(cudaGetLastError());
         *followUp = true;
     }
+    return 0;
+}
+
+// Coefficients of one frame of N substeps of length h (xpbd_begin_frame, xpbd_solver.cu:2481-2514,
+// plus the switches of the substep's phases).
+FrameCoeffs frameCoeffs(float h, int N) {
+    FrameCoeffs fc{};
+    fc.numSubsteps = N; fc.substeps = N; fc.firstSubstep = 0;
+    float at = S.ks > 0.f ? 1.f / (S.ks * h * h) : 0.f;
+    fc.velScale = (1.f - S.damping) / (1.f + S.alpha * h);
+    fc.betaGammaHS = at * S.betaS * h;
+    fc.alphaTilde = at;
+    fc.doBend = (S.B > 0 && S.kb > 0.f) ? 1 : 0;
+    fc.alphaB = fc.doBend ? 1.f / (S.kb * h * h) : 0.f;
+    fc.betaGammaHB = fc.alphaB * S.betaB * h;
+    fc.h = h; fc.invH = 1.f / h; fc.invH2 = 1.f / (h * h);
+    fc.doStrain = (S.T > 0 && S.youngE > 0.f) ? 1 : 0;
+    fc.fallback = (fc.doStrain && S.ks <= 0.f) ? 1 : 0;
+    fc.doEdges = (S.ks > 0.f || fc.fallback) ? 1 : 0;
+    fc.fallbackInvEh2 = fc.fallback ? 1.f / (S.youngE * h * h) : 0.f;
+    fc.perpDamp = S.betaS > 0.f ? 1 : 0;
+    fc.betaS = S.betaS;
+    fc.omega = S.omega;
+    fc.dampingOverH = fmaxf(0.f, S.strainDamping) / h;
+    fc.guarded = (S.volumePasses > 0 && S.T > 0) ? 1 : 0;
+    fc.volumePasses = S.volumePasses;
+    fc.tensileStrength = S.tissueHardening;
+    fc.bulkDampingOverH = S.bulkDampingSeconds / h;
+    fc.invScale = 1.f / (1.f + fc.dampingOverH); fc.invBulkScale = 1.f / (1.f + fc.bulkDampingOverH);
+    fc.minVolume = S.minVolume;
+    fc.contact = (S.toolArmed && S.contactModel == 0) ? 1 : 0;
+    fc.friction = (S.toolArmed && S.contactModel == 1) ? 1 : 0;
+    fc.muS = S.muStatic; fc.muD = S.muDynamic; fc.jawThickness = S.jawThickness; fc.contactRadius = S.contactRadius;
+    fc.contactAlphaH2 = S.cp.contactAlpha / (h * h);
+    fc.cut = (S.cutReady && S.toolSet && !S.pressure) ? 1 : 0;
+    fc.spinBudget = (long long)((double)S.syncBudgetSeconds * 1e3 * S.clockKHz);
+    fc.syncTestExtra = S.syncTestExtra;
+    fc.rotations = 1; fc.rotParity = S.rotParity;
+    return fc;
+}
+
+// LCS_Step's frame: the shape of the launch mode, and in automatic mode on a mesh that fits one
+// CTA or one cluster, the session's 2nd to 4th frames each timed in one candidate shape.
+int launchFrame(const FrameCoeffs& fc, bool* followUp) {
+    unsigned* state = S.state.p;
+    CK(cudaMemsetAsync(state + 1, 0, 2 * sizeof(unsigned), S.stream));
+    if (S.brickCount.p) CK(cudaMemsetAsync(S.brickCount.p, 0, sizeof(unsigned), S.stream));
+    const Shapes u = usableShapes(fc);
+    int shape = requestedShape(u);
+    int timed = -1;   // the automatic trial shape timed in this frame
+    const bool trials = S.launchMode == 0 && (u.stage || u.clusterFits) && S.autoShape < 0;
+    if (trials && S.autoTrial >= 1 && S.autoTrial <= 3) {
+        timed = S.autoTrial - 1;   // 0 one CTA, 1 whole GPU, 2 cluster
+        if (u.usable[timed]) shape = timed;
+        else { timed = -1; shape = kShapeGrid; }
+    } else if (trials && S.autoTrial > 3) {
+        shape = kShapeGrid;
+    }
+    if (timed >= 0) {
+        if (!S.autoEv[0]) { CK(cudaEventCreate(&S.autoEv[0])); CK(cudaEventCreate(&S.autoEv[1])); }
+        CK(cudaEventRecord(S.autoEv[0], S.stream));
+    }
+    int rc = launchShape(shape, u, fc, deviceMesh(), state, followUp);
+    if (rc) return rc;
     if (timed >= 0) CK(cudaEventRecord(S.autoEv[1], S.stream));
-    if (S.launchMode == 0 && (stage || clusterFits) && S.autoShape < 0) {   // record the trial
+    if (trials) {   // record the trial
         S.autoTrial++;
         if (timed >= 0) {
             CK(cudaEventSynchronize(S.autoEv[1]));
@@ -423,6 +489,7 @@ int launchFrame(const FrameCoeffs& fc, bool* followUp) {
 LCS_API int LCS_Init(const ReconInitDescAbi* desc, const float* cornerPos, const int* voxelCorner, const int* voxelIsectOffset,
                      const int* voxelIsectCount, const void* isect, const void* surfaceEdges) {
     freeAll();
+    forgetStepScratch();
     if (!desc) return -1000;
     if (desc->voxelCount <= 0 || desc->cornerCount <= 0 || desc->triCapacity <= 0 || !cornerPos) return -1001;
     if ((long long)(desc->dimsX + 1) * (desc->dimsY + 1) * (desc->dimsZ + 1) != desc->cornerCount) return -1001;
@@ -532,6 +599,7 @@ LCS_API int LCS_InitPhysics(const PhysicsInitDesc* desc, const float* mass, cons
     rc = uploadFrameState();
     if (rc) return rc;
     CK(cudaStreamSynchronize(S.stream));
+    S.generation = ++g_sessionGeneration;
     S.physReady = true;
     return 0;
 }
@@ -756,38 +824,7 @@ LCS_API int LCS_Step(float dt) {
     const int N = S.numSubsteps > 0 ? S.numSubsteps : 1;
     float h = dt / (float)N;
     if (!(h > 0.f) || !std::isfinite(h)) return XPBD_ERR_BAD_DT;
-    FrameCoeffs fc{};
-    fc.numSubsteps = N; fc.substeps = N; fc.firstSubstep = 0;
-    float at = S.ks > 0.f ? 1.f / (S.ks * h * h) : 0.f;
-    fc.velScale = (1.f - S.damping) / (1.f + S.alpha * h);
-    fc.betaGammaHS = at * S.betaS * h;
-    fc.alphaTilde = at;
-    fc.doBend = (S.B > 0 && S.kb > 0.f) ? 1 : 0;
-    fc.alphaB = fc.doBend ? 1.f / (S.kb * h * h) : 0.f;
-    fc.betaGammaHB = fc.alphaB * S.betaB * h;
-    fc.h = h; fc.invH = 1.f / h; fc.invH2 = 1.f / (h * h);
-    fc.doStrain = (S.T > 0 && S.youngE > 0.f) ? 1 : 0;
-    fc.fallback = (fc.doStrain && S.ks <= 0.f) ? 1 : 0;
-    fc.doEdges = (S.ks > 0.f || fc.fallback) ? 1 : 0;
-    fc.fallbackInvEh2 = fc.fallback ? 1.f / (S.youngE * h * h) : 0.f;
-    fc.perpDamp = S.betaS > 0.f ? 1 : 0;
-    fc.betaS = S.betaS;
-    fc.omega = S.omega;
-    fc.dampingOverH = fmaxf(0.f, S.strainDamping) / h;
-    fc.guarded = (S.volumePasses > 0 && S.T > 0) ? 1 : 0;
-    fc.volumePasses = S.volumePasses;
-    fc.tensileStrength = S.tissueHardening;
-    fc.bulkDampingOverH = S.bulkDampingSeconds / h;
-    fc.invScale = 1.f / (1.f + fc.dampingOverH); fc.invBulkScale = 1.f / (1.f + fc.bulkDampingOverH);
-    fc.minVolume = S.minVolume;
-    fc.contact = (S.toolArmed && S.contactModel == 0) ? 1 : 0;
-    fc.friction = (S.toolArmed && S.contactModel == 1) ? 1 : 0;
-    fc.muS = S.muStatic; fc.muD = S.muDynamic; fc.jawThickness = S.jawThickness; fc.contactRadius = S.contactRadius;
-    fc.contactAlphaH2 = S.cp.contactAlpha / (h * h);
-    fc.cut = (S.cutReady && S.toolSet && !S.pressure) ? 1 : 0;
-    fc.spinBudget = (long long)((double)S.syncBudgetSeconds * 1e3 * S.clockKHz);
-    fc.syncTestExtra = S.syncTestExtra;
-    fc.rotations = 1; fc.rotParity = S.rotParity;
+    FrameCoeffs fc = frameCoeffs(h, N);
     if (fc.doStrain && h != S.lastH) {
         tetAlphaKernel<<<(S.T + 255) / 256, 256, 0, S.stream>>>(S.T, fc.invH2, S.tetStiff.p, S.tetAlpha.p);
         CK(cudaGetLastError());
@@ -940,6 +977,80 @@ LCS_API int LCS_GetVoxelCutMask(unsigned* out) {
     CK(cudaMemcpyAsync(out, S.cutMask.p, S.cutMask.n * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
     return cudaStatus(cudaStreamSynchronize(S.stream));
 }
+LCS_API int GBT_GetActive(int* outN) {
+    if (!S.physReady || !outN) return -1;
+    CK(cudaMemcpyAsync(outN, S.active.p, (size_t)S.N * sizeof(int), cudaMemcpyDeviceToHost, S.stream));
+    return cudaStatus(cudaStreamSynchronize(S.stream));
+}
+
+// Restore of the state one frame carries into the next (the reference keeps it in recon_corner_pos,
+// physics_vel, physics_nbr_idx, physics_bend_pairs, physics_active, the cut module's voxel mask,
+// edge fractions and topology revision, and physics_particle_rot): a checkpoint taken with the
+// getters, or another solver's state to continue from.  Null arguments keep the current values.
+// Every table is checked before anything is written, so a rejected call (-1004) changes nothing;
+// the liveness flags are derived again at the next frame.
+LCS_API int GBT_SetState(const float* pos3N, const float* vel3N, const int* nbr6N, const void* bendPairs, const int* active,
+                         const unsigned* cutMaskV, const float* edgeCutT6N, const float* rot9N, int setRevision, unsigned revision) {
+    if (!S.physReady) return XPBD_ERR_NOT_READY;
+    if ((cutMaskV || edgeCutT6N || setRevision) && !S.cutReady) return XPBD_ERR_BAD_ARG;
+    const size_t N = (size_t)S.N;
+    for (size_t k = 0; pos3N && k < 3 * N; k++) if (!std::isfinite(pos3N[k])) return XPBD_ERR_BAD_ARG;
+    for (size_t k = 0; vel3N && k < 3 * N; k++) if (!std::isfinite(vel3N[k])) return XPBD_ERR_BAD_ARG;
+    for (size_t k = 0; rot9N && k < 9 * N; k++) if (!std::isfinite(rot9N[k])) return XPBD_ERR_BAD_ARG;
+    for (size_t i = 0; active && i < N; i++) if (active[i] != 0 && active[i] != 1) return XPBD_ERR_BAD_ARG;
+    if (nbr6N) {   // a live slot holds the lattice neighbour in its own direction, or -1
+        const long long stride[3] = {1, S.dx + 1, (long long)(S.dx + 1) * (S.dy + 1)};
+        const int extent[3] = {S.dx, S.dy, S.dz};
+        for (size_t i = 0; i < N; i++) {
+            const int c[3] = {(int)(i % (S.dx + 1)), (int)(i / (S.dx + 1) % (S.dy + 1)), (int)(i / stride[2])};
+            for (int s = 0; s < 6; s++) {
+                const int v = nbr6N[6 * i + s], a = s >> 1, to = c[a] + ((s & 1) ? 1 : -1);
+                if (v != -1 && (to < 0 || to > extent[a] || v != (long long)i + ((s & 1) ? stride[a] : -stride[a]))) return XPBD_ERR_BAD_ARG;
+            }
+        }
+    }
+    if (cutMaskV) for (size_t v = 0; v < S.cutMask.n; v++) if (cutMaskV[v] >> 12) return XPBD_ERR_BAD_ARG;
+    std::vector<BendRecord> bends;
+    if (bendPairs) {   // only the alive flags may differ from the records the session was built with
+        bends.resize(S.bendPairs.n);
+        CK(cudaMemcpyAsync(bends.data(), S.bendPairs.p, bends.size() * sizeof(BendRecord), cudaMemcpyDeviceToHost, S.stream));
+        CK(cudaStreamSynchronize(S.stream));
+        const BendRecord* in = (const BendRecord*)bendPairs;
+        for (size_t q = 0; q < bends.size(); q++) {
+            BendRecord a = bends[q], b = in[q];
+            a.alive = b.alive = 0;
+            if (std::memcmp(&a, &b, sizeof(BendRecord)) != 0 || (in[q].alive != 0 && in[q].alive != 1)) return XPBD_ERR_BAD_ARG;
+            bends[q].alive = in[q].alive;
+        }
+    }
+    const int grid = (S.N + 255) / 256;
+    if (pos3N) {
+        CK(cudaMemcpyAsync(S.packedXyz.p, pos3N, 3 * N * sizeof(float), cudaMemcpyHostToDevice, S.stream));
+        unpackXyzKernel<<<grid, 256, 0, S.stream>>>(S.N, S.packedXyz.p, S.pos.p);
+        CK(cudaGetLastError());
+        unpackXyzKernel<<<grid, 256, 0, S.stream>>>(S.N, S.packedXyz.p, S.prev.p);
+        CK(cudaGetLastError());
+    }
+    if (vel3N) {
+        CK(cudaStreamSynchronize(S.stream));   // packedXyz is free again
+        CK(cudaMemcpyAsync(S.packedXyz.p, vel3N, 3 * N * sizeof(float), cudaMemcpyHostToDevice, S.stream));
+        unpackXyzKernel<<<grid, 256, 0, S.stream>>>(S.N, S.packedXyz.p, S.vel.p);
+        CK(cudaGetLastError());
+    }
+    if (nbr6N) CK(cudaMemcpyAsync(S.nbr.p, nbr6N, 6 * N * sizeof(int), cudaMemcpyHostToDevice, S.stream));
+    if (bendPairs) CK(cudaMemcpyAsync(S.bendPairs.p, bends.data(), bends.size() * sizeof(BendRecord), cudaMemcpyHostToDevice, S.stream));
+    if (active) CK(cudaMemcpyAsync(S.active.p, active, N * sizeof(int), cudaMemcpyHostToDevice, S.stream));
+    if (cutMaskV) CK(cudaMemcpyAsync(S.cutMask.p, cutMaskV, S.cutMask.n * sizeof(unsigned), cudaMemcpyHostToDevice, S.stream));
+    if (edgeCutT6N) CK(cudaMemcpyAsync(S.edgeCutT.p, edgeCutT6N, 6 * N * sizeof(float), cudaMemcpyHostToDevice, S.stream));
+    if (rot9N) CK(cudaMemcpyAsync(S.rotParity ? S.rotB.p : S.rotA.p, rot9N, 9 * N * sizeof(float), cudaMemcpyHostToDevice, S.stream));
+    // pageable sources: each copy has taken its bytes when it returns
+    if (setRevision) CK(cudaMemcpyAsync(S.counters.p, &revision, sizeof(unsigned), cudaMemcpyHostToDevice, S.stream));
+    const unsigned never = ~0u;   // liveness: never derived
+    CK(cudaMemcpyAsync(S.state.p, &never, sizeof(unsigned), cudaMemcpyHostToDevice, S.stream));
+    S.generation = ++g_sessionGeneration;
+    return cudaStatus(cudaStreamSynchronize(S.stream));
+}
+
 LCS_API int LCS_GetCutDebug(unsigned* out18, float* alphaOut) {
     if (!S.cutReady || !out18) return -1;
     std::memset(out18, 0, 18 * sizeof(unsigned));
@@ -1002,22 +1113,29 @@ LCS_API int LCS_SetLaunchMode(int mode) {
 // Allocation-free step.  Some hosts cannot let a plugin allocate device memory while they run:
 // engines and simulators that hand out all GPU memory from their own pool or a fixed budget, and
 // real-time loops where a cudaMalloc/cudaFree (which can synchronise the whole device) would stall
-// a frame.  LCS_StepNoAlloc advances the session exactly as LCS_Step does, but every piece of
-// frame scratch -- the grid barrier's arrival counter and status word, the liveness record, the
-// per-tet compliances of the frame -- lives in the file-scope array below, which the driver
-// reserves when the library is loaded and keeps on every GPU that loads it until the process
-// exits.  Its size caps the mesh: at most kNoAllocMaxTets tets.
+// a frame.  LCS_StepNoAlloc advances the session exactly as LCS_Step does, in the shape LCS_Step
+// would use, but every piece of frame scratch -- the grid barrier's arrival counter and status
+// word, the liveness record, the per-tet compliances of the frame -- lives in the file-scope array
+// below, which the driver reserves when the library is loaded and keeps on every GPU that loads it
+// until the process exits.  Its size caps the mesh: at most kNoAllocMaxTets tets.
 // ---------------------------------------------------------------------------------------------
 namespace {
 constexpr size_t kNoAllocHeaderBytes = 256;                        // state words, 256-byte aligned
 constexpr size_t kNoAllocAlphaBytes = (size_t)4 << 20;             // 4 MiB of per-tet compliances
 constexpr int kNoAllocMaxTets = (int)(kNoAllocAlphaBytes / sizeof(float2));   // 524,288 tets
 static __device__ __align__(256) unsigned char g_stepScratch[kNoAllocHeaderBytes + kNoAllocAlphaBytes];
-// Device address of g_stepScratch per device, resolved on the first call made with that device
-// current (the symbol itself is only a host-side stand-in).
+// Device address of g_stepScratch per device (the symbol itself is only a host-side stand-in),
+// looked up by the first LCS_StepNoAlloc of each session (LCS_Init and LCS_Shutdown forget it, so a
+// reloaded module after a device reset is looked up again), and the session whose liveness record
+// the array holds.
 constexpr int kMaxDevices = 64;
 unsigned char* g_stepScratchAddr[kMaxDevices] = {};
+unsigned long long g_stepScratchOwner[kMaxDevices] = {};
 }  // namespace
+
+void forgetStepScratch() {
+    for (int d = 0; d < kMaxDevices; d++) { g_stepScratchAddr[d] = nullptr; g_stepScratchOwner[d] = 0; }
+}
 
 LCS_API int LCS_StepNoAlloc(float dt) {
     if (!S.physReady) return -1;
@@ -1029,6 +1147,7 @@ LCS_API int LCS_StepNoAlloc(float dt) {
         void* address = nullptr;
         CK(cudaGetSymbolAddress(&address, g_stepScratch));
         g_stepScratchAddr[device] = (unsigned char*)address;
+        g_stepScratchOwner[device] = 0;
     }
     unsigned char* scratch = g_stepScratchAddr[device];
     unsigned* state = (unsigned*)scratch;
@@ -1037,43 +1156,13 @@ LCS_API int LCS_StepNoAlloc(float dt) {
     const int N = S.numSubsteps > 0 ? S.numSubsteps : 1;
     float h = dt / (float)N;
     if (!(h > 0.f) || !std::isfinite(h)) return XPBD_ERR_BAD_DT;
-    FrameCoeffs fc{};
-    fc.numSubsteps = N; fc.substeps = N; fc.firstSubstep = 0;
-    float at = S.ks > 0.f ? 1.f / (S.ks * h * h) : 0.f;
-    fc.velScale = (1.f - S.damping) / (1.f + S.alpha * h);
-    fc.betaGammaHS = at * S.betaS * h;
-    fc.alphaTilde = at;
-    fc.doBend = (S.B > 0 && S.kb > 0.f) ? 1 : 0;
-    fc.alphaB = fc.doBend ? 1.f / (S.kb * h * h) : 0.f;
-    fc.betaGammaHB = fc.alphaB * S.betaB * h;
-    fc.h = h; fc.invH = 1.f / h; fc.invH2 = 1.f / (h * h);
-    fc.doStrain = (S.T > 0 && S.youngE > 0.f) ? 1 : 0;
-    fc.fallback = (fc.doStrain && S.ks <= 0.f) ? 1 : 0;
-    fc.doEdges = (S.ks > 0.f || fc.fallback) ? 1 : 0;
-    fc.fallbackInvEh2 = fc.fallback ? 1.f / (S.youngE * h * h) : 0.f;
-    fc.perpDamp = S.betaS > 0.f ? 1 : 0;
-    fc.betaS = S.betaS;
-    fc.omega = S.omega;
-    fc.dampingOverH = fmaxf(0.f, S.strainDamping) / h;
-    fc.guarded = (S.volumePasses > 0 && S.T > 0) ? 1 : 0;
-    fc.volumePasses = S.volumePasses;
-    fc.tensileStrength = S.tissueHardening;
-    fc.bulkDampingOverH = S.bulkDampingSeconds / h;
-    fc.invScale = 1.f / (1.f + fc.dampingOverH); fc.invBulkScale = 1.f / (1.f + fc.bulkDampingOverH);
-    fc.minVolume = S.minVolume;
-    fc.contact = (S.toolArmed && S.contactModel == 0) ? 1 : 0;
-    fc.friction = (S.toolArmed && S.contactModel == 1) ? 1 : 0;
-    fc.muS = S.muStatic; fc.muD = S.muDynamic; fc.jawThickness = S.jawThickness; fc.contactRadius = S.contactRadius;
-    fc.contactAlphaH2 = S.cp.contactAlpha / (h * h);
-    fc.cut = (S.cutReady && S.toolSet && !S.pressure) ? 1 : 0;
-    fc.spinBudget = (long long)((double)S.syncBudgetSeconds * 1e3 * S.clockKHz);
-    fc.syncTestExtra = S.syncTestExtra;
-    fc.rotations = 1; fc.rotParity = S.rotParity;
+    FrameCoeffs fc = frameCoeffs(h, N);
 
-    // The array keeps whatever the previous call left: the liveness record restarts at "never
-    // derived" (word 0 = ~0u), the barrier counter and status at zero, and the compliances are
-    // written again for this session's tets.
-    CK(cudaMemsetAsync(state, 0xFF, sizeof(unsigned), S.stream));
+    // The array keeps whatever the previous call left.  The liveness record (word 0) is kept when
+    // this session wrote it and restarts at "never derived" otherwise; the barrier counter, status
+    // and frame parity restart at zero; the compliances are written again for this session's tets.
+    if (g_stepScratchOwner[device] != S.generation) CK(cudaMemsetAsync(state, 0xFF, sizeof(unsigned), S.stream));
+    g_stepScratchOwner[device] = S.generation;
     CK(cudaMemsetAsync(state + 1, 0, 3 * sizeof(unsigned), S.stream));
     if (S.brickCount.p) CK(cudaMemsetAsync(S.brickCount.p, 0, sizeof(unsigned), S.stream));
     if (fc.doStrain) {
@@ -1082,32 +1171,53 @@ LCS_API int LCS_StepNoAlloc(float dt) {
     }
     DeviceMesh m = deviceMesh();
     m.tetAlpha = alpha;
-    CutParams cu = cutParams();
-    ToolPose from = S.toolFrom, to = S.tool;
-    ContactParams cp = S.cp;
-    bool single = S.launchMode == 2 || (S.launchMode == 0 && S.T < 65536 && S.N < 32768);
-    if (single) {   // closing frame pass as a whole-GPU launch after the one-CTA frame
-        fc.closingPass = 0;
-        (fc.guarded || fc.friction ? frameKernelBlockExt : frameKernelBlock)<<<1, kFrameThreads, 0, S.stream>>>(m, fc, from, to, cp, cu, state);
-        CK(cudaGetLastError());
-        particleRotKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(m, state + 3, 0);
-        CK(cudaGetLastError());
-    } else {
-        fc.closingPass = 1;
-        void* args[] = {&m, (void*)&fc, &from, &to, &cp, &cu, &state};
-        const bool ext = fc.guarded || fc.friction;
-        CK(cudaLaunchCooperativeKernel(ext ? (const void*)frameKernelGridExt : (const void*)frameKernelGrid, dim3(ext ? S.gridBlocksExt : S.gridBlocks),
-                                       dim3(kFrameThreads), args, 0, S.stream));
-    }
+    const Shapes u = usableShapes(fc);
+    const int shape = requestedShape(u);   // no timed trials here: they would create events
+    bool followUp = false;
+    int rc = launchShape(shape, u, fc, m, state, &followUp);
+    if (rc) return rc;
     unsigned words[2] = {0u, 0u};   // status, current particle-frame buffer
     CK(cudaMemcpyAsync(words, state + 2, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
     CK(cudaStreamSynchronize(S.stream));
     if (fc.cut) S.havePrev = true;
     if (S.toolArmed) S.toolFrom = S.tool;
     if (words[0] != 0u) return LCS_ERR_DEVICE_TIMEOUT;
-    S.rotParity = (int)((words[1] & 1u) ^ (single ? 1u : 0u));
+    S.rotParity = (int)((words[1] & 1u) ^ (followUp ? 1u : 0u));
     return 0;
 }
+
+// ---------------------------------------------------------------------------------------------
+// Entry points of the reference's unified contact/grasp/scissors solver (plugin_api.cpp:30-58,
+// 202-226, 245-261), which this library does not provide.  The reference adapter
+// (endoscopic_tissue/native_backend.py:229-263) binds every one of them and checks the three
+// record sizes, so they are exported: the sizes are the reference's record layouts
+// (XpbdBladeState 52 B, XpbdScissorsState 244 B, XpbdScissorsResult 124 B, xpbd_solver.h:464-477)
+// and every other call returns LCS_ERR_UNSUPPORTED without touching the session.
+// ---------------------------------------------------------------------------------------------
+LCS_API int LCS_PressureBladeAbiVersion() { return 52; }
+LCS_API int LCS_ScissorsAbiVersion() { return 244; }
+LCS_API int LCS_ScissorsResultAbiVersion() { return 124; }
+LCS_API int LCS_SetPressureBlade(const void*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_GetPressureBlade(float*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_SetScissors(const void*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_GetScissors(void*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_GetScissorsLoads(float*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_SetScissorsWrist(float, float, float) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_SetJawGeometry(const float*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_SetKnifeGeometry(int, const float*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_KnifeBodyDepth(float*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_RefineContactSurface(int) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_SurfaceDepth(float*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_SetGraspPatch(float, float, float) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_SetToolDynamics(float, float, float, float) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_SetJawDynamics(float, float, float, float) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_SetInstrumentControl(int) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_GetGraspCoreFlags(int, int*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_GetSolvedTool(float*, float*, int*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_GetSolvedJaw(float*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_GetContactReaction(float*, int*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_GetJawLoad(float*) { return LCS_ERR_UNSUPPORTED; }
+LCS_API int LCS_GetMaterialQuality(float*) { return LCS_ERR_UNSUPPORTED; }
 
 LCS_API int LCS_SetBarrierTest(int extraArrivals, float budgetSeconds) {
     if (extraArrivals < 0 || !(budgetSeconds > 0.f) || budgetSeconds > 10.f) return XPBD_ERR_BAD_ARG;
@@ -1119,6 +1229,7 @@ LCS_API void LCS_Shutdown() {
     if (S.stream) cudaStreamSynchronize(S.stream);
     LCS_ProfileEnable(0);
     freeAll();
+    forgetStepScratch();
 }
 
 // ---------------------------------------------------------------------------------------------

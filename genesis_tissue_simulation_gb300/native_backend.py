@@ -205,7 +205,7 @@ UNIFIED_SIGNATURES = (
     ("LCS_SetJawDynamics", (F, F, F, F), I), ("LCS_SetInstrumentControl", (I,), I),
     ("LCS_GetGraspCoreFlags", (I, P), I), ("LCS_GetSolvedTool", (P, P, P), I), ("LCS_GetSolvedJaw", (P,), I),
     ("LCS_GetPressureBlade", (P,), I), ("LCS_GetContactReaction", (P, P), I), ("LCS_GetJawLoad", (P,), I),
-    ("LCS_GetMaterialQuality", (P,), I),
+    ("LCS_GetMaterialQuality", (P,), I), ("LCS_GetScissorsLoads", (P,), I), ("LCS_SetScissorsWrist", (F, F, F), I),
 )
 
 
@@ -302,8 +302,10 @@ class NativeTissue(_Session):
 
     Its initialisation enables the unified contact/grasp solver (contact model 2, tissue guard,
     grasp patch, tool dynamics, pressure blade).  This library implements the plain XPBD branch
-    only, so constructing a ``NativeTissue`` against it raises ``RuntimeError`` naming the first
-    unified entry point and its status (-4001, or a missing symbol).  Use :class:`PlainTissue`.
+    only; it exports the unified entry points with the reference's record sizes, so the whole
+    signature table binds, and constructing a ``NativeTissue`` against it raises ``RuntimeError``
+    at the first unified call (``LCS_SetGraspPatch failed with native status -4001``).  Use
+    :class:`PlainTissue`.
     """
 
     def __init__(self, grid: TissueGrid, settings=Settings(), dll_path=None, initial_command=Command()):

@@ -105,6 +105,35 @@ LCS_API void LCS_ProfileSections(int enabled);                       /* plugin_a
 LCS_API int LCS_ProfileSectionsRead(char* text, int capacity);       /* plugin_api.cpp:26: "name=ms count=n" lines */
 LCS_API void LCS_Shutdown(void);
 
+/* ---- the reference's unified contact/grasp/scissors solver (plugin_api.cpp:30-58, 202-226,
+ * 245-261): not provided.  Exported so the reference adapter (native_backend.py:229-263) binds
+ * unchanged; the record-size checks answer the reference's layouts, every other call returns
+ * LCS_ERR_UNSUPPORTED (-4001) and leaves the session as it was. ------------------------------------ */
+LCS_API int LCS_PressureBladeAbiVersion(void);     /* = 52, XpbdBladeState (plugin_api.cpp:259) */
+LCS_API int LCS_ScissorsAbiVersion(void);          /* = 244, XpbdScissorsState (plugin_api.cpp:253) */
+LCS_API int LCS_ScissorsResultAbiVersion(void);    /* = 124, XpbdScissorsResult (plugin_api.cpp:254) */
+LCS_API int LCS_SetPressureBlade(const void* bladeState);                              /* plugin_api.cpp:260 */
+LCS_API int LCS_GetPressureBlade(float* values);                                       /* plugin_api.cpp:261 */
+LCS_API int LCS_SetScissors(const void* scissorsState);                                /* plugin_api.cpp:255 */
+LCS_API int LCS_GetScissors(void* scissorsResult);                                     /* plugin_api.cpp:256 */
+LCS_API int LCS_GetScissorsLoads(float* values);                                       /* plugin_api.cpp:257 */
+LCS_API int LCS_SetScissorsWrist(float front, float length, float radius);             /* plugin_api.cpp:258 */
+LCS_API int LCS_SetJawGeometry(const float* bounds);                                   /* plugin_api.cpp:224 */
+LCS_API int LCS_SetKnifeGeometry(int enabled, const float* boxes);                     /* plugin_api.cpp:35 */
+LCS_API int LCS_KnifeBodyDepth(float* depth);                                          /* plugin_api.cpp:36 */
+LCS_API int LCS_RefineContactSurface(int passes);                                      /* plugin_api.cpp:45 */
+LCS_API int LCS_SurfaceDepth(float* depth);                                            /* plugin_api.cpp:32 */
+LCS_API int LCS_SetGraspPatch(float sigma, float compliance, float damping);           /* plugin_api.cpp:216 */
+LCS_API int LCS_SetToolDynamics(float mass, float stiffness, float damping, float maxTravel);   /* plugin_api.cpp:219 */
+LCS_API int LCS_SetJawDynamics(float mass, float stiffness, float damping, float speed);       /* plugin_api.cpp:221 */
+LCS_API int LCS_SetInstrumentControl(int guided);                                      /* plugin_api.cpp:218 */
+LCS_API int LCS_GetGraspCoreFlags(int count, int* flags);                              /* plugin_api.cpp:226 */
+LCS_API int LCS_GetSolvedTool(float* hinge, float* error, int* live);                  /* plugin_api.cpp:220 */
+LCS_API int LCS_GetSolvedJaw(float* gap);                                              /* plugin_api.cpp:222 */
+LCS_API int LCS_GetContactReaction(float* force, int* contacts);                       /* plugin_api.cpp:202 */
+LCS_API int LCS_GetJawLoad(float* load);                                               /* plugin_api.cpp:30 */
+LCS_API int LCS_GetMaterialQuality(float* quality);                                    /* plugin_api.cpp:207 */
+
 /* ---- module diagnostics without an LCS_ export in the reference -------------------------------- */
 LCS_API int LCS_TetCount(void);                  /* xpbd_tet_count (xpbd_solver.h:202) */
 LCS_API int LCS_TetColorCount(void);             /* xpbd_tet_color_count (xpbd_solver.h:203) */
@@ -128,6 +157,17 @@ LCS_API int LCS_GetTetColors(int* outT);         /* greedy colour of each tet, s
 LCS_API int LCS_GetEdgeColors(int* out6N);       /* colour of each lattice edge at its owner slot, else -1 */
 LCS_API int LCS_GetBendPairs(void* out);         /* the live 32-byte bend records */
 LCS_API int LCS_GetVoxelCutMask(unsigned* outV); /* cumulative 12-bit cut mask per voxel */
+LCS_API int GBT_GetActive(int* outN);           /* physics_active (V/physics.h:69): the live active flags */
+/* Restore of the state one LCS_Step hands to the next (no LCS_ export in the reference, which keeps
+ * it behind physics_vel / physics_nbr_idx / physics_bend_pairs / physics_active / physics_particle_rot,
+ * V/physics.h:66-72, recon_corner_pos, V/dc_recon.h:68, and its cut module's mask, fractions and
+ * revision): positions and velocities 3N floats, the neighbour table 6N ints (each slot its lattice
+ * neighbour or -1), the 32-byte bend records (only alive flags may differ from the session's), active
+ * flags N ints (0/1), voxel cut mask V (12 bits), first-cut edge fractions 6N, particle frames 9N,
+ * and the topology revision when setRevision != 0.  Null keeps a table.  A checkpoint is the getters'
+ * output; the replay tests load the reference build's state.  Invalid tables: -1004, nothing written. */
+LCS_API int GBT_SetState(const float* pos3N, const float* vel3N, const int* nbr6N, const void* bendPairs, const int* active,
+                         const unsigned* cutMaskV, const float* edgeCutT6N, const float* rot9N, int setRevision, unsigned revision);
 LCS_API int LCS_SetLaunchMode(int mode);         /* 0 automatic, 1 whole-GPU cooperative grid, 2 one CTA, 3 one thread-block cluster (plain frames) */
 /* Failure-detection test mode of the grid barrier: every barrier awaits `extraArrivals` arrivals that
  * never come and gives up after `budgetSeconds` (normal budget 2 s); LCS_Step then returns -4002 and
@@ -196,17 +236,20 @@ LCS_API int GBT_DiffInfo(int* out4);   /* grid launch (1) or one CTA (0), CTAs, 
 LCS_API void GBT_DiffEnd(void);
 
 /* LCS_StepNoAlloc has no counterpart in the reference.  It advances the session by one frame
- * exactly as LCS_Step does, for hosts that cannot let a plugin allocate GPU memory while they run
- * (engines that own every device allocation through their own pool or budget, and real-time
+ * exactly as LCS_Step does, in the launch shape LCS_Step would pick (automatic mode: the shape its
+ * timed trials kept, or before them one CTA where the nodes fit its shared memory, else the whole
+ * GPU; it runs no trials itself), for hosts that cannot let a plugin allocate GPU memory while they
+ * run (engines that own every device allocation through their own pool or budget, and real-time
  * loops where an allocation, which may synchronise the device, would stall a frame).  It calls no
  * cudaMalloc, cudaFree or other allocating routine: the frame's scratch (barrier counter, status,
  * liveness record, per-tet compliances) is a fixed 4 MiB + 256 B array inside the library, which
  * every GPU that loads the library holds until the process exits.  Limit: meshes of at most
  * 524,288 tets; larger ones return LCS_ERR_SCRATCH_LIMIT (-4003) without stepping.  The first call
- * on a device looks up that array's device address, so make it before any stream capture.  All
- * calls share the one array (each call re-initialises what it needs), so calls that overlap on the
- * GPU, e.g. from two processes' sessions on one device, race.  The inputs and outputs are the
- * session's buffers set up by LCS_Init/LCS_InitPhysics/LCS_InitCut; the status is LCS_Step's. */
+ * after each LCS_Init looks up that array's device address on the current device, so make it before
+ * any stream capture.  All calls in one process share the array; the library is not thread safe,
+ * and two host threads stepping at once would race on it.  Frames stepped here are not recorded by
+ * LCS_ProfileEnable.  The inputs and outputs are the session's buffers set up by
+ * LCS_Init/LCS_InitPhysics/LCS_InitCut; the status is LCS_Step's. */
 LCS_API int LCS_StepNoAlloc(float dt);
 
 #ifdef __cplusplus

@@ -3,20 +3,21 @@
 # oracle/_ref/libLiverCudaSim.so, for sm_103a.  Test infrastructure: the GPU parity tests drive it
 # through the same LCS_* harness as libgbtissue.so to pin the CPU oracle against the reference.
 #
-#   stage:  where /root/reference exists, copy the plugin's native sources (unmodified) into the
-#           git-ignored oracle/_ref/src, so they travel to a GPU machine with the working tree;
+#   stage:  when REFERENCE_ROOT names the reference checkout, copy the plugin's native sources
+#           (unmodified) into the git-ignored oracle/_ref/src, so they travel to a GPU machine with
+#           the working tree (REFERENCE_ROOT=<reference checkout> bash oracle/build_ref.sh stage);
 #   build:  compile oracle/_ref/src with nvcc (-rdc) and g++ directly, no CMake.  The only shims are
 #           a force-included overload for the CUDA 13 cudaGraphAddNode signature (oracle/ref_shim.h)
 #           and __declspec(x) defined away for plugin_api.cpp.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF_TREE="${REFERENCE_ROOT:-/root/reference}/endoscopic_tissue/native/vendor"
+REF_TREE="${REFERENCE_ROOT:+$REFERENCE_ROOT/endoscopic_tissue/native/vendor}"
 OUT="$HERE/_ref"
 SRC="$OUT/src"
 mode="${1:-all}"
 
 if [[ "$mode" == "all" || "$mode" == "stage" ]]; then
-  if [[ -d "$REF_TREE" ]]; then
+  if [[ -n "$REF_TREE" && -d "$REF_TREE" ]]; then
     rm -rf "$SRC"
     mkdir -p "$SRC"
     cp -r "$REF_TREE/cuda" "$REF_TREE/src" "$SRC/"

@@ -6,8 +6,13 @@
 // (endoscopic_tissue/native/vendor/src/plugin_api.cpp) so one Python harness drives the oracle,
 // the CUDA library and (on a GPU machine) the reference build identically.
 //
-// Built twice from this one source:
-//   liboracle_f32.so  ORACLE_REAL=float   FP32, the arithmetic the reference performs
+// Built three times from this one source:
+//   liboracle_f32.so  ORACLE_REAL=float   FP32, the arithmetic the reference performs, in the CUDA
+//                     library's operation order (frame-constant reciprocals, one reciprocal of the 2x2
+//                     pivot, an own J^(-2/3) and log), so the library matches it bit for bit
+//   liboracle_f32w.so ORACLE_REAL=float, ORACLE_AS_WRITTEN: the tet projection exactly as the
+//                     reference writes it (its divisions, the library power and logarithm), the
+//                     independent anchor for every arithmetic rewrite of the CUDA path
 //   liboracle_f64.so  ORACLE_REAL=double  FP64 accuracy oracle (same algorithm, double throughout)
 // Both compile with -ffp-contract=off so results are identical on x86-64 and aarch64 hosts.
 // OpenMP parallelises each colour (members of one colour touch disjoint nodes, so the order
@@ -657,14 +662,23 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
     V3 cof[3] = {cross(F[1], F[2]), cross(F[2], F[0]), cross(F[0], F[1])};
     Real ad = S.aDev[e], ah = S.aHyd[e];
     Real J = dot(F[0], cof[0]), pJ = std::fmax(J, Real(0.05));
+#ifdef ORACLE_AS_WRITTEN
+    // the reference's own operations (xpbd_solver.cu:773, 781): the library power and logarithm
+    Real iso = std::pow(pJ, Real(-2.f / 3.f));
+#else
     Real iso = powMinusTwoThirds(pJ);
+#endif
     Real q = std::fmax(iso * I1 - Real(3), Real(0));
     Real CD = std::sqrt(std::fmax(q, Real(1e-12)));
     Real devScale = Real(1) / CD;
     Real volGrad = J > Real(0.05) ? iso * I1 / (Real(3) * pJ) : Real(0);
     // guarded (tissue guard armed): logarithmic bulk strain with a linear floor below J = 0.05
     const bool guarded = S.volumePasses > 0;
+#ifdef ORACLE_AS_WRITTEN
+    Real CH = guarded ? std::log(pJ) + std::fmin(Real(0), (J - Real(0.05)) / Real(0.05)) : J - Real(1);
+#else
     Real CH = guarded ? logPositive(pJ) + std::fmin(Real(0), (J - Real(0.05)) / Real(0.05)) : J - Real(1);
+#endif
     V3 gd[4], gh[4];
     for (int k = 1; k < 4; k++) {
         V3 b = br[k - 1];
@@ -682,8 +696,19 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
         vd += dot(gd[k], dx); vh += dot(gh[k], dx);
     }
     (void)hh;
-    // the frame constant 1 / (1 + D/h) and one reciprocal of A (the library's form of the solve)
     Real scale = Real(1) + dampingOverH, bulkScale = guarded ? Real(1) + bulkDampingOverH : scale;
+#ifdef ORACLE_AS_WRITTEN
+    // the reference's divisions as written (xpbd_solver.cu:805-816)
+    Real eAd = ad / scale, eAh = ah / bulkScale;
+    Real A = dd + eAd, Bc = dh, gamma = Bc / A;
+    Real schur = eAh + eAd * gamma * gamma;
+    for (int k = 0; k < 4; k++) { V3 r = gh[k] - gd[k] * gamma; schur += w[k] * dot(r, r); }
+    Real rd = (-CD - dampingOverH * vd) / scale;
+    Real rh = (-CH - (bulkScale - Real(1)) * vh) / bulkScale;
+    if (!(A > 0) || !(schur > 0)) return;
+    Real dlH = S.omega * (rh - gamma * rd) / schur, dlD = (S.omega * rd - Bc * dlH) / A;
+#else
+    // the frame constant 1 / (1 + D/h) and one reciprocal of A (the library's form of the solve)
     Real invScale = Real(1) / scale, invBulk = Real(1) / bulkScale;
     Real eAd = ad * invScale, eAh = ah * invBulk;
     Real A = dd + eAd, invA = Real(1) / A, Bc = dh, gamma = Bc * invA;
@@ -693,6 +718,7 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
     Real rh = (-CH - (bulkScale - Real(1)) * vh) * invBulk;
     if (!(A > 0) || !(schur > 0)) return;
     Real dlH = S.omega * (rh - gamma * rd) / schur, dlD = (S.omega * rd - Bc * dlH) * invA;
+#endif
     if (!isFin(dlD) || !isFin(dlH)) return;
     if (guarded) {   // trust region on the update: no corner moves more than 0.15 of the shortest rest edge scale
         Real largest = 0;
@@ -1276,6 +1302,55 @@ API int ORC_GetCornerPos64(double* out) {
 API int ORC_SetCornerPos(const float* in) {     // replay mode: overwrite the live positions (cut topology tests)
     if (!S.reconReady || !in) return -1;
     for (int i = 0; i < S.N; i++) S.pos[i] = v3(in[3 * i], in[3 * i + 1], in[3 * i + 2]);
+    return 0;
+}
+// The library's state restore (same arguments and checks): the replay tests load one state into the
+// oracle, the CUDA library and (read back from it) the reference build's successor.
+API int GBT_SetState(const float* pos3N, const float* vel3N, const int* nbr6N, const void* bendPairs, const int* active,
+                     const unsigned* cutMaskV, const float* edgeCutT6N, const float* rot9N, int setRevision, unsigned revision) {
+    if (!S.physReady) return ERR_NOT_READY;
+    if ((cutMaskV || edgeCutT6N || setRevision) && !S.cutReady) return ERR_BAD_ARG;
+    const size_t N = (size_t)S.N;
+    for (size_t k = 0; pos3N && k < 3 * N; k++) if (!std::isfinite(pos3N[k])) return ERR_BAD_ARG;
+    for (size_t k = 0; vel3N && k < 3 * N; k++) if (!std::isfinite(vel3N[k])) return ERR_BAD_ARG;
+    for (size_t k = 0; rot9N && k < 9 * N; k++) if (!std::isfinite(rot9N[k])) return ERR_BAD_ARG;
+    for (size_t i = 0; active && i < N; i++) if (active[i] != 0 && active[i] != 1) return ERR_BAD_ARG;
+    if (nbr6N) {
+        const long long stride[3] = {1, S.dx + 1, (long long)(S.dx + 1) * (S.dy + 1)};
+        const int extent[3] = {S.dx, S.dy, S.dz};
+        for (size_t i = 0; i < N; i++) {
+            const int c[3] = {(int)(i % (S.dx + 1)), (int)(i / (S.dx + 1) % (S.dy + 1)), (int)(i / stride[2])};
+            for (int s = 0; s < 6; s++) {
+                const int v = nbr6N[6 * i + s], a = s >> 1, to = c[a] + ((s & 1) ? 1 : -1);
+                if (v != -1 && (to < 0 || to > extent[a] || v != (long long)i + ((s & 1) ? stride[a] : -stride[a]))) return ERR_BAD_ARG;
+            }
+        }
+    }
+    if (cutMaskV) for (size_t v = 0; v < S.cutMask.size(); v++) if (cutMaskV[v] >> 12) return ERR_BAD_ARG;
+    if (bendPairs) {
+        const BendPair* in = (const BendPair*)bendPairs;
+        for (size_t q = 0; q < S.bends.size(); q++) {
+            BendPair a = S.bends[q], b = in[q];
+            a.alive = b.alive = 0;
+            if (std::memcmp(&a, &b, sizeof(BendPair)) != 0 || (in[q].alive != 0 && in[q].alive != 1)) return ERR_BAD_ARG;
+        }
+        for (size_t q = 0; q < S.bends.size(); q++) S.bends[q].alive = in[q].alive;
+    }
+    if (pos3N) for (size_t i = 0; i < N; i++) S.pos[i] = S.prev[i] = v3(pos3N[3 * i], pos3N[3 * i + 1], pos3N[3 * i + 2]);
+    if (pos3N && S.cutReady) S.prevCorner = S.pos;
+    if (vel3N) for (size_t i = 0; i < N; i++) S.vel[i] = v3(vel3N[3 * i], vel3N[3 * i + 1], vel3N[3 * i + 2]);
+    if (nbr6N) std::memcpy(S.nbr.data(), nbr6N, 6 * N * sizeof(int));
+    if (active) std::memcpy(S.active.data(), active, N * sizeof(int));
+    if (cutMaskV) std::memcpy(S.cutMask.data(), cutMaskV, S.cutMask.size() * sizeof(unsigned));
+    if (edgeCutT6N) std::memcpy(S.edgeCutT.data(), edgeCutT6N, 6 * N * sizeof(float));
+    if (rot9N) for (size_t k = 0; k < 9 * N; k++) S.particleRot[k] = rot9N[k];
+    if (setRevision) S.revision = revision;
+    S.livenessStale = true; S.livenessRevision = 0xffffffffu;
+    return 0;
+}
+API int GBT_GetActive(int* out) {
+    if (!S.physReady || !out) return -1;
+    std::memcpy(out, S.active.data(), (size_t)S.N * sizeof(int));
     return 0;
 }
 API int LCS_GetVelocities(float* out) {

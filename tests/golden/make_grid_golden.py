@@ -1,6 +1,6 @@
 """Generate the grid golden fixtures from the reference's own producer (endoscopic_tissue/grid.py).
 
-Run where the reference tree is mounted:  python tests/golden/make_grid_golden.py [reference_root]
+Run where the reference tree is mounted:  python tests/golden/make_grid_golden.py <reference_root>
 Writes grid_hashes.json (SHA-256, shape and dtype of every TissueGrid array for several build_grid
 configurations) and grid_small.npz (all arrays of one small lattice).
 """
@@ -13,7 +13,9 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-ROOT = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_grid_golden.py <reference_root>")
+ROOT = Path(sys.argv[1])
 CASES = {
     "c1_16x8x16": dict(spacing=0.2, size=(3.18, 1.58, 3.18), density=1000.0),
     "default_block_0p6": dict(spacing=0.6),

@@ -15,6 +15,15 @@ ROOT = Path(__file__).resolve().parents[1]
 HEADER = ROOT / "include" / "gbtissue.h"
 
 
+# entry points of the reference's unified solver: exported by the CUDA library (defined status), not by the oracle
+UNIFIED = ("LCS_SetPressureBlade", "LCS_SetScissors", "LCS_GetScissors", "LCS_SetJawGeometry", "LCS_SetKnifeGeometry",
+           "LCS_KnifeBodyDepth", "LCS_RefineContactSurface", "LCS_SurfaceDepth", "LCS_SetGraspPatch",
+           "LCS_SetToolDynamics", "LCS_SetJawDynamics", "LCS_SetInstrumentControl", "LCS_GetGraspCoreFlags",
+           "LCS_GetSolvedTool", "LCS_GetSolvedJaw", "LCS_GetPressureBlade", "LCS_GetContactReaction",
+           "LCS_GetJawLoad", "LCS_GetMaterialQuality", "LCS_GetScissorsLoads", "LCS_SetScissorsWrist")
+UNIFIED_SIZES = ("LCS_PressureBladeAbiVersion", "LCS_ScissorsAbiVersion", "LCS_ScissorsResultAbiVersion")
+
+
 def declared_symbols(prefixes=("LCS_",)):
     names = re.findall(r"LCS_API\s+[\w\s\*]+?\b((?:LCS|GBT)_\w+)\s*\(", HEADER.read_text())
     return sorted(n for n in set(names) if n.startswith(prefixes))
@@ -49,7 +58,8 @@ def test_cuda_library_exports_declared_symbols():
 def test_oracle_exports_declared_symbols(oracle_libs):
     for path in oracle_libs:
         dll = ctypes.CDLL(str(path))
-        missing = [n for n in declared_symbols() if n not in ("LCS_SetLaunchMode", "LCS_SetBarrierTest", "LCS_StepNoAlloc") and not hasattr(dll, n)]
+        skip = ("LCS_SetLaunchMode", "LCS_SetBarrierTest", "LCS_StepNoAlloc") + UNIFIED + UNIFIED_SIZES
+        missing = [n for n in declared_symbols() if n not in skip and not hasattr(dll, n)]
         assert not missing, (path.name, missing)
 
 
@@ -58,3 +68,35 @@ def test_oracle_abi_versions(oracle_libs):
     assert dll.LCS_PhysicsAbiVersion() == 52
     assert dll.LCS_GraspToolAbiVersion() == 92
     assert dll.LCS_ContactModelVersion() == 28
+
+
+def _adapter_table():
+    import json
+    data = json.loads((ROOT / "tests" / "golden" / "adapter_signatures.json").read_text())
+    return data["signatures"] + data["scissors_signatures"]
+
+
+def test_reference_adapter_table_binds():
+    """Every entry point the reference adapter binds (native_backend.py:229-263, the scissors pair
+    included; tests/golden/make_adapter_signatures.py) exists in libgbtissue.so with the adapter's
+    argtypes/restype, the record-size checks the adapter makes pass, and every entry point of the
+    unified solver answers LCS_ERR_UNSUPPORTED.  Only host-side calls are made (no session)."""
+    lib = native_build.build()
+    dll = ctypes.CDLL(str(lib))
+    kinds = {"P": ctypes.c_void_p, "I": ctypes.c_int32, "F": ctypes.c_float, None: None}
+    bound = {}
+    for name, args, res in _adapter_table():
+        fn = dll[name]
+        fn.argtypes, fn.restype = tuple(kinds[a] for a in args), kinds[res]
+        bound[name] = (fn, args)
+    for name, structure in (("LCS_PhysicsAbiVersion", PhysicsDesc), ("LCS_GraspToolAbiVersion", Grasper),
+                            ("LCS_PressureBladeAbiVersion", Blade), ("LCS_ScissorsAbiVersion", ScissorsControl),
+                            ("LCS_ScissorsResultAbiVersion", ScissorsResult)):
+        assert bound[name][0]() == ctypes.sizeof(structure), name
+    assert bound["LCS_ContactModelVersion"][0]() == 28
+    buf = (ctypes.c_float * 4096)()
+    dummy = {"P": ctypes.cast(buf, ctypes.c_void_p), "I": 1, "F": 0.5}
+    for name in UNIFIED:
+        fn, args = bound[name]
+        assert fn(*(dummy[a] for a in args)) == -4001, name
+    assert len(bound) == 49

@@ -85,3 +85,77 @@ def test_autotune_keeps_state(gpu_lib, small_batch):
         assert len(choice["ms_per_frame"]) == 6 and all(ms > 0 or ms == -1 for ms in choice["ms_per_frame"])
         assert all(ms > 0 for ms in choice["ms_per_frame"][:3])
         assert np.array_equal(b.positions(), before)
+
+
+def test_graph_follows_grasp_param_changes(gpu_lib, small_batch):
+    """GBT_BatchSetGraspParams between graph replays: the graph is recaptured with the new contact
+    parameters, so the graph path stays bit-identical to plain launches."""
+    stiffer = GraspParams(**dict(GRASP, contact_compliance=1.0e-9, ccd_omega=0.6, ccd_displacement=0.02))
+    runs = []
+    for use_graph in (False, True):
+        with BT.TissueBatch(small_batch.grids, dt=1 / 60, substeps=small_batch.substeps, ks=1e6,
+                            stiffness_scale=small_batch.stiffness_scale(), grasp_params=GraspParams(**GRASP), dll_path=gpu_lib) as b:
+            b.set_launch(0, 256)
+            b.set_gravity(0.0, -981.0, 0.0)
+            b.set_capsules(small_batch.capsules_at(0))
+            frames = []
+            for k in range(STEPS):
+                if k == STEPS // 2:
+                    b.set_grasp_params(stiffer)
+                b.step_many([small_batch.capsules_at(k + 1)], use_graph=use_graph)
+                frames.append(b.positions())
+            runs.append(frames)
+    plain, graph = runs
+    for k in range(STEPS):
+        assert np.array_equal(plain[k], graph[k]), (k, float(np.abs(plain[k] - graph[k]).max()))
+    assert not np.array_equal(plain[-1], _run_without_change(gpu_lib, small_batch)), "the parameter change had no effect"
+
+
+def _run_without_change(lib, workload):
+    with BT.TissueBatch(workload.grids, dt=1 / 60, substeps=workload.substeps, ks=1e6,
+                        stiffness_scale=workload.stiffness_scale(), grasp_params=GraspParams(**GRASP), dll_path=lib) as b:
+        b.set_launch(0, 256)
+        b.set_gravity(0.0, -981.0, 0.0)
+        b.set_capsules(workload.capsules_at(0))
+        for k in range(STEPS):
+            b.step_many([workload.capsules_at(k + 1)], use_graph=True)
+        return b.positions()
+
+
+def test_c4_batch_instances_match_solo_oracle(gpu_lib, oracle_libs):
+    """The C4 table itself (256 uneven instances): the autotuned shape replaying a CUDA graph, and
+    four instances spread over the size range (smallest, two middle, largest) each bit-identical to a
+    solo FP32 oracle session over 5 frames."""
+    steps = 5
+    c4 = BT.make_c4(steps=steps)
+    with BT.TissueBatch(c4.grids, dt=1 / 60, substeps=c4.substeps, ks=1e6, stiffness_scale=c4.stiffness_scale(),
+                        grasp_params=GraspParams(**GRASP), strain_damping_s=0.0, dll_path=gpu_lib) as b:
+        b.set_gravity(0.0, -981.0, 0.0)
+        b.set_capsules(c4.capsules_at(0))
+        choice = b.autotune(trial_steps=2)
+        frames = []
+        for k in range(steps):
+            b.step_many([c4.capsules_at(k + 1)], use_graph=True)
+            frames.append(b.positions())
+        per_instance = {}
+        order = np.argsort([len(g.positions) for g in c4.grids])
+        chosen = [int(order[0]), int(order[len(order) // 3]), int(order[2 * len(order) // 3]), int(order[-1])]
+        for i in chosen:
+            per_instance[i] = [b.instance_positions(f, i).copy() for f in frames]
+    assert choice["mode"] in (0, 1, 2)
+    for i in chosen:
+        g = c4.grids[i]
+        s = PlainTissue(g, dt=1 / 60, substeps=c4.substeps, ks=1e6, strain_damping_s=0.0, grasp_params=GraspParams(**GRASP),
+                        dll_path=oracle_libs[0])
+        try:
+            mu, kappa = s.tet_stiffness()
+            scale = c4.stiffness_scale()[i]
+            s.set_tet_stiffness(mu * scale, kappa * scale)
+            s.set_gravity(0.0, -981.0, 0.0)
+            s.set_capsule(c4.capsule_paths[i][0])
+            for k in range(steps):
+                s.set_capsule(c4.capsule_paths[i][k + 1])
+                s.step()
+                assert np.array_equal(per_instance[i][k], s.positions()), (i, k)
+        finally:
+            s.close()

@@ -56,6 +56,7 @@ def test_c1_plain_step_matches_oracle(gpu_lib, oracle_libs):
     fp64_err = float(np.abs(gpu[-1]["pos"] - f64[-1]["pos"])[active].max())
     print(f"C1 100 steps: |gpu - oracle fp32| = 0, |gpu - oracle fp64| = {fp64_err:.3e} cm "
           f"({fp64_err / W.bbox_diagonal(w.grid):.3e} of the diagonal)")
+    assert fp64_err <= tol, f"C1 100 steps: |gpu - FP64 oracle| = {fp64_err} > {tol}"
 
 
 @pytest.mark.parametrize("mode", [1, 2, 3])
@@ -139,3 +140,27 @@ def test_c2_small_cluster_and_automatic_shapes(gpu_lib, oracle_libs, mode):
         assert np.array_equal(a["pos"], b["pos"])
         assert np.array_equal(a["vel"], b["vel"])
 
+
+
+def test_c2_full_size_matches_oracle(gpu_lib, oracle_libs):
+    """The C2 workload at its own size (64 x 32 x 48 cells, 589,824 tets, 20 substeps): bit-identical
+    positions and velocities to the FP32 oracle after 10 and 20 frames."""
+    w = W.make("c2", steps=20)
+    gpu = trajectory(w, gpu_lib, 20, 10)
+    cpu = trajectory(w, oracle_libs[0], 20, 10)
+    for a, b in zip(gpu, cpu):
+        assert np.array_equal(a["pos"], b["pos"]), float(np.abs(a["pos"] - b["pos"]).max())
+        assert np.array_equal(a["vel"], b["vel"]), float(np.abs(a["vel"] - b["vel"]).max())
+
+
+def test_c3_full_size_topology_bit_exact(gpu_lib, oracle_libs):
+    """The C3 blade workload at its own size over 60 frames: neighbour table, topology revision,
+    voxel cut mask, edge fractions, bend liveness and positions identical to the FP32 oracle."""
+    w = W.make("c3", steps=60)
+    gpu = trajectory(w, gpu_lib, 60, 20, topology=True)
+    cpu = trajectory(w, oracle_libs[0], 60, 20, topology=True)
+    assert cpu[-1]["rev"] > 0, "the blade never crossed the tissue"
+    for a, b in zip(gpu, cpu):
+        assert a["rev"] == b["rev"] == severed_edges(w.grid.neighbors, a["nbr"])
+        for key in ("nbr", "mask", "frac", "bends", "dbg", "pos", "vel"):
+            assert np.array_equal(a[key], b[key]), key

@@ -68,3 +68,18 @@ def test_cuda_library_refuses_invalid_inputs(gpu_lib):
     got = _refusals(gpu_lib)
     assert got == EXPECTED, got
     _then_a_valid_session_runs(gpu_lib)
+
+
+@pytest.mark.gpu
+def test_reference_session_class_stops_at_the_unified_solver(gpu_lib):
+    """The reference's own session class (NativeTissue, unchanged call sequence) binds the whole
+    signature table and stops at its first unified-solver call with the defined status."""
+    from genesis_tissue_simulation_gb300.native_backend import NativeTissue
+    g = build_grid(0.5, size=(2.0, 1.0, 1.5))
+    with pytest.raises(RuntimeError, match="LCS_SetGraspPatch failed with native status -4001"):
+        NativeTissue(g, dll_path=gpu_lib)
+    from genesis_tissue_simulation_gb300.native_backend import PlainTissue
+    with PlainTissue(g, dll_path=gpu_lib) as s:       # the session was released: a new one opens
+        s.set_gravity(0.0, -981.0, 0.0)
+        s.step()
+        assert np.isfinite(s.positions()).all()

@@ -4,8 +4,10 @@ Engines that manage every device allocation through their own pool or budget, an
 where an allocation (which may synchronise the device) would stall a frame, call LCS_StepNoAlloc:
 it uses a fixed scratch array inside the library instead of any allocation.  These tests check,
 through the C ABI, that two calls in a row give the same tissue as two calls of LCS_Step (the
-tolerance of the other parity tests, 1e-4 of the bounding-box diagonal, and in fact bit for bit),
-and that a mesh larger than the array's limit is refused.  This file is collected last.
+tolerance of the other parity tests, 1e-4 of the bounding-box diagonal, and in fact bit for bit:
+positions, velocities, neighbour table, topology revision, particle frames and the rebuilt surface)
+in each launch shape, and that a mesh larger than the array's limit is refused.  This file is
+collected last.
 """
 import ctypes
 
@@ -19,9 +21,10 @@ LCS_ERR_SCRATCH_LIMIT = -4003
 SMALL = (4.78, 2.38, 3.98)
 
 
-def two_steps(workload, lib, entry):
+def two_steps(workload, lib, entry, mode):
     session = workload.open(lib)
     try:
+        session.dll.LCS_SetLaunchMode(mode)
         step = getattr(session.dll, entry)
         step.argtypes, step.restype = (ctypes.c_float,), ctypes.c_int
         frames = []
@@ -30,22 +33,32 @@ def two_steps(workload, lib, entry):
             assert step(session.dt) == 0, entry
             if detect:
                 session.check("LCS_DetectCut")
-            frames.append((session.positions(), session.neighbors(), session.topology_revision()))
+            session.check("LCS_Finalize")
+            surface = session.surface()
+            frames.append(dict(pos=session.positions(), vel=session.velocities(), nbr=session.neighbors(),
+                               rev=session.topology_revision(), rot=session.particle_frames(),
+                               tri=surface["tri"], spos=surface["pos"]))
         return frames
     finally:
+        session.dll.LCS_SetLaunchMode(0)
         session.close()
 
 
+# launch mode 0 picks one CTA for these meshes (their nodes stage in shared memory), 1 the
+# whole-GPU cooperative kernel, whose barrier counter and status words live in the scratch array,
+# 2 one CTA explicitly
+@pytest.mark.parametrize("mode", [0, 1, 2])
 @pytest.mark.parametrize("name,scale", [("c1", None), ("c2", SMALL), ("c3", SMALL)])
-def test_no_alloc_step_matches_step(gpu_lib, name, scale):
+def test_no_alloc_step_matches_step(gpu_lib, name, scale, mode):
     w = W.make(name, steps=2, scale=scale)
     tol = 1e-4 * W.bbox_diagonal(w.grid)
-    ref = two_steps(w, gpu_lib, "LCS_Step")
-    out = two_steps(w, gpu_lib, "LCS_StepNoAlloc")
-    for (pa, na, ra), (pb, nb, rb) in zip(ref, out):
-        assert float(np.abs(pa - pb).max()) <= tol
-        assert np.array_equal(pa, pb)
-        assert np.array_equal(na, nb) and ra == rb
+    ref = two_steps(w, gpu_lib, "LCS_Step", mode)
+    out = two_steps(w, gpu_lib, "LCS_StepNoAlloc", mode)
+    for a, b in zip(ref, out):
+        assert float(np.abs(a["pos"] - b["pos"]).max()) <= tol
+        for key in ("pos", "vel", "nbr", "rot", "tri", "spos"):
+            assert np.array_equal(a[key], b[key]), key
+        assert a["rev"] == b["rev"]
 
 
 def test_no_alloc_step_refuses_meshes_beyond_its_limit(gpu_lib):
