@@ -119,6 +119,15 @@ def dist_setup():
     return world, rank, local
 
 
+def workload_config(args, w, tets, edges, n_active, world):
+    """The bench line's `config`: the workload, the same for both arms."""
+    return {"workload": w.name, "cells": [64, 32, 48] if args.workload == "c2" else None, "tets": tets,
+            "active_nodes": n_active, "lattice_nodes": len(w.grid.positions), "edges": edges,
+            "substeps": int(w.params["substeps"]), "parallelism": f"replicas{world}",
+            "l2": "flushed before every timed step (256 MiB write)",
+            "timing": "CUDA events around each frame launch on the library stream"}
+
+
 def run_reference_arm(args, world, rank):
     """CPU restatement of the reference path on all host threads, same workload and metric."""
     if rank != 0:
@@ -128,7 +137,7 @@ def run_reference_arm(args, world, rank):
     lib = ROOT / "oracle" / "_build" / "liboracle_f32.so"
     w = W.make(args.workload)
     session = w.open(lib)
-    tets = session.tet_count
+    tets, edges = session.tet_count, int(session.functions["LCS_EdgeCount"]())
     try:
         threads = int(session.dll.ORC_Threads())
         for k in range(args.warmup):
@@ -145,11 +154,11 @@ def run_reference_arm(args, world, rank):
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": w.name, "substeps": w.params["substeps"], "tets": tets,
-                       "active_nodes": int((w.grid.active != 0).sum()), "parallelism": "host threads"},
+            "config": workload_config(args, w, tets, edges, int((w.grid.active != 0).sum()), world),
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} full steps of {w.name} after {args.warmup} warm-up steps, "
-                                       f"CPU restatement (FP32, OpenMP within each colour, {threads} threads)"},
+                                       f"CPU restatement (FP32, OpenMP within each colour, {threads} threads), "
+                                       "wall clock per step (the CPU path has no L2 flush or CUDA events)"},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -256,6 +265,8 @@ def workload_measurement(lib, name, steps, warmup, cpu_budget_s=6.0):
            "substeps": substeps, "steps": steps, "timing": "CUDA events around each LCS_Step (rod-phase detection timed on the wall clock only)"}
     if w.blade_path:
         out["topology_revision_after"] = int(revision)
+    if cpu_budget_s <= 0:
+        return out
     # CPU restatement, bounded sample
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
     s = w.open(ROOT / "oracle" / "_build" / "liboracle_f32.so")
@@ -349,6 +360,12 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, ra
             b.positions(out=positions)
         e2e_s = time.perf_counter() - e0
         assert np.isfinite(positions).all(), "non-finite batched state"
+        gathered, gather_s = None, 0.0
+        if world > 1:   # the split's only exchange: rank 0 collects every instance's positions
+            local = [b.instance_positions(positions, j).copy() for j in range(len(w.grids))]
+            g0 = time.perf_counter()
+            gathered = BT.gather_instance_positions(shards, local, rank, world)
+            gather_s = time.perf_counter() - g0
     counts = torch.tensor([info["nodes"], info["edges"], info["tets"]], dtype=torch.float64, device="cuda")
     if world > 1:
         import torch.distributed as dist
@@ -405,6 +422,9 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, ra
         "e2e": {"value": count * frames / e2e_s, "unit": "instance-steps/s", "h2d_bytes_per_step": 92 * count,
                 "d2h_bytes_per_step": 12 * info["nodes"]},
         "l2": "state larger than L2 (no flush)",
+        **({"gather": {"instances": len(gathered), "nodes": int(sum(len(p) for p in gathered)), "seconds": gather_s,
+                       "how": "torch.distributed.gather_object of each rank's instance positions to rank 0, after the timed frames"}}
+           if gathered is not None else {}),
         "roofline": {"bound": "hbm", "achieved": achieved, "unit": "GB/s", "algorithmic_bytes_per_launch": w.substeps * bytes_per_substep,
                      "traffic": ncu_traffic_per_launch("ncu_batch_frame_c4")},
     }
@@ -525,6 +545,31 @@ def finalize_measurement(lib, calls=50, warmup=3):
     return out
 
 
+def frames_measurement(lib, calls=50, warmup=3):
+    """One particle-frame pass (physics_compute_rotations: k_ComputeParticleRot over every node) on
+    the C2 lattice after 3 sagging frames, through GBT_ComputeParticleFrames (launch + stream
+    synchronise); wall clock per call, median."""
+    from genesis_tissue_simulation_gb300 import workloads as W
+
+    w = W.make("c2", steps=3)
+    s = w.open(lib)
+    try:
+        w.run(s, steps=3)
+        fn = s.dll.GBT_ComputeParticleFrames
+        times = []
+        for k in range(calls + warmup):
+            t0 = time.perf_counter()
+            assert fn() == 0
+            if k >= warmup:
+                times.append(time.perf_counter() - t0)
+    finally:
+        s.close()
+    nodes = len(w.grid.positions)
+    ms = 1e3 * float(np.median(times))
+    return {"workload": f"c2 lattice, {nodes:,} nodes, after 3 frames", "ms_per_pass_wall": ms,
+            "nodes_per_s": nodes / (ms / 1e3), "timing": f"wall clock around GBT_ComputeParticleFrames, median of {calls}"}
+
+
 def main():
     parser = argparse.ArgumentParser()
     parser.add_argument("--gpus", type=int, default=1)
@@ -536,7 +581,7 @@ def main():
     parser.add_argument("--no-batched", action="store_true")
     parser.add_argument("--no-adjoint", action="store_true")
     parser.add_argument("--no-workloads", action="store_true", help="skip the C1 and C3 lines")
-    parser.add_argument("--only", default="all", choices=("all", "batched", "adjoint", "finalize"),
+    parser.add_argument("--only", default="all", choices=("all", "batched", "adjoint", "finalize", "frames", "c1", "c3"),
                         help="run one section alone and print its JSON object (for profiling)")
     parser.add_argument("--batched-frames", type=int, default=20)
     args = parser.parse_args()
@@ -562,6 +607,8 @@ def main():
     if args.only != "all":   # one section alone (profiling runs): its JSON object, no bench line
         section = (batched_measurement(lib, args.batched_frames, max(args.warmup, 3)) if args.only == "batched"
                    else finalize_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1)) if args.only == "finalize"
+                   else frames_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1)) if args.only == "frames"
+                   else workload_measurement(lib, args.only, max(args.steps, 1), args.warmup, cpu_budget_s=0.0) if args.only in ("c1", "c3")
                    else adjoint_measurement(lib, reps=max(args.steps, 1)))
         print(json.dumps({"only": args.only, **section}), flush=True)
         return
@@ -636,10 +683,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * device_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": w.name, "cells": [64, 32, 48] if args.workload == "c2" else None, "tets": tets,
-                   "active_nodes": n_active, "lattice_nodes": len(w.grid.positions), "edges": edges, "substeps": substeps,
-                   "parallelism": f"replicas{world}", "l2": "flushed before every timed step (256 MiB write)",
-                   "timing": "CUDA events around each frame launch on the library stream"},
+        "config": workload_config(args, w, tets, edges, n_active, world),
         "proj_per_s": value * projections, "projections_per_step": projections,
         "wall_steps_per_s": world * args.steps / wall,
         "e2e": {"value": world * args.steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 92 + 4,

@@ -221,6 +221,28 @@ def shard_instances(costs, world):
     return [sorted(s) for s in shards]
 
 
+def gather_instance_positions(shards, local, rank, world, dst=0):
+    """The only exchange of a sharded batch: rank `dst` receives every rank's instance positions.
+    `shards` is shard_instances' split, `local` this rank's positions of its own instances (list, in
+    its shard's order).  Returns the positions of all instances in instance order on `dst`, None on
+    the other ranks.  Uses torch.distributed (gloo or NCCL; with NCCL the current CUDA device must
+    be set)."""
+    import torch.distributed as dist
+    if world == 1:
+        return list(local)
+    if len(local) != len(shards[rank]):
+        raise ValueError("gather_instance_positions: one array per instance of this rank's shard")
+    parts = [None] * world if rank == dst else None
+    dist.gather_object([np.ascontiguousarray(p) for p in local], parts, dst=dst)
+    if rank != dst:
+        return None
+    out = [None] * sum(len(s) for s in shards)
+    for r, shard in enumerate(shards):
+        for j, i in enumerate(shard):
+            out[i] = parts[r][j]
+    return out
+
+
 def instance_costs(workload):
     """Per-instance cost for sharding: lattice edges plus tets, from the grids alone."""
     costs = []

@@ -883,6 +883,16 @@ LCS_API int LCS_Finalize() {
     S.rotParity = p ^ 1;
     return buildSurface();
 }
+// physics_compute_rotations (V/physics.cu:399-411) alone: one particle-frame pass from the current
+// lattice, without the surface rebuild LCS_Finalize adds.
+LCS_API int GBT_ComputeParticleFrames() {
+    if (!S.physReady) return -1;
+    const int p = S.rotParity;
+    particleRotKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(deviceMesh(), nullptr, p);
+    CK(cudaGetLastError());
+    S.rotParity = p ^ 1;
+    return cudaStatus(cudaStreamSynchronize(S.stream));
+}
 // Surface readback (plugin_api.cpp:84-100): a non-indexed triangle soup, 3 vertices per triangle.
 LCS_API int LCS_GetSurfaceCounts(int* vertexCount, int* indexCount) {
     if (!S.surfaceReady) return -1;

@@ -184,6 +184,28 @@ __device__ __forceinline__ float powMinusTwoThirds(float J) {
     return y * y;
 }
 
+// arccos c for the bending angle (c in [-1, 1]), by the half-angle reduction of the arcsine:
+// |c| <= 1/2: acos c = pi/2 - asin c; c > 1/2: acos c = 2 asin s; c < -1/2: acos c = pi - 2 asin s,
+// with s = sqrt((1 - |c|)/2) <= 1/2 (1 - |c| and the halving are exact there).  asin x = x + x z P(z),
+// z = x^2 <= 1/4, P of degree 5 fitted by weighted least squares to (asin x - x)/(x z) on Chebyshev
+// nodes of [0, 1/4] (oracle/fit_acos.py); pi/2 and pi as an FP32 head plus tail.  <= 1.1 ulp from the
+// exact arccos; the CPU restatement evaluates the same sequence.
+__device__ __forceinline__ float acosBend(float c) {
+    const float a = fabsf(c);
+    const bool mid = a <= 0.5f;
+    const float z = mid ? c * c : (1.f - a) * 0.5f;
+    const float x = mid ? c : sqrtf(z);
+    float p = 0.03748363f;
+    p = p * z + 0.014460857f;
+    p = p * z + 0.03180234f;
+    p = p * z + 0.044517495f;
+    p = p * z + 0.075005025f;
+    p = p * z + 0.1666666f;
+    const float asinx = x + x * (z * p);
+    if (mid) return 1.57079637f - (asinx - -4.37113883e-8f);
+    return c > 0.f ? 2.f * asinx : 3.14159274f - (2.f * asinx - -8.74227766e-8f);
+}
+
 // log x for the guarded bulk strain (x >= 0.05, a positive normal float): x = m 2^e with m in
 // (sqrt(1/2), sqrt(2)], log m = 2 atanh(s), s = (m - 1)/(m + 1), by its odd series to s^11 (the
 // truncation is below 3e-9 relative), e ln 2 with ln 2 split into an exactly representable head
@@ -281,7 +303,7 @@ __device__ __forceinline__ void projectBend(const DeviceMesh& m, int e, const Fr
     float c = fmaxf(-1.f, fminf(1.f, dot(nu, nv)));
     float s = sqrtf(fmaxf(1.f - c * c, 0.f));
     if (s < 1e-4f) return;
-    float C = acosf(c) - __int_as_float(r.w);
+    float C = acosBend(c) - __int_as_float(r.w);
     f3 gj = nv - nu * c, gk = nu - nv * c, gi = (gj + gk) * -1.f;
     float wg = wi * dot(gi, gi) + wj * dot(gj, gj) + wk * dot(gk, gk);
     float g = fc.betaGammaHB;

@@ -146,6 +146,7 @@ LCS_API int LCS_GetVelocities(float* out3N);     /* xpbd_get_velocities (xpbd_so
  * pointer of GBT_ParticleRotDevice stays valid until the next LCS_Step / LCS_Finalize (the frames
  * alternate between two buffers). */
 LCS_API int GBT_GetParticleRot(float* out9N);
+LCS_API int GBT_ComputeParticleFrames(void);   /* physics_compute_rotations (V/physics.cu:399-411): one frame pass, no surface */
 LCS_API void* GBT_ParticleRotDevice(void);
 
 /* ---- extensions (no counterpart in the reference ABI) ------------------------------------------ */

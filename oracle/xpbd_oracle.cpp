@@ -115,6 +115,28 @@ static inline float powMinusTwoThirds(float J) {
 }
 static inline double powMinusTwoThirds(double J) { return std::pow(J, -2.0 / 3.0); }
 
+// arccos c for the bending angle (c in [-1, 1]).  FP32: the half-angle reduction of the arcsine
+// (|c| <= 1/2: pi/2 - asin c; c > 1/2: 2 asin s; c < -1/2: pi - 2 asin s; s = sqrt((1 - |c|)/2)),
+// asin x = x + x z P(z), z = x^2, P of degree 5 fitted by least squares (fit_acos.py), pi/2 and pi
+// as head plus tail; <= 1.1 ulp; the CUDA kernels evaluate the same sequence.  FP64: the library
+// arccos.
+static inline float acosBend(float c) {
+    const float a = std::fabs(c);
+    const bool mid = a <= 0.5f;
+    const float z = mid ? c * c : (1.f - a) * 0.5f;
+    const float x = mid ? c : std::sqrt(z);
+    float p = 0.03748363f;
+    p = p * z + 0.014460857f;
+    p = p * z + 0.03180234f;
+    p = p * z + 0.044517495f;
+    p = p * z + 0.075005025f;
+    p = p * z + 0.1666666f;
+    const float asinx = x + x * (z * p);
+    if (mid) return 1.57079637f - (asinx - -4.37113883e-8f);
+    return c > 0.f ? 2.f * asinx : 3.14159274f - (2.f * asinx - -8.74227766e-8f);
+}
+static inline double acosBend(double c) { return std::acos(c); }
+
 // log x for the guarded bulk strain (x >= 0.05, a positive normal float).  FP32: x = m 2^e with
 // m in (sqrt(1/2), sqrt(2)], log m = 2 atanh(s), s = (m - 1)/(m + 1), by its odd series to s^11,
 // e ln 2 with ln 2 split into an exact head and a tail; the CUDA kernels evaluate the same sequence.
@@ -636,7 +658,11 @@ static void projectBend(int e) {
     Real c = std::fmax(Real(-1), std::fmin(Real(1), dot(nu, nv)));
     Real s = std::sqrt(std::fmax(Real(1) - c * c, Real(0)));
     if (s < Real(1e-4)) return;
-    Real C = std::acos(c) - S.bTheta[e];
+#ifdef ORACLE_AS_WRITTEN
+    Real C = std::acos(c) - S.bTheta[e];   // acosf (xpbd_solver.cu:553)
+#else
+    Real C = acosBend(c) - S.bTheta[e];
+#endif
     V3 gj = nv - nu * c, gk = nu - nv * c, gi = (gj + gk) * Real(-1);
     Real wg = wi * dot(gi, gi) + wj * dot(gj, gj) + wk * dot(gk, gk);
     Real g = S.betaGammaHB;
@@ -1407,10 +1433,17 @@ API int LCS_ProfileRead(int steps, float* ms) {
 API void LCS_Shutdown() { resetCut(); resetPhysics(); S.reconReady = false; }
 API double ORC_LogPositive(double x) { return (double)logPositive((Real)x); }   // the guarded bulk strain's log
 API double ORC_PowMinusTwoThirds(double x) { return (double)powMinusTwoThirds((Real)x); }
+API double ORC_AcosBend(double x) { return (double)acosBend((Real)x); }
 API int ORC_GuardStats(long long* out3) {   // feasibility chain activity since the guard was armed
     if (!out3) return ERR_BAD_ARG;
     for (int k = 0; k < 3; k++) out3[k] = S.guardStats[k];
     return 0;
+}
+API int ORC_SetThreads(int n) {   // host threads of the colour sweeps (several oracle processes on one host)
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#endif
+    return n > 0 ? 0 : ERR_BAD_ARG;
 }
 API int ORC_Threads() {
 #ifdef _OPENMP

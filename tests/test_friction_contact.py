@@ -28,8 +28,17 @@ def grasper(top, k, steps, closing):
                    V3(0.0, 1.0, 0.0), 0.35, 1.2, gap, 0.0)
 
 
-def friction_run(lib, steps=10, closing=False, launch_mode=None, enabled=1, reference=False):
+def surfaceless_grid():
+    """The C1 lattice with no surface edges: the reconstructed surface has no triangles, so the
+    reference's contact model 1 takes its node-contact branch (k_FindToolContacts +
+    k_SolveFrictionContacts, xpbd_solver.cu:3655-3665), the branch this library implements; with a
+    surface it contacts the triangle soup instead (the unified solver's surface contact)."""
     g = build_grid(0.2, size=(3.18, 1.58, 3.18), density=1000.0)
+    return g.__class__(**{**vars(g), "surface_edges": np.zeros((0, 8), dtype=np.int32)})
+
+
+def friction_run(lib, steps=10, closing=False, launch_mode=None, enabled=1, reference=False):
+    g = surfaceless_grid()
     s = PlainTissue(g, dt=1 / 60, substeps=10, ks=1e6, young_pa=6000.0, strain_damping_s=0.0, grasp_params=GraspParams(**GRASP),
                     dll_path=lib, reference=reference)
     try:

@@ -60,6 +60,28 @@ def test_pow_minus_two_thirds_accuracy(oracle_libs):
     assert err.max() <= 2.5, (float(err.max()), float(xs[err.argmax()]))
 
 
+def test_acos_bend_accuracy(oracle_libs):
+    """The FP32 arccos of the bending angle (own routine, identical on host and device; coefficients
+    derived by oracle/fit_acos.py) against float64 arccos: within 1.1 ulp on [-1, 1], and equal bit for
+    bit to the same operation sequence evaluated in numpy float32."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("fit_acos", str(oracle_libs[0].parents[1] / "fit_acos.py"))
+    fit = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(fit)
+    dll = ctypes.CDLL(str(oracle_libs[0]))
+    dll.ORC_AcosBend.argtypes, dll.ORC_AcosBend.restype = (ctypes.c_double,), ctypes.c_double
+    rng = np.random.default_rng(1)
+    xs = np.float32(np.concatenate([np.linspace(-1, 1, 6001), rng.uniform(-1, 1, 4000), 1 - rng.uniform(0, 1e-4, 500),
+                                    0.5 + rng.uniform(-1e-4, 1e-4, 500), [-1.0, -0.5, 0.0, 0.5, 1.0]]))
+    got = np.array([dll.ORC_AcosBend(float(x)) for x in xs], dtype=np.float32)
+    ref = np.arccos(xs.astype(np.float64))
+    err = np.abs(got.astype(np.float64) - ref) / np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+    assert float(err.max()) <= 1.1, (float(err.max()), float(xs[err.argmax()]))
+    coef = np.float32([0.1666666, 0.075005025, 0.044517495, 0.03180234, 0.014460857, 0.03748363])
+    assert np.array_equal(fit.acos_bend(xs, coef), got)
+    assert np.array_equal(fit.fit(), coef), "the routine's coefficients are the fit's"
+
+
 def test_log_positive_accuracy(oracle_libs):
     """The FP32 logarithm of the guarded bulk strain (own routine, identical on host and device)
     against numpy's: within 2 ulp on [0.05, 1e4]."""

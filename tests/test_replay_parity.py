@@ -98,8 +98,8 @@ def _guard_scenario(minimum):
 
 
 def _friction_scenario(closing):
-    from test_friction_contact import GRASP, grasper
-    grid = build_grid(0.2, size=C1, density=1000.0)
+    from test_friction_contact import GRASP, grasper, surfaceless_grid
+    grid = surfaceless_grid()     # the reference's node-contact branch of contact model 1
     top = float(grid.positions[grid.active != 0, 1].max())
     steps = 10
 

@@ -1,6 +1,7 @@
 """Instances shard over GPUs with no exchange (the C4 split): every instance on exactly one rank,
-loads balanced by cost, and the ranks' timings combine into one rate (slowest rank).  The
-multi-rank path runs as two `gloo` processes on the CPU."""
+loads balanced by cost, each rank steps only its own instances, rank 0 gathers the positions (the
+only data exchange), and the ranks' timings combine into one rate (slowest rank).  The multi-rank
+path runs as two `gloo` processes on the CPU, each stepping its instances through the FP32 oracle."""
 import os
 import socket
 
@@ -38,34 +39,71 @@ def test_subset_keeps_instances():
     assert sub.capsules_at(1) == [w.capsule_paths[4][1], w.capsule_paths[1][1]]
 
 
-def _rank(rank, world, port, out):
+def _solo_frames(w, i, lib, steps, threads=None):
+    """Instance i of a batch workload stepped alone through the FP32 oracle (the CPU stand-in for one
+    GPU's share: each instance evolves exactly as it does alone, which the GPU batch tests assert)."""
+    from genesis_tissue_simulation_gb300.native_backend import GraspParams, PlainTissue
+    from genesis_tissue_simulation_gb300 import workloads as W
+    s = PlainTissue(w.grids[i], dt=1 / 60, substeps=w.substeps, ks=1e6, strain_damping_s=w.strain_damping_s,
+                    grasp_params=GraspParams(**dict(W.DEFAULT_GRASP, ccd_velocity=0.0)), dll_path=lib)
+    try:
+        if threads:
+            assert s.dll.ORC_SetThreads(threads) == 0
+        mu, kappa = s.tet_stiffness()
+        scale = w.stiffness_scale()[i]
+        s.set_tet_stiffness(mu * scale, kappa * scale)
+        s.set_gravity(0.0, -981.0, 0.0)
+        s.set_capsule(w.capsule_paths[i][0])
+        for k in range(steps):
+            s.set_capsule(w.capsule_paths[i][k + 1])
+            s.step()
+        return s.positions()
+    finally:
+        s.close()
+
+
+SHARD_STEPS = 3
+
+
+def _shard_workload():
+    return BT.make_c4(count=8, seed=5, steps=SHARD_STEPS, size_range=((3, 6), (2, 4), (3, 6)))
+
+
+def _rank(rank, world, port, lib, out):
     os.environ["MASTER_ADDR"], os.environ["MASTER_PORT"] = "127.0.0.1", str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        w = BT.make_c4(count=10, steps=2)
+        w = _shard_workload()
         shards = BT.shard_instances(BT.instance_costs(w), world)
-        mine = w.subset(shards[rank])
-        # each rank "times" its share (seconds proportional to its cost); the slowest counts
-        seconds = torch.tensor([1e-6 * sum(BT.instance_costs(mine))], dtype=torch.float64)
-        count = torch.tensor([len(mine.grids)], dtype=torch.float64)
+        # each rank steps its own instances only, with no exchange during the frames
+        mine = [_solo_frames(w, i, lib, SHARD_STEPS, threads=1) for i in shards[rank]]
+        gathered = BT.gather_instance_positions(shards, mine, rank, world)
+        seconds = torch.tensor([1e-6 * sum(BT.instance_costs(w.subset(shards[rank])))], dtype=torch.float64)
+        count = torch.tensor([len(shards[rank])], dtype=torch.float64)
         dist.all_reduce(seconds, op=dist.ReduceOp.MAX)
         dist.all_reduce(count)
-        out[rank] = (float(seconds), float(count), shards[rank])
+        out[rank] = (float(seconds), float(count), shards[rank], None if gathered is None else [g.tolist() for g in gathered])
     finally:
         dist.destroy_process_group()
 
 
-def test_two_ranks_split_and_combine():
+def test_two_ranks_step_shards_and_gather(oracle_libs):
+    """Two gloo ranks each step their cost-balanced shard of a batch; rank 0 gathers every
+    instance's positions, which equal an unsharded run bit for bit."""
     with socket.socket() as sk:
         sk.bind(("127.0.0.1", 0))
         port = sk.getsockname()[1]
     manager = mp.get_context("spawn").Manager()
     out = manager.dict()
-    mp.start_processes(_rank, args=(2, port, out), nprocs=2, join=True, start_method="spawn")
-    (s0, c0, a), (s1, c1, b) = out[0], out[1]
-    assert s0 == s1 and c0 == c1 == 10
-    assert sorted(a + b) == list(range(10)) and not set(a) & set(b)
-    w = BT.make_c4(count=10, steps=2)
+    mp.start_processes(_rank, args=(2, port, str(oracle_libs[0]), out), nprocs=2, join=True, start_method="spawn")
+    (s0, c0, a, gathered), (s1, c1, b, none) = out[0], out[1]
+    w = _shard_workload()
+    assert s0 == s1 and c0 == c1 == len(w.grids)
+    assert sorted(a + b) == list(range(len(w.grids))) and not set(a) & set(b) and a and b
+    assert none is None and len(gathered) == len(w.grids)
+    for i in range(len(w.grids)):
+        alone = _solo_frames(w, i, oracle_libs[0], SHARD_STEPS)
+        assert np.array_equal(np.asarray(gathered[i], dtype=np.float32), alone), i
     costs = BT.instance_costs(w)
     assert s0 == pytest.approx(1e-6 * max(sum(costs[i] for i in a), sum(costs[i] for i in b)))
 
