@@ -228,7 +228,7 @@ def call_sequence_wall(name, steps, warmup, lib=None):
     return out
 
 
-def workload_measurement(lib, name, steps, warmup, cpu_budget_s=6.0):
+def workload_measurement(lib, name, steps, warmup, cpu_budget_s=6.0, launch_mode=0):
     """Steps/s of another plain-path workload through the C ABI: device time from the library's
     events around each frame (CUDA events), plus its CPU restatement on all host cores over a
     bounded sample.  C1: 16x8x16 cells, 10 substeps, no tool.  C3: the C2 block with the blade swept
@@ -242,6 +242,8 @@ def workload_measurement(lib, name, steps, warmup, cpu_budget_s=6.0):
     w = W.make(name, steps=warmup + steps + 1)
     s = w.open(lib)
     try:
+        if launch_mode:   # a fixed launch shape (profiling), else the automatic choice
+            assert s.dll.LCS_SetLaunchMode(launch_mode) == 0
         tets, edges = s.tet_count, int(s.functions["LCS_EdgeCount"]())
         for k in range(warmup):
             s.step(detect_cut=w.command(s, k))
@@ -257,6 +259,8 @@ def workload_measurement(lib, name, steps, warmup, cpu_budget_s=6.0):
         s.functions["LCS_ProfileEnable"](0)
         revision = s.topology_revision() if w.blade_path else 0
     finally:
+        if launch_mode:
+            s.dll.LCS_SetLaunchMode(0)
         s.close()
     device_s = float(ms[0]) / 1e3
     substeps = int(w.params["substeps"])
@@ -584,6 +588,8 @@ def main():
     parser.add_argument("--only", default="all", choices=("all", "batched", "adjoint", "finalize", "frames", "c1", "c3"),
                         help="run one section alone and print its JSON object (for profiling)")
     parser.add_argument("--batched-frames", type=int, default=20)
+    parser.add_argument("--launch-mode", type=int, default=0, choices=(0, 1, 2, 3),
+                        help="--only c1/c3: 1 whole GPU, 2 one CTA, 3 one cluster (default: automatic)")
     args = parser.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -608,7 +614,8 @@ def main():
         section = (batched_measurement(lib, args.batched_frames, max(args.warmup, 3)) if args.only == "batched"
                    else finalize_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1)) if args.only == "finalize"
                    else frames_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1)) if args.only == "frames"
-                   else workload_measurement(lib, args.only, max(args.steps, 1), args.warmup, cpu_budget_s=0.0) if args.only in ("c1", "c3")
+                   else workload_measurement(lib, args.only, max(args.steps, 1), args.warmup, cpu_budget_s=0.0,
+                                             launch_mode=args.launch_mode) if args.only in ("c1", "c3")
                    else adjoint_measurement(lib, reps=max(args.steps, 1)))
         print(json.dumps({"only": args.only, **section}), flush=True)
         return
