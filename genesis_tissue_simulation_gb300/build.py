@@ -22,6 +22,9 @@ CSRC = PACKAGE_DIR / "csrc"
 BUILD = CSRC / "_build"
 INCLUDE = PACKAGE_DIR.parent / "include"
 LIBRARY = BUILD / "libgbtissue.so"
+# the same sources with every element gather index checked (GBT_DEBUG_BOUNDS): tests only
+DEBUG_BUILD = CSRC / "_build_debug"
+DEBUG_LIBRARY = DEBUG_BUILD / "libgbtissue_debug.so"
 SOURCES = ("frame_kernels.cu", "lcs_api.cu", "mesh_build.cu", "batch_api.cu", "adjoint_kernels.cu", "adjoint_api.cu",
            "surface_kernels.cu")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
@@ -39,39 +42,41 @@ def common_flags():
             "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden"]
 
 
-def _compile(source: str) -> Path:
-    obj = BUILD / (Path(source).stem + ".o")
-    cmd = [nvcc_path(), *common_flags(), "-c", str(CSRC / source), "-o", str(obj)]
+def _compile(source: str, debug: bool = False) -> Path:
+    obj = (DEBUG_BUILD if debug else BUILD) / (Path(source).stem + ".o")
+    cmd = [nvcc_path(), *common_flags(), *(["-DGBT_DEBUG_BOUNDS"] if debug else []), "-c", str(CSRC / source), "-o", str(obj)]
     result = subprocess.run(cmd, capture_output=True, text=True)
     if result.returncode != 0:
         raise RuntimeError(f"nvcc failed for {source}:\n{result.stderr}")
     return obj
 
 
-def _stale() -> bool:
-    if not LIBRARY.exists():
+def _stale(library: Path = LIBRARY) -> bool:
+    if not library.exists():
         return True
-    built = LIBRARY.stat().st_mtime
+    built = library.stat().st_mtime
     inputs = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
     return any(p.stat().st_mtime > built for p in inputs)
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile libgbtissue.so unless it is newer than every source; returns its path."""
-    if not force and not _stale():
-        return LIBRARY
-    BUILD.mkdir(parents=True, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, debug: bool = False) -> Path:
+    """Compile libgbtissue.so (debug: libgbtissue_debug.so, gather indices checked) unless it is newer
+    than every source; returns its path."""
+    library, folder = (DEBUG_LIBRARY, DEBUG_BUILD) if debug else (LIBRARY, BUILD)
+    if not force and not _stale(library):
+        return library
+    folder.mkdir(parents=True, exist_ok=True)
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as pool:
-        objects = list(pool.map(_compile, SOURCES))
-    tmp = LIBRARY.with_suffix(".so.tmp")
+        objects = list(pool.map(lambda src: _compile(src, debug), SOURCES))
+    tmp = library.with_suffix(".so.tmp")
     cmd = [nvcc_path(), ARCH, "-shared", "-o", str(tmp), *map(str, objects)]
     result = subprocess.run(cmd, capture_output=True, text=True)
     if result.returncode != 0:
         raise RuntimeError(f"link failed:\n{result.stderr}")
-    os.replace(tmp, LIBRARY)
+    os.replace(tmp, library)
     if verbose:
-        print(f"built {LIBRARY}", file=sys.stderr)
-    return LIBRARY
+        print(f"built {library}", file=sys.stderr)
+    return library
 
 
 if __name__ == "__main__":

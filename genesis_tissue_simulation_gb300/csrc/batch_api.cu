@@ -56,6 +56,7 @@ struct Batch {
     Buf<float2> tetStiff, tetAlpha;
     Buf<int> nodeBaseD, nodeCountD, order, ctaStart;
     Buf<unsigned> derived, state;
+    Buf<unsigned> bounds;                            // debug builds: out-of-range gather record
     Buf<ContactFrame> frames;
     unsigned* hostStatus = nullptr;
     ContactFrame* framesHost = nullptr; size_t framesHostCap = 0;
@@ -84,7 +85,7 @@ void releaseAll() {
                     &G.edgeSupport, &G.nodeInstance, &G.nodeBaseD, &G.nodeCountD, &G.order, &G.ctaStart}) b->release();
     for (auto* b : {&G.edgeEnds, &G.unionEdge, &G.unionBend, &G.unionTet, &G.instEdge, &G.instBend, &G.instTet}) b->release();
     G.edgeRest.release(); G.bendIJK.release(); G.tetIds.release(); G.bendPairs.release(); G.tetStiff.release(); G.tetAlpha.release();
-    G.derived.release(); G.state.release(); G.frames.release();
+    G.derived.release(); G.state.release(); G.frames.release(); G.bounds.release();
     if (G.framesHost) cudaFreeHost(G.framesHost);
     G.framesHost = nullptr; G.framesHostCap = 0;
     G.packedXyz.release();
@@ -142,6 +143,7 @@ DeviceMesh batchMesh() {
     m.edgeSupport = G.edgeSupport.p;
     m.nodeInstance = G.nodeInstance.p; m.contactFrames = G.frames.p; m.nInstances = G.count;
     std::memcpy(m.typeB, G.typeB, sizeof(G.typeB));
+    m.bounds = G.bounds.p;
     return m;
 }
 
@@ -487,6 +489,10 @@ LCS_API int GBT_BatchInit(int count, const GbtInstanceDesc* inst, const GbtBatch
     rc = packInstances(G.smCount * 2);
     if (rc) return rc;
     G.tool.assign(count, ToolPose{}); G.toolFrom = G.tool;
+#ifdef GBT_DEBUG_BOUNDS
+    CK(G.bounds.alloc(3));
+    CK(cudaMemsetAsync(G.bounds.p, 0, 3 * sizeof(unsigned), G.stream));
+#endif
     CK(cudaStreamSynchronize(G.stream));
     G.ready = true;
     return 0;
@@ -624,6 +630,21 @@ LCS_API int GBT_BatchProfileRead(float* msTotal) {
     }
     *msTotal = total;
     return 0;
+}
+
+// Debug builds (GBT_DEBUG_BOUNDS): the batch's out-of-range gather record, then cleared (release
+// builds: LCS_ERR_UNSUPPORTED).
+LCS_API int GBT_BatchDebugBoundsRead(unsigned* out3) {
+#ifdef GBT_DEBUG_BOUNDS
+    if (!G.ready || !out3 || !G.bounds.p) return XPBD_ERR_BAD_ARG;
+    CK(cudaMemcpyAsync(out3, G.bounds.p, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, G.stream));
+    CK(cudaMemsetAsync(G.bounds.p, 0, 3 * sizeof(unsigned), G.stream));
+    CK(cudaStreamSynchronize(G.stream));
+    return 0;
+#else
+    (void)out3;
+    return LCS_ERR_UNSUPPORTED;
+#endif
 }
 
 LCS_API void GBT_BatchShutdown() {

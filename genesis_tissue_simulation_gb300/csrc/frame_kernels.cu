@@ -449,7 +449,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 for (int k = m.tetRange[c].x + r; k < m.tetRange[c].y; k += R) {
                     refreshTet(m, k);
                     if (fc.fallback && (m.tetMeta[k] & 8))
-                        for (int o = 0; o < 3; o++) m.edgeSupport[m.tetOwner[3 * k + o]] = 1;
+                        for (int o = 0; o < 3; o++) m.edgeSupport[checkSlot(m, m.tetOwner[3 * k + o], kSiteTetSlot)] = 1;
                 }
             derivedAt = revision;
         }

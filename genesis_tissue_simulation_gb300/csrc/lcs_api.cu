@@ -120,6 +120,7 @@ struct Session {
     // changes whenever the liveness flags must be derived again from scratch (a new mesh, a restored
     // state); LCS_StepNoAlloc keeps its liveness record only for the generation that wrote it
     unsigned long long generation = 0;
+    DBuf<unsigned> bounds;                  // debug builds: out-of-range gather record (violations, index, site)
 };
 Session S;
 unsigned long long g_sessionGeneration = 0;
@@ -144,7 +145,7 @@ void freePhysics() {
     for (auto* b : {&S.pinned, &S.active, &S.nbr, &S.edgeColorOffD, &S.bendColorOffD, &S.tetColorOffD, &S.edgeOwner, &S.edgeLive,
                     &S.bendSrc, &S.bendLive, &S.tetMeta, &S.tetOwner, &S.edgeSupport}) b->release();
     S.edgeEnds.release(); S.edgeRest.release(); S.bendIJK.release(); S.bendPairs.release(); S.tetIds.release();
-    S.tetAlpha.release(); S.tetStiff.release(); S.state.release();
+    S.tetAlpha.release(); S.tetStiff.release(); S.state.release(); S.bounds.release();
     S.fiberLambda.release(); S.feasTarget.release(); S.needed.release(); S.incOff.release(); S.incTet.release(); S.guardFlags.release();
     S.rotA.release(); S.rotB.release(); S.rotParity = 0;
     S.volumePasses = 0; S.minVolume = 0.f;
@@ -305,6 +306,7 @@ DeviceMesh deviceMesh() {
     m.fiberLambda = S.fiberLambda.p; m.feasTarget = S.feasTarget.p; m.needed = S.needed.p;
     m.incOff = S.incOff.p; m.incTet = S.incTet.p; m.guardFlags = S.guardFlags.p;
     m.particleRot[0] = S.rotA.p; m.particleRot[1] = S.rotB.p;
+    m.bounds = S.bounds.p;
     return m;
 }
 
@@ -598,6 +600,10 @@ LCS_API int LCS_InitPhysics(const PhysicsInitDesc* desc, const float* mass, cons
     S.rotParity = 0;
     rc = uploadFrameState();
     if (rc) return rc;
+#ifdef GBT_DEBUG_BOUNDS
+    CK(S.bounds.alloc(3));
+    CK(cudaMemsetAsync(S.bounds.p, 0, 3 * sizeof(unsigned), S.stream));
+#endif
     CK(cudaStreamSynchronize(S.stream));
     S.generation = ++g_sessionGeneration;
     S.physReady = true;
@@ -1228,6 +1234,21 @@ LCS_API int LCS_GetSolvedJaw(float*) { return LCS_ERR_UNSUPPORTED; }
 LCS_API int LCS_GetContactReaction(float*, int*) { return LCS_ERR_UNSUPPORTED; }
 LCS_API int LCS_GetJawLoad(float*) { return LCS_ERR_UNSUPPORTED; }
 LCS_API int LCS_GetMaterialQuality(float*) { return LCS_ERR_UNSUPPORTED; }
+
+// Debug builds (GBT_DEBUG_BOUNDS): the session's out-of-range gather record -- violations since the
+// last read, the first bad index and its site (BoundsSite) -- then cleared.  Release builds record
+// nothing and answer LCS_ERR_UNSUPPORTED.
+LCS_API int GBT_DebugBoundsRead(unsigned* out3) {
+#ifdef GBT_DEBUG_BOUNDS
+    if (!S.physReady || !out3 || !S.bounds.p) return XPBD_ERR_BAD_ARG;
+    CK(cudaMemcpyAsync(out3, S.bounds.p, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaMemsetAsync(S.bounds.p, 0, 3 * sizeof(unsigned), S.stream));
+    return cudaStatus(cudaStreamSynchronize(S.stream));
+#else
+    (void)out3;
+    return LCS_ERR_UNSUPPORTED;
+#endif
+}
 
 LCS_API int LCS_SetBarrierTest(int extraArrivals, float budgetSeconds) {
     if (extraArrivals < 0 || !(budgetSeconds > 0.f) || budgetSeconds > 10.f) return XPBD_ERR_BAD_ARG;

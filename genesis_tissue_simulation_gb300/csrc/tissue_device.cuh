@@ -58,7 +58,36 @@ struct DeviceMesh {
     // particle frames (9 floats per node, rows of R): two buffers, current and previous, that
     // alternate on every frame pass
     float* particleRot[2];
+    // debug builds (GBT_DEBUG_BOUNDS): out-of-range gather records [violations, first bad index,
+    // site of the first]; null otherwise
+    unsigned* bounds;
 };
+
+// Gather-index checks of the debug build (GBT_DEBUG_BOUNDS, the stand-in for a memory checker):
+// an element's node index outside the nodes the kernel serves, or a neighbour-table slot outside
+// the table, is recorded in m.bounds and replaced by a valid index so the access stays in range.
+// Release builds compile both to the index itself.
+enum BoundsSite : unsigned { kSiteEdge = 1, kSiteBend = 2, kSiteTet = 3, kSiteEdgeSlot = 4, kSiteTetSlot = 5, kSiteNeighbour = 6 };
+__device__ __forceinline__ void recordBounds(unsigned* rec, int index, unsigned site) {
+    if (!rec) return;
+    if (atomicAdd(rec, 1u) == 0u) { rec[1] = (unsigned)index; rec[2] = site; }
+}
+__device__ __forceinline__ int checkNode(const DeviceMesh& m, int i, unsigned site) {
+#ifdef GBT_DEBUG_BOUNDS
+    if ((unsigned)(i - m.nodeBase) >= (unsigned)m.nNodes) { recordBounds(m.bounds, i, site); return m.nodeBase; }
+#else
+    (void)m; (void)site;
+#endif
+    return i;
+}
+__device__ __forceinline__ int checkSlot(const DeviceMesh& m, int s, unsigned site) {
+#ifdef GBT_DEBUG_BOUNDS
+    if ((unsigned)(s - 6 * m.nodeBase) >= (unsigned)(6 * m.nNodes)) { recordBounds(m.bounds, s, site); return 6 * m.nodeBase; }
+#else
+    (void)m; (void)site;
+#endif
+    return s;
+}
 
 // A node's position: plain device memory, or its slot in the cluster's distributed shared memory.
 template <bool Dsm>
@@ -234,8 +263,9 @@ struct EdgeRecord { int2 ij; int live; float rest; f3 qi, qj; };
 __device__ __forceinline__ EdgeRecord loadEdge(const DeviceMesh& m, int e, const FrameCoeffs& fc) {
     EdgeRecord r;
     r.live = m.edgeLive[e];
-    if (fc.fallback && r.live && m.edgeSupport[m.edgeOwner[e]]) r.live = 0;   // a live tet carries the edge
+    if (fc.fallback && r.live && m.edgeSupport[checkSlot(m, m.edgeOwner[e], kSiteEdgeSlot)]) r.live = 0;   // a live tet carries the edge
     r.ij = m.edgeEnds[e];
+    r.ij.x = checkNode(m, r.ij.x, kSiteEdge); r.ij.y = checkNode(m, r.ij.y, kSiteEdge);
     r.rest = m.edgeRest[e];
     r.qi = xyz(m.prev[r.ij.x]);
     r.qj = xyz(m.prev[r.ij.y]);
@@ -293,6 +323,7 @@ template <bool Dsm = false>
 __device__ __forceinline__ void projectBend(const DeviceMesh& m, int e, const FrameCoeffs& fc) {
     if (m.bendLive[e] == 0) return;
     int4 r = m.bendIJK[e];
+    r.x = checkNode(m, r.x, kSiteBend); r.y = checkNode(m, r.y, kSiteBend); r.z = checkNode(m, r.z, kSiteBend);
     float4 Pi = posRef<Dsm>(m, r.x), Pj = posRef<Dsm>(m, r.y), Pk = posRef<Dsm>(m, r.z);
     float wi = Pi.w, wj = Pj.w, wk = Pk.w;
     if (wi + wj + wk <= 0.f) return;
@@ -326,6 +357,8 @@ __device__ __forceinline__ TetRecord loadTet(const DeviceMesh& m, int k) {
     TetRecord t;
     t.meta = m.tetMeta[k];
     t.ids = m.tetIds[k];
+    t.ids.x = checkNode(m, t.ids.x, kSiteTet); t.ids.y = checkNode(m, t.ids.y, kSiteTet);
+    t.ids.z = checkNode(m, t.ids.z, kSiteTet); t.ids.w = checkNode(m, t.ids.w, kSiteTet);
     t.alpha = m.tetAlpha[k];
     t.q[0] = xyz(m.prev[t.ids.x]); t.q[1] = xyz(m.prev[t.ids.y]); t.q[2] = xyz(m.prev[t.ids.z]); t.q[3] = xyz(m.prev[t.ids.w]);
     return t;
@@ -415,12 +448,15 @@ __device__ __forceinline__ void projectTet(const DeviceMesh& m, int k, const Fra
 // (xpbd_solver.cu:429-466).
 __device__ __forceinline__ void refreshEdge(const DeviceMesh& m, int e) {
     int2 ij = m.edgeEnds[e];
-    m.edgeLive[e] = (m.nbr[m.edgeOwner[e]] >= 0 && m.active[ij.x] != 0 && m.active[ij.y] != 0) ? 1 : 0;
+    ij.x = checkNode(m, ij.x, kSiteEdge); ij.y = checkNode(m, ij.y, kSiteEdge);
+    m.edgeLive[e] = (m.nbr[checkSlot(m, m.edgeOwner[e], kSiteEdgeSlot)] >= 0 && m.active[ij.x] != 0 && m.active[ij.y] != 0) ? 1 : 0;
 }
 __device__ __forceinline__ void refreshTet(const DeviceMesh& m, int k) {
     const int* o = m.tetOwner + 3 * k;
     int4 d = m.tetIds[k];
-    bool live = m.nbr[o[0]] >= 0 && m.nbr[o[1]] >= 0 && m.nbr[o[2]] >= 0 && m.active[d.x] != 0 && m.active[d.y] != 0 &&
+    d.x = checkNode(m, d.x, kSiteTet); d.y = checkNode(m, d.y, kSiteTet); d.z = checkNode(m, d.z, kSiteTet); d.w = checkNode(m, d.w, kSiteTet);
+    const int o0 = checkSlot(m, o[0], kSiteTetSlot), o1 = checkSlot(m, o[1], kSiteTetSlot), o2 = checkSlot(m, o[2], kSiteTetSlot);
+    bool live = m.nbr[o0] >= 0 && m.nbr[o1] >= 0 && m.nbr[o2] >= 0 && m.active[d.x] != 0 && m.active[d.y] != 0 &&
                 m.active[d.z] != 0 && m.active[d.w] != 0;
     int meta = m.tetMeta[k];
     m.tetMeta[k] = (meta & ~8) | (live ? 8 : 0);

@@ -169,6 +169,14 @@ LCS_API int GBT_GetActive(int* outN);           /* physics_active (V/physics.h:6
  * output; the replay tests load the reference build's state.  Invalid tables: -1004, nothing written. */
 LCS_API int GBT_SetState(const float* pos3N, const float* vel3N, const int* nbr6N, const void* bendPairs, const int* active,
                          const unsigned* cutMaskV, const float* edgeCutT6N, const float* rot9N, int setRevision, unsigned revision);
+/* Debug builds (libgbtissue_debug.so, compiled with GBT_DEBUG_BOUNDS; the stand-in for a memory
+ * checker): every element gather index (edge ends, bend nodes, tet nodes, neighbour-table owner
+ * slots) is checked against the nodes the kernel serves; a violation is counted, its index and site
+ * (1 edge, 2 bend, 3 tet, 4 edge owner slot, 5 tet owner slot) recorded and the access redirected in
+ * range.  out3 = {violations, first index, first site}, cleared by the read.  Release builds:
+ * LCS_ERR_UNSUPPORTED. */
+LCS_API int GBT_DebugBoundsRead(unsigned* out3);
+LCS_API int GBT_BatchDebugBoundsRead(unsigned* out3);
 LCS_API int LCS_SetLaunchMode(int mode);         /* 0 automatic, 1 whole-GPU cooperative grid, 2 one CTA, 3 one thread-block cluster (plain frames) */
 /* Failure-detection test mode of the grid barrier: every barrier awaits `extraArrivals` arrivals that
  * never come and gives up after `budgetSeconds` (normal budget 2 s); LCS_Step then returns -4002 and

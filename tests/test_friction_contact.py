@@ -37,7 +37,7 @@ def surfaceless_grid():
     return g.__class__(**{**vars(g), "surface_edges": np.zeros((0, 8), dtype=np.int32)})
 
 
-def friction_run(lib, steps=10, closing=False, launch_mode=None, enabled=1, reference=False):
+def friction_run(lib, steps=10, closing=False, launch_mode=None, enabled=1, reference=False, on_close=None):
     g = surfaceless_grid()
     s = PlainTissue(g, dt=1 / 60, substeps=10, ks=1e6, young_pa=6000.0, strain_damping_s=0.0, grasp_params=GraspParams(**GRASP),
                     dll_path=lib, reference=reference)
@@ -53,6 +53,8 @@ def friction_run(lib, steps=10, closing=False, launch_mode=None, enabled=1, refe
             s.check("LCS_SetGraspTool", ctypes.byref(grasper(top, k, steps, closing)))
             s.step()
             frames.append(s.positions())
+        if on_close is not None:
+            on_close(s)
         return g, frames
     finally:
         if launch_mode is not None:

@@ -17,7 +17,7 @@ from genesis_tissue_simulation_gb300.native_backend import Capsule, GraspParams,
 GRASP = dict(W.DEFAULT_GRASP, ccd_velocity=0.0)
 
 
-def guarded_run(lib, steps=12, minimum=0.9, passes=1, launch_mode=None, press=0.6):
+def guarded_run(lib, steps=12, minimum=0.9, passes=1, launch_mode=None, press=0.6, on_close=None):
     """C1 lattice, guard armed as the reference adapter arms it (strength 80, bulk damping 0.01 s),
     a capsule pressed ``press`` cm into the top.  Returns positions after every step and the
     oracle's feasibility counters (None for the CUDA library)."""
@@ -41,6 +41,8 @@ def guarded_run(lib, steps=12, minimum=0.9, passes=1, launch_mode=None, press=0.
         if hasattr(s.dll, "ORC_GuardStats"):
             stats = np.zeros(3, dtype=np.int64)
             s.dll.ORC_GuardStats(stats.ctypes.data_as(ctypes.c_void_p))
+        if on_close is not None:
+            on_close(s)
         return g, frames, stats
     finally:
         if launch_mode is not None:
