@@ -364,6 +364,19 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, ra
             b.positions(out=positions)
         e2e_s = time.perf_counter() - e0
         assert np.isfinite(positions).all(), "non-finite batched state"
+        tables = b.element_tables()
+        explicit_ms = None
+        if tables == "implicit":   # the same frames on the explicit element tables, for comparison
+            b.set_element_tables(False)
+            b.step_many(w.capsule_array_at(warmup + 2 * frames)[None], use_graph=True)
+            torch.cuda.synchronize()
+            b.profile(1)
+            for k in range(warmup + 2 * frames, warmup + 2 * frames + min(frames, 10)):
+                b.step_many(w.capsule_array_at(k + 1)[None], use_graph=True)
+            torch.cuda.synchronize()
+            explicit_ms = b.profile_read() / min(frames, 10)
+            b.profile(0)
+            b.set_element_tables(True)
         gathered, gather_s = None, 0.0
         if world > 1:   # the split's only exchange: rank 0 collects every instance's positions
             local = [b.instance_positions(positions, j).copy() for j in range(len(w.grids))]
@@ -419,7 +432,9 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, ra
         "proj_per_s": value * w.substeps * (info["edges"] + info["tets"]) / count,
         "instances": count, "lattice_nodes": info["nodes"], "active_nodes": n_active, "tets": info["tets"],
         "edges": info["edges"], "substeps": w.substeps, "launch": {"mode": tune["mode"], "threads": tune["threads"],
-                                                                    "autotune_ms_per_frame": tune["ms_per_frame"]},
+                                                                    "autotune_ms_per_frame": tune["ms_per_frame"],
+                                                                    "element_tables": tables,
+                                                                    "explicit_tables_ms_per_frame": explicit_ms},
         "plain_instance_steps_per_s": plain_rate, "plain_sample": f"{len(picks)} instances spread over the size order, "
                                                                   f"{plain_frames} frames each after 4 warm-up frames (past the automatic launch-shape trials)",
         "batched_over_plain": value / plain_rate,

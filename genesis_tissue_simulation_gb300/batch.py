@@ -33,6 +33,7 @@ SIGNATURES = (
     ("GBT_BatchGetPositions", (P,), I), ("GBT_BatchNodeRange", (I, P, P), I), ("GBT_BatchInfo", (P,), I),
     ("GBT_BatchSetLaunch", (I, I), I), ("GBT_BatchAutotune", (F, I, P, P, P), I), ("GBT_BatchProfileEnable", (I,), None),
     ("GBT_BatchProfileRead", (P,), I), ("GBT_BatchShutdown", (), None),
+    ("GBT_BatchSetElementTables", (I,), I), ("GBT_BatchElementTables", (), I),
 )
 
 
@@ -132,6 +133,13 @@ class TissueBatch:
             self.check("GBT_BatchStepMany", self.dt, steps, ct.byref(tools), int(use_graph))
         else:
             self.check("GBT_BatchStepMany", self.dt, int(steps), None, int(use_graph))
+
+    def set_element_tables(self, implicit_codes: bool):
+        """Implicit lattice codes (True) or explicit element tables (False) in the frame kernels."""
+        self.check("GBT_BatchSetElementTables", int(bool(implicit_codes)))
+
+    def element_tables(self) -> str:
+        return "implicit" if self.f["GBT_BatchElementTables"]() else "explicit"
 
     def set_launch(self, mode, threads=256):
         self.check("GBT_BatchSetLaunch", mode, threads)

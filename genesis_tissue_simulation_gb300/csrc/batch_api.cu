@@ -57,6 +57,10 @@ struct Batch {
     Buf<int> nodeBaseD, nodeCountD, order, ctaStart;
     Buf<unsigned> derived, state;
     Buf<unsigned> bounds;                            // debug builds: out-of-range gather record
+    // implicit lattice elements (tissue_device.cuh): codes in colour order, per-instance geometry,
+    // per-instance per-type stiffness and compliances; `useCodes` selects them over the explicit tables
+    Buf<unsigned> tetCode, edgeCode; Buf<int4> instGeo; Buf<float2> instStiff, instAlpha;
+    bool codesAvailable = false, useCodes = false;
     Buf<ContactFrame> frames;
     unsigned* hostStatus = nullptr;
     ContactFrame* framesHost = nullptr; size_t framesHostCap = 0;
@@ -86,6 +90,8 @@ void releaseAll() {
     for (auto* b : {&G.edgeEnds, &G.unionEdge, &G.unionBend, &G.unionTet, &G.instEdge, &G.instBend, &G.instTet}) b->release();
     G.edgeRest.release(); G.bendIJK.release(); G.tetIds.release(); G.bendPairs.release(); G.tetStiff.release(); G.tetAlpha.release();
     G.derived.release(); G.state.release(); G.frames.release(); G.bounds.release();
+    G.tetCode.release(); G.edgeCode.release(); G.instGeo.release(); G.instStiff.release(); G.instAlpha.release();
+    G.codesAvailable = G.useCodes = false;
     if (G.framesHost) cudaFreeHost(G.framesHost);
     G.framesHost = nullptr; G.framesHostCap = 0;
     G.packedXyz.release();
@@ -144,6 +150,7 @@ DeviceMesh batchMesh() {
     m.nodeInstance = G.nodeInstance.p; m.contactFrames = G.frames.p; m.nInstances = G.count;
     std::memcpy(m.typeB, G.typeB, sizeof(G.typeB));
     m.bounds = G.bounds.p;
+    if (G.useCodes) { m.tetCode = G.tetCode.p; m.edgeCode = G.edgeCode.p; m.instGeo = G.instGeo.p; m.instAlpha = G.instAlpha.p; }
     return m;
 }
 
@@ -280,6 +287,10 @@ int prepareAlphas(float h) {
     if (G.T > 0 && G.youngE > 0.f && h != G.lastH) {
         tetAlphaKernel<<<(G.T + 255) / 256, 256, 0, G.stream>>>(G.T, 1.f / (h * h), G.tetStiff.p, G.tetAlpha.p);
         CK(cudaGetLastError());
+        if (G.codesAvailable) {   // the same operation on each instance's six Kuhn types
+            tetAlphaKernel<<<(6 * G.count + 255) / 256, 256, 0, G.stream>>>(6 * G.count, 1.f / (h * h), G.instStiff.p, G.instAlpha.p);
+            CK(cudaGetLastError());
+        }
         G.lastH = h;
     }
     return 0;
@@ -464,6 +475,55 @@ LCS_API int GBT_BatchInit(int count, const GbtInstanceDesc* inst, const GbtBatch
         }
         uTet.push_back(make_int2(lo, (int)tIds.size()));
     }
+    // Implicit element codes (tissue_device.cuh), when every element is where the lattice formula
+    // puts it: instance nodes below 2^15, instances below 2^13, each tet's nodes the Kuhn path of its
+    // type from its corner 0, each edge an axis step of its lower end, one stiffness per instance and
+    // Kuhn type, and no tet-support fallback (ks > 0).
+    std::vector<unsigned> tCode, eCode;
+    std::vector<int4> geo(count);
+    std::vector<float2> iStiff((size_t)6 * count, make_float2(0.f, 0.f));
+    std::vector<char> seenType((size_t)6 * count, 0);
+    bool codes = count < (1 << 13) && G.ks > 0.f;
+    for (int i = 0; i < count && codes; i++) {
+        const int nx = inst[i].dimsX + 1, nxy = (inst[i].dimsX + 1) * (inst[i].dimsY + 1);
+        geo[i] = make_int4(G.nodeBase[i], nx, nxy, 0);
+        codes = G.nodeCount[i] < (1 << 15);
+    }
+    static const int kPath[6][4] = {{0, 1, 3, 7}, {0, 3, 2, 7}, {0, 2, 6, 7}, {0, 6, 4, 7}, {0, 4, 5, 7}, {0, 5, 1, 7}};
+    auto corner = [](int c, int nx, int nxy) { return (c & 1) + ((c >> 1) & 1) * nx + ((c >> 2) & 1) * nxy; };
+    if (codes) {
+        const std::vector<int>& nodeInstance = nodeInst;
+        tCode.resize(tIds.size());
+        for (size_t k = 0; k < tIds.size() && codes; k++) {
+            const int4 d = tIds[k];
+            const int i = nodeInstance[d.x], type = tMeta[k] & 7;
+            const int4 g = geo[i];
+            const int local = d.x - g.x;
+            const int want[4] = {d.x, d.x + corner(kPath[type][1], g.y, g.z), d.x + corner(kPath[type][2], g.y, g.z),
+                                 d.x + corner(7, g.y, g.z)};
+            codes = want[0] == d.x && want[1] == d.y && want[2] == d.z && want[3] == d.w;
+            float2& st = iStiff[(size_t)6 * i + type];
+            if (!seenType[(size_t)6 * i + type]) { st = tStiff[k]; seenType[(size_t)6 * i + type] = 1; }
+            codes = codes && std::memcmp(&st, &tStiff[k], sizeof(float2)) == 0;
+            tCode[k] = (unsigned)local | (unsigned)type << 15 | kCodeLive | (unsigned)i << 19;
+        }
+        eCode.resize(eEnds.size());
+        for (size_t k = 0; k < eEnds.size() && codes; k++) {
+            const int2 d = eEnds[k];
+            const int i = nodeInstance[d.x];
+            const int4 g = geo[i];
+            const int step = d.y - d.x, axis = step == 1 ? 0 : step == g.y ? 1 : step == g.z ? 2 : -1;
+            codes = axis >= 0 && eOwner[k] == 6 * d.x + 2 * axis + 1 && nodeInstance[d.y] == i;
+            eCode[k] = (unsigned)(d.x - g.x) | (unsigned)(axis & 3) << 15 | kCodeLive | (unsigned)i << 19;
+        }
+    }
+    G.codesAvailable = codes;
+    G.useCodes = codes;
+    if (codes) {
+        CK(G.tetCode.upload(tCode.data(), tCode.size(), G.stream)); CK(G.edgeCode.upload(eCode.data(), eCode.size(), G.stream));
+        CK(G.instGeo.upload(geo.data(), count, G.stream)); CK(G.instStiff.upload(iStiff.data(), iStiff.size(), G.stream));
+        CK(G.instAlpha.alloc((size_t)6 * count));
+    }
     std::vector<float4> zero4(G.N, make_float4(0, 0, 0, 0));
     std::vector<int> ones(std::max(std::max(G.E, G.B), 1), 1), zeros6((size_t)6 * G.N, 0);
     std::vector<unsigned> derived(count, ~0u), state(4, 0u);
@@ -557,6 +617,19 @@ LCS_API int GBT_BatchNodeRange(int instance, int* base, int* count) {
     *base = G.nodeBase[instance]; *count = G.nodeCount[instance];
     return 0;
 }
+
+// Element tables of the frame kernels: 1 the implicit lattice codes (the default where the batch
+// qualifies), 0 the explicit tables; both give identical results.  Returns -4001 when 1 is asked of a
+// batch that does not qualify.
+LCS_API int GBT_BatchSetElementTables(int implicitCodes) {
+    if (!G.ready) return XPBD_ERR_NOT_READY;
+    if (implicitCodes && !G.codesAvailable) return LCS_ERR_UNSUPPORTED;
+    if ((implicitCodes != 0) != G.useCodes) dropGraph();
+    G.useCodes = implicitCodes != 0;
+    return 0;
+}
+
+LCS_API int GBT_BatchElementTables() { return G.ready && G.useCodes ? 1 : 0; }
 
 LCS_API int GBT_BatchSetLaunch(int mode, int threads) {
     if (!G.ready || mode < 0 || mode > 2) return XPBD_ERR_BAD_ARG;

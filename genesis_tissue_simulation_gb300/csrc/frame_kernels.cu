@@ -400,7 +400,8 @@ __device__ __noinline__ void frictionPhase(const DeviceMesh& m, const FrameCoeff
 // Ahead (only where registers allow: the one-CTA-per-SM kernels): with edge pairs, the thread's
 // first pair of colour c+1 is loaded before colour c's edges are projected, and the node passes
 // take two nodes at a time.
-template <class Sync, bool Extended, bool Dsm = false, bool Rotations = false, int EdgeGroup = 1, bool Ahead = false>
+// Codes: batched instances, whose element tables may be the implicit lattice codes.
+template <class Sync, bool Extended, bool Dsm = false, bool Rotations = false, int EdgeGroup = 1, bool Ahead = false, bool Codes = false>
 __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
                          const ContactParams& cp, const CutParams& cu, unsigned* state, Sync& sync) {
     const int r = sync.spreadRank(), R = sync.size();
@@ -442,12 +443,12 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 if (!sync.sync()) return;
             }
             for (int c = 0; c < m.nEdgeColors; c++)
-                for (int e = m.edgeRange[c].x + r; e < m.edgeRange[c].y; e += R) refreshEdge(m, e);
+                for (int e = m.edgeRange[c].x + r; e < m.edgeRange[c].y; e += R) refreshEdge<Codes>(m, e);
             for (int c = 0; c < m.nBendColors; c++)
                 for (int b = m.bendRange[c].x + r; b < m.bendRange[c].y; b += R) m.bendLive[b] = m.bendPairs[m.bendSrc[b]].alive != 0 ? 1 : 0;
             for (int c = 0; c < m.nTetColors; c++)
                 for (int k = m.tetRange[c].x + r; k < m.tetRange[c].y; k += R) {
-                    refreshTet(m, k);
+                    refreshTet<Codes>(m, k);
                     if (fc.fallback && (m.tetMeta[k] & 8))
                         for (int o = 0; o < 3; o++) m.edgeSupport[checkSlot(m, m.tetOwner[3 * k + o], kSiteTetSlot)] = 1;
                 }
@@ -482,7 +483,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         auto loadFirstTet = [&]() {
             const int2 first = m.nTetColors > 0 ? m.tetRange[0] : make_int2(0, 0);
             hasNext = first.x + r < first.y;
-            if (hasNext) next = loadTet(m, first.x + r);
+            if (hasNext) next = loadTet<Codes>(m, first.x + r);
             tetLoaded = true;
         };
         if (fc.doEdges) {
@@ -491,8 +492,8 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
             if (Ahead && EdgeGroup == 2 && m.nEdgeColors > 0) {
                 const int2 g0 = m.edgeRange[0];
                 h0 = g0.x + r < g0.y; h1 = g0.x + r + R < g0.y;
-                if (h0) n0 = loadEdge(m, g0.x + r, fc);
-                if (h1) n1 = loadEdge(m, g0.x + r + R, fc);
+                if (h0) n0 = loadEdge<Codes>(m, g0.x + r, fc);
+                if (h1) n1 = loadEdge<Codes>(m, g0.x + r + R, fc);
             }
             for (int c = 0; c < m.nEdgeColors; c++) {
                 int2 rg = m.edgeRange[c];
@@ -502,17 +503,17 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                     if (c + 1 < m.nEdgeColors) {
                         const int2 ng = m.edgeRange[c + 1];
                         h0 = ng.x + r < ng.y; h1 = ng.x + r + R < ng.y;
-                        if (h0) n0 = loadEdge(m, ng.x + r, fc);
-                        if (h1) n1 = loadEdge(m, ng.x + r + R, fc);
+                        if (h0) n0 = loadEdge<Codes>(m, ng.x + r, fc);
+                        if (h1) n1 = loadEdge<Codes>(m, ng.x + r + R, fc);
                     }
                     if (k1) applyEdgePair<Dsm>(m, c0, c1, fc);
                     else if (k0) applyEdge<Dsm>(m, c0, fc);
                     for (int e = rg.x + r + 2 * R; e < rg.y; e += 2 * R) {
-                        if (e + R < rg.y) applyEdgePair<Dsm>(m, loadEdge(m, e, fc), loadEdge(m, e + R, fc), fc);
-                        else applyEdge<Dsm>(m, loadEdge(m, e, fc), fc);
+                        if (e + R < rg.y) applyEdgePair<Dsm>(m, loadEdge<Codes>(m, e, fc), loadEdge<Codes>(m, e + R, fc), fc);
+                        else applyEdge<Dsm>(m, loadEdge<Codes>(m, e, fc), fc);
                     }
                 } else {
-                    for (int e = rg.x + r; e < rg.y; e += R) applyEdge<Dsm>(m, loadEdge(m, e, fc), fc);
+                    for (int e = rg.x + r; e < rg.y; e += R) applyEdge<Dsm>(m, loadEdge<Codes>(m, e, fc), fc);
                 }
                 if (Ahead && c + 1 == m.nEdgeColors && fc.doStrain && !fc.doBend) loadFirstTet();
                 if (!sync.sync()) return;
@@ -534,9 +535,9 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 bool hasCur = hasNext;
                 int2 nrg = c + 1 < m.nTetColors ? m.tetRange[c + 1] : make_int2(0, 0);
                 hasNext = nrg.x + r < nrg.y;
-                if (hasNext) next = loadTet(m, nrg.x + r);
+                if (hasNext) next = loadTet<Codes>(m, nrg.x + r);
                 if (hasCur) applyTet<Dsm>(m, cur, fc, guarded);
-                for (int k = rg.x + r + R; k < rg.y; k += R) projectTet<Dsm>(m, k, fc, guarded);
+                for (int k = rg.x + r + R; k < rg.y; k += R) projectTet<Dsm, Codes>(m, k, fc, guarded);
                 if (!sync.sync()) return;
                 mark(s, kPhaseTets);
             }
@@ -599,8 +600,8 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
             for (int c = 0; c < m.nEdgeColors; c++) {
                 int2 rg = m.edgeRange[c];
                 for (int e = rg.x + r; e < rg.y; e += R) {
-                    if (m.edgeLive[e] == 0) continue;
-                    int2 ij = m.edgeEnds[e];
+                    int2 ij;
+                    if (!edgeNodes<Codes>(m, e, ij)) continue;
                     float4 Pi = posRef<Dsm>(m, ij.x), Pj = posRef<Dsm>(m, ij.y);
                     float wi = Pi.w, wj = Pj.w;
                     if (wi + wj <= 0.f) continue;
@@ -681,7 +682,7 @@ __device__ __forceinline__ void runInstances(const DeviceMesh& m, const FrameCoe
         v.edgeRange = it.edgeRange + (size_t)i * m.nEdgeColors;
         v.bendRange = it.bendRange + (size_t)i * m.nBendColors;
         v.tetRange = it.tetRange + (size_t)i * m.nTetColors;
-        runFrame<BlockSync, false>(v, fc, none, none, cp, noCut, it.derived + i, b);
+        runFrame<BlockSync, false, false, false, 1, false, true>(v, fc, none, none, cp, noCut, it.derived + i, b);
         __syncthreads();
     }
 }
@@ -727,7 +728,7 @@ __global__ void __launch_bounds__(kClusterThreads) frameKernelCluster(DeviceMesh
         v.dsm = bases; v.dsmLogB = kClusterLogThreads; v.dsmLogK = logK;
         for (int n = sync.r; n < v.nNodes; n += sync.n) posRef<true>(v, v.nodeBase + n) = m.pos[v.nodeBase + n];
         cluster.sync();
-        runFrame<ClusterSync, false, true>(v, fc, none, none, cp, noCut, it.derived + i, sync);
+        runFrame<ClusterSync, false, true, false, 1, false, true>(v, fc, none, none, cp, noCut, it.derived + i, sync);
         cluster.sync();
         for (int n = sync.r; n < v.nNodes; n += sync.n) m.pos[v.nodeBase + n] = posRef<true>(v, v.nodeBase + n);
     }
@@ -765,11 +766,11 @@ __global__ void __launch_bounds__(512) frameKernelInstances512(DeviceMesh m, Fra
     runInstances(m, fc, cp, it);
 }
 
-template <bool Extended, int EdgeGroup, bool Ahead>
+template <bool Extended, int EdgeGroup, bool Ahead, bool Codes = false>
 __device__ __forceinline__ void gridFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolPose& from, const ToolPose& to,
                                           const ContactParams& cp, const CutParams& cu, unsigned* state) {
     GridSync g{state + 1, state + 2, gridDim.x, 0u, fc.spinBudget, (unsigned)fc.syncTestExtra};
-    runFrame<GridSync, Extended, false, true, EdgeGroup, Ahead>(m, fc, from, to, cp, cu, state, g);
+    runFrame<GridSync, Extended, false, true, EdgeGroup, Ahead, Codes>(m, fc, from, to, cp, cu, state, g);
 }
 // A single mesh: one CTA per SM, so the tet projection keeps its registers without spilling (a
 // colour of ~19 k tets still finds a warp for every scheduler).
@@ -781,7 +782,7 @@ __global__ void __launch_bounds__(kFrameThreads, 1) frameKernelGrid(DeviceMesh m
 // table holds several elements per thread.
 __global__ void __launch_bounds__(kFrameThreads, 2) frameKernelLockstep(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                      ContactParams cp, CutParams cu, unsigned* state) {
-    gridFrame<false, 2, false>(m, fc, from, to, cp, cu, state);
+    gridFrame<false, 2, false, true>(m, fc, from, to, cp, cu, state);
 }
 __global__ void __launch_bounds__(kFrameThreads, 1) frameKernelGridExt(DeviceMesh m, FrameCoeffs fc, ToolPose from, ToolPose to,
                                                                      ContactParams cp, CutParams cu, unsigned* state) {

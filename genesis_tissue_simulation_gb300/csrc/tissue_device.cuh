@@ -61,7 +61,29 @@ struct DeviceMesh {
     // debug builds (GBT_DEBUG_BOUNDS): out-of-range gather records [violations, first bad index,
     // site of the first]; null otherwise
     unsigned* bounds;
+    // Batched lattices addressed implicitly (null: the explicit element tables above).  One 32-bit
+    // code per element, colour order as the explicit tables -- a tet: local node of its corner 0
+    // (bits 0-14), Kuhn type (15-17), live (18), instance (19-31); an edge: local node of its lower
+    // end (0-14), axis (15-16), live (18), instance (19-31) -- and per instance its first node and
+    // lattice strides (instGeo: base, nx, nx*ny, 0) and its six Kuhn types' compliances
+    // (instAlpha[6 i + type]).  Every node of a tet or edge follows from the code, so a colour sweep
+    // streams 4 B per element besides the edge rest lengths.
+    unsigned* tetCode; unsigned* edgeCode; const int4* instGeo; const float2* instAlpha;
 };
+
+// Corners a, b of Kuhn type t on its path 0 -> a -> b -> 7 (kKuhn in mesh_build.cu), 3 bits each,
+// type t at bit 6t.
+constexpr unsigned long long kKuhnPath = (1ull | 3ull << 3) | (3ull | 2ull << 3) << 6 | (2ull | 6ull << 3) << 12 |
+                                         (6ull | 4ull << 3) << 18 | (4ull | 5ull << 3) << 24 | (5ull | 1ull << 3) << 30;
+__device__ __forceinline__ int cornerOffset(unsigned corner, int nx, int nxy) {
+    return (int)(corner & 1u) + ((corner >> 1) & 1u ? nx : 0) + ((corner >> 2) & 1u ? nxy : 0);
+}
+// The nodes of an implicit tet: corner 0 at n0, then its Kuhn path.
+__device__ __forceinline__ int4 kuhnNodes(int type, int n0, int nx, int nxy) {
+    const unsigned a = (unsigned)(kKuhnPath >> (6 * type)) & 7u, b = (unsigned)(kKuhnPath >> (6 * type + 3)) & 7u;
+    return make_int4(n0, n0 + cornerOffset(a, nx, nxy), n0 + cornerOffset(b, nx, nxy), n0 + 1 + nx + nxy);
+}
+constexpr unsigned kCodeLive = 1u << 18;
 
 // Gather-index checks of the debug build (GBT_DEBUG_BOUNDS, the stand-in for a memory checker):
 // an element's node index outside the nodes the kernel serves, or a neighbour-table slot outside
@@ -260,11 +282,20 @@ __device__ __forceinline__ float logPositive(float x) {
 // ---------------------------------------------------------------------------------------------
 // What an edge projection reads that the sweep does not write (see TetRecord below).
 struct EdgeRecord { int2 ij; int live; float rest; f3 qi, qj; };
+template <bool Codes = false>   // Codes: the kernel may meet implicit lattice codes (batched instances)
 __device__ __forceinline__ EdgeRecord loadEdge(const DeviceMesh& m, int e, const FrameCoeffs& fc) {
     EdgeRecord r;
-    r.live = m.edgeLive[e];
-    if (fc.fallback && r.live && m.edgeSupport[checkSlot(m, m.edgeOwner[e], kSiteEdgeSlot)]) r.live = 0;   // a live tet carries the edge
-    r.ij = m.edgeEnds[e];
+    if (Codes && m.edgeCode) {   // implicit lattice (no tet-support fallback there): ends from the code
+        const unsigned code = m.edgeCode[e];
+        const int4 g = m.instGeo[code >> 19];
+        const int axis = (int)((code >> 15) & 3u), n0 = g.x + (int)(code & 0x7FFFu);
+        r.live = (code & kCodeLive) ? 1 : 0;
+        r.ij = make_int2(n0, n0 + (axis == 0 ? 1 : axis == 1 ? g.y : g.z));
+    } else {
+        r.live = m.edgeLive[e];
+        if (fc.fallback && r.live && m.edgeSupport[checkSlot(m, m.edgeOwner[e], kSiteEdgeSlot)]) r.live = 0;   // a live tet carries the edge
+        r.ij = m.edgeEnds[e];
+    }
     r.ij.x = checkNode(m, r.ij.x, kSiteEdge); r.ij.y = checkNode(m, r.ij.y, kSiteEdge);
     r.rest = m.edgeRest[e];
     r.qi = xyz(m.prev[r.ij.x]);
@@ -353,13 +384,23 @@ __device__ __forceinline__ void projectBend(const DeviceMesh& m, int e, const Fr
 // substep-start positions of its nodes.  Loading it ahead (before the barrier of the preceding
 // colour) takes two dependent L2 round trips off each colour's critical path.
 struct TetRecord { int4 ids; int meta; float2 alpha; f3 q[4]; };
+template <bool Codes = false>
 __device__ __forceinline__ TetRecord loadTet(const DeviceMesh& m, int k) {
     TetRecord t;
-    t.meta = m.tetMeta[k];
-    t.ids = m.tetIds[k];
+    if (Codes && m.tetCode) {   // implicit lattice: nodes from the code, compliances per instance and Kuhn type
+        const unsigned code = m.tetCode[k];
+        const int inst = (int)(code >> 19), type = (int)((code >> 15) & 7u);
+        const int4 g = m.instGeo[inst];
+        t.ids = kuhnNodes(type, g.x + (int)(code & 0x7FFFu), g.y, g.z);
+        t.meta = type | ((code & kCodeLive) ? 8 : 0);
+        t.alpha = m.instAlpha[6 * inst + type];
+    } else {
+        t.meta = m.tetMeta[k];
+        t.ids = m.tetIds[k];
+        t.alpha = m.tetAlpha[k];
+    }
     t.ids.x = checkNode(m, t.ids.x, kSiteTet); t.ids.y = checkNode(m, t.ids.y, kSiteTet);
     t.ids.z = checkNode(m, t.ids.z, kSiteTet); t.ids.w = checkNode(m, t.ids.w, kSiteTet);
-    t.alpha = m.tetAlpha[k];
     t.q[0] = xyz(m.prev[t.ids.x]); t.q[1] = xyz(m.prev[t.ids.y]); t.q[2] = xyz(m.prev[t.ids.z]); t.q[3] = xyz(m.prev[t.ids.w]);
     return t;
 }
@@ -439,25 +480,68 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
         posRef<Dsm>(m, id[c]) = make_float4(o.x, o.y, o.z, w[c]);
     }
 }
-template <bool Dsm = false>
+template <bool Dsm = false, bool Codes = false>
 __device__ __forceinline__ void projectTet(const DeviceMesh& m, int k, const FrameCoeffs& fc, bool guardedForm = false) {
-    applyTet<Dsm>(m, loadTet(m, k), fc, guardedForm);
+    applyTet<Dsm>(m, loadTet<Codes>(m, k), fc, guardedForm);
 }
 
 // Liveness of one colour-ordered element from the live topology, k_RefreshLiveness
 // (xpbd_solver.cu:429-466).
+// The two nodes of edge e and whether it is live (either table form).
+template <bool Codes = false>
+__device__ __forceinline__ bool edgeNodes(const DeviceMesh& m, int e, int2& ij) {
+    if (Codes && m.edgeCode) {
+        const unsigned code = m.edgeCode[e];
+        const int4 g = m.instGeo[code >> 19];
+        const int axis = (int)((code >> 15) & 3u), n0 = g.x + (int)(code & 0x7FFFu);
+        ij = make_int2(checkNode(m, n0, kSiteEdge), checkNode(m, n0 + (axis == 0 ? 1 : axis == 1 ? g.y : g.z), kSiteEdge));
+        return (code & kCodeLive) != 0;
+    }
+    ij = make_int2(checkNode(m, m.edgeEnds[e].x, kSiteEdge), checkNode(m, m.edgeEnds[e].y, kSiteEdge));
+    return m.edgeLive[e] != 0;
+}
+template <bool Codes = false>
 __device__ __forceinline__ void refreshEdge(const DeviceMesh& m, int e) {
+    if (Codes && m.edgeCode) {   // the link's own slot, 6 (lower end) + 2 axis + 1
+        const unsigned code = m.edgeCode[e];
+        const int4 g = m.instGeo[code >> 19];
+        const int axis = (int)((code >> 15) & 3u);
+        const int i = checkNode(m, g.x + (int)(code & 0x7FFFu), kSiteEdge);
+        const int j = checkNode(m, i + (axis == 0 ? 1 : axis == 1 ? g.y : g.z), kSiteEdge);
+        const bool live = m.nbr[checkSlot(m, 6 * i + 2 * axis + 1, kSiteEdgeSlot)] >= 0 && m.active[i] != 0 && m.active[j] != 0;
+        m.edgeCode[e] = live ? (code | kCodeLive) : (code & ~kCodeLive);
+        return;
+    }
     int2 ij = m.edgeEnds[e];
     ij.x = checkNode(m, ij.x, kSiteEdge); ij.y = checkNode(m, ij.y, kSiteEdge);
     m.edgeLive[e] = (m.nbr[checkSlot(m, m.edgeOwner[e], kSiteEdgeSlot)] >= 0 && m.active[ij.x] != 0 && m.active[ij.y] != 0) ? 1 : 0;
 }
+template <bool Codes = false>
 __device__ __forceinline__ void refreshTet(const DeviceMesh& m, int k) {
-    const int* o = m.tetOwner + 3 * k;
-    int4 d = m.tetIds[k];
+    int4 d; int o0, o1, o2;
+    unsigned code = 0;
+    if (Codes && m.tetCode) {   // the three path edges 0 -> a -> b -> 7, each owned by its lower end's +axis slot
+        code = m.tetCode[k];
+        const int type = (int)((code >> 15) & 7u);
+        const int4 g = m.instGeo[code >> 19];
+        d = kuhnNodes(type, g.x + (int)(code & 0x7FFFu), g.y, g.z);
+        const unsigned a = (unsigned)(kKuhnPath >> (6 * type)) & 7u, b = (unsigned)(kKuhnPath >> (6 * type + 3)) & 7u;
+        const unsigned s1 = a, s2 = a ^ b, s3 = b ^ 7u;   // the single-axis step of each path edge
+        auto axisOf = [](unsigned bit) { return bit == 1u ? 0 : bit == 2u ? 1 : 2; };
+        o0 = 6 * d.x + 2 * axisOf(s1) + 1; o1 = 6 * d.y + 2 * axisOf(s2) + 1; o2 = 6 * d.z + 2 * axisOf(s3) + 1;
+    } else {
+        const int* o = m.tetOwner + 3 * k;
+        d = m.tetIds[k];
+        o0 = o[0]; o1 = o[1]; o2 = o[2];
+    }
     d.x = checkNode(m, d.x, kSiteTet); d.y = checkNode(m, d.y, kSiteTet); d.z = checkNode(m, d.z, kSiteTet); d.w = checkNode(m, d.w, kSiteTet);
-    const int o0 = checkSlot(m, o[0], kSiteTetSlot), o1 = checkSlot(m, o[1], kSiteTetSlot), o2 = checkSlot(m, o[2], kSiteTetSlot);
+    o0 = checkSlot(m, o0, kSiteTetSlot); o1 = checkSlot(m, o1, kSiteTetSlot); o2 = checkSlot(m, o2, kSiteTetSlot);
     bool live = m.nbr[o0] >= 0 && m.nbr[o1] >= 0 && m.nbr[o2] >= 0 && m.active[d.x] != 0 && m.active[d.y] != 0 &&
                 m.active[d.z] != 0 && m.active[d.w] != 0;
+    if (Codes && m.tetCode) {
+        m.tetCode[k] = live ? (code | kCodeLive) : (code & ~kCodeLive);
+        return;
+    }
     int meta = m.tetMeta[k];
     m.tetMeta[k] = (meta & ~8) | (live ? 8 : 0);
 }

@@ -213,6 +213,14 @@ LCS_API int GBT_BatchSetLaunch(int mode, int threads);
 /* Times the six shapes {0/256, 1/256, 1/512, 2/2, 2/4, 2/8} and keeps the fastest; msPerFrame6 gets
  * each one's ms per frame (-1: not usable for this batch). */
 LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threadsOut, float* msPerFrame6);
+/* Element tables of the frame kernels: 1 implicit lattice codes -- 4 bytes per tet and per edge (plus
+ * the edge rest length), nodes and compliances derived from the instance's lattice strides and
+ * Kuhn type -- used by default when every instance qualifies (instances of < 32,768 nodes, fewer
+ * than 8,192 instances, one stiffness per instance and Kuhn type, ks > 0); 0 the explicit tables
+ * (node ids, flags and compliance per element).  Identical results; returns -4001 when 1 is asked
+ * of a batch that does not qualify.  GBT_BatchElementTables: the form in use (1 / 0). */
+LCS_API int GBT_BatchSetElementTables(int implicitCodes);
+LCS_API int GBT_BatchElementTables(void);
 LCS_API void GBT_BatchProfileEnable(int enabled);
 LCS_API int GBT_BatchProfileRead(float* msTotal);                      /* device ms of the profiled step calls */
 LCS_API void GBT_BatchShutdown(void);

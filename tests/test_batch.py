@@ -159,3 +159,41 @@ def test_c4_batch_instances_match_solo_oracle(gpu_lib, oracle_libs):
                 assert np.array_equal(per_instance[i][k], s.positions()), (i, k)
         finally:
             s.close()
+
+
+@pytest.mark.parametrize("mode,threads", [(0, 256), (1, 512), (2, 4)])
+def test_implicit_and_explicit_element_tables_agree(gpu_lib, small_batch, mode, threads):
+    """The implicit lattice codes (4 B per tet and edge, nodes from the instance strides and Kuhn
+    type) and the explicit element tables give the same frames bit for bit, graph replay included."""
+    runs = []
+    for implicit in (True, False):
+        with BT.TissueBatch(small_batch.grids, dt=1 / 60, substeps=small_batch.substeps, ks=1e6,
+                            stiffness_scale=small_batch.stiffness_scale(), grasp_params=GraspParams(**GRASP), dll_path=gpu_lib) as b:
+            assert b.element_tables() == "implicit"      # the default for a qualifying batch
+            b.set_element_tables(implicit)
+            assert b.element_tables() == ("implicit" if implicit else "explicit")
+            b.set_launch(mode, threads)
+            b.set_gravity(0.0, -981.0, 0.0)
+            b.set_capsules(small_batch.capsules_at(0))
+            frames = []
+            for k in range(STEPS):
+                b.step_many([small_batch.capsules_at(k + 1)], use_graph=k % 2 == 0)
+                frames.append(b.positions())
+            runs.append(frames)
+    for k in range(STEPS):
+        assert np.array_equal(runs[0][k], runs[1][k]), k
+
+
+def test_per_tet_stiffness_keeps_explicit_tables(gpu_lib):
+    """A batch with per-tet stiffness that varies inside a Kuhn type does not qualify for the codes."""
+    wl = BT.make_c4(count=3, seed=2, steps=2, size_range=((3, 5), (2, 4), (3, 5)))
+    stiff = []
+    for g in wl.grids:
+        with PlainTissue(g, dt=1 / 60, substeps=4, ks=1e6, dll_path=gpu_lib) as s:
+            mu, kappa = s.tet_stiffness()
+        mu = mu * np.linspace(0.5, 1.5, len(mu), dtype=np.float32)
+        stiff.append((mu, kappa))
+    with BT.TissueBatch(wl.grids, dt=1 / 60, substeps=4, ks=1e6, tet_stiffness=stiff, dll_path=gpu_lib) as b:
+        assert b.element_tables() == "explicit"
+        with pytest.raises(RuntimeError):
+            b.set_element_tables(True)
