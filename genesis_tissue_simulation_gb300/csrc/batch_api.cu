@@ -489,9 +489,9 @@ LCS_API int GBT_BatchInit(int count, const GbtInstanceDesc* inst, const GbtBatch
         geo[i] = make_int4(G.nodeBase[i], nx, nxy, 0);
         codes = G.nodeCount[i] < (1 << 15);
     }
-    static const int kPath[6][4] = {{0, 1, 3, 7}, {0, 3, 2, 7}, {0, 2, 6, 7}, {0, 6, 4, 7}, {0, 4, 5, 7}, {0, 5, 1, 7}};
-    auto corner = [](int c, int nx, int nxy) { return (c & 1) + ((c >> 1) & 1) * nx + ((c >> 2) & 1) * nxy; };
     if (codes) {
+        // the device decodes with kuhnNodes / kuhnOwners; the same functions must give back every
+        // tet's explicit nodes and link slots, or the batch keeps the explicit tables
         const std::vector<int>& nodeInstance = nodeInst;
         tCode.resize(tIds.size());
         for (size_t k = 0; k < tIds.size() && codes; k++) {
@@ -499,9 +499,11 @@ LCS_API int GBT_BatchInit(int count, const GbtInstanceDesc* inst, const GbtBatch
             const int i = nodeInstance[d.x], type = tMeta[k] & 7;
             const int4 g = geo[i];
             const int local = d.x - g.x;
-            const int want[4] = {d.x, d.x + corner(kPath[type][1], g.y, g.z), d.x + corner(kPath[type][2], g.y, g.z),
-                                 d.x + corner(7, g.y, g.z)};
-            codes = want[0] == d.x && want[1] == d.y && want[2] == d.z && want[3] == d.w;
+            const int4 want = kuhnNodes(type, d.x, g.y, g.z);
+            int own[3];
+            kuhnOwners(type, d.x, g.y, g.z, own);
+            codes = type < 6 && want.x == d.x && want.y == d.y && want.z == d.z && want.w == d.w &&
+                    own[0] == tOwner[3 * k] && own[1] == tOwner[3 * k + 1] && own[2] == tOwner[3 * k + 2];
             float2& st = iStiff[(size_t)6 * i + type];
             if (!seenType[(size_t)6 * i + type]) { st = tStiff[k]; seenType[(size_t)6 * i + type] = 1; }
             codes = codes && std::memcmp(&st, &tStiff[k], sizeof(float2)) == 0;

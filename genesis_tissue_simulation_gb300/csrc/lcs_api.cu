@@ -149,6 +149,9 @@ void freePhysics() {
     S.fiberLambda.release(); S.feasTarget.release(); S.needed.release(); S.incOff.release(); S.incTet.release(); S.guardFlags.release();
     S.rotA.release(); S.rotB.release(); S.rotParity = 0;
     S.volumePasses = 0; S.minVolume = 0.f;
+    // a live physics session's shutdown restores the tissue material defaults (physics.cu:218 ->
+    // xpbd_shutdown, xpbd_solver.cu:3829); a material set before the first LCS_InitPhysics stays
+    if (S.physReady) { S.tissueHardening = 80.f; S.bulkDampingSeconds = 0.003125f; }
     S.autoShape = -1; S.autoTrial = 0; S.autoMs[0] = S.autoMs[1] = S.autoMs[2] = -1.f;
     S.physReady = false; S.toolArmed = false; S.E = S.B = S.T = 0; S.lastH = -1.f;
 }

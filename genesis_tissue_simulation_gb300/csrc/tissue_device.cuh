@@ -75,13 +75,26 @@ struct DeviceMesh {
 // type t at bit 6t.
 constexpr unsigned long long kKuhnPath = (1ull | 3ull << 3) | (3ull | 2ull << 3) << 6 | (2ull | 6ull << 3) << 12 |
                                          (6ull | 4ull << 3) << 18 | (4ull | 5ull << 3) << 24 | (5ull | 1ull << 3) << 30;
-__device__ __forceinline__ int cornerOffset(unsigned corner, int nx, int nxy) {
+__host__ __device__ __forceinline__ int cornerOffset(unsigned corner, int nx, int nxy) {
     return (int)(corner & 1u) + ((corner >> 1) & 1u ? nx : 0) + ((corner >> 2) & 1u ? nxy : 0);
 }
 // The nodes of an implicit tet: corner 0 at n0, then its Kuhn path.
-__device__ __forceinline__ int4 kuhnNodes(int type, int n0, int nx, int nxy) {
+__host__ __device__ __forceinline__ int4 kuhnNodes(int type, int n0, int nx, int nxy) {
     const unsigned a = (unsigned)(kKuhnPath >> (6 * type)) & 7u, b = (unsigned)(kKuhnPath >> (6 * type + 3)) & 7u;
     return make_int4(n0, n0 + cornerOffset(a, nx, nxy), n0 + cornerOffset(b, nx, nxy), n0 + 1 + nx + nxy);
+}
+// The neighbour-table slots of an implicit tet's three lattice edges (a tet is live only while all
+// three links are), in the order mesh_build.cu lists them.  The corners of type t form the lattice
+// path 0 -> p -> q -> 7 with p one axis bit and q two; the Kuhn order visits q before p for types
+// 1, 3 and 5.  Each edge is owned by its lower end's +axis slot (6 node + 2 axis + 1).
+__host__ __device__ __forceinline__ void kuhnOwners(int type, int n0, int nx, int nxy, int o[3]) {
+    const unsigned a = (unsigned)(kKuhnPath >> (6 * type)) & 7u, b = (unsigned)(kKuhnPath >> (6 * type + 3)) & 7u;
+    const bool monotone = (a & (a - 1u)) == 0u;   // a is a single axis bit
+    const unsigned p = monotone ? a : b, q = monotone ? b : a;
+    auto axisOf = [](unsigned bit) { return bit == 1u ? 0 : bit == 2u ? 1 : 2; };
+    o[0] = 6 * n0 + 2 * axisOf(p) + 1;
+    o[1] = 6 * (n0 + cornerOffset(p, nx, nxy)) + 2 * axisOf(p ^ q) + 1;
+    o[2] = 6 * (n0 + cornerOffset(q, nx, nxy)) + 2 * axisOf(q ^ 7u) + 1;
 }
 constexpr unsigned kCodeLive = 1u << 18;
 
@@ -520,15 +533,15 @@ template <bool Codes = false>
 __device__ __forceinline__ void refreshTet(const DeviceMesh& m, int k) {
     int4 d; int o0, o1, o2;
     unsigned code = 0;
-    if (Codes && m.tetCode) {   // the three path edges 0 -> a -> b -> 7, each owned by its lower end's +axis slot
+    if (Codes && m.tetCode) {   // the three lattice edges of the tet's Kuhn path
         code = m.tetCode[k];
         const int type = (int)((code >> 15) & 7u);
         const int4 g = m.instGeo[code >> 19];
-        d = kuhnNodes(type, g.x + (int)(code & 0x7FFFu), g.y, g.z);
-        const unsigned a = (unsigned)(kKuhnPath >> (6 * type)) & 7u, b = (unsigned)(kKuhnPath >> (6 * type + 3)) & 7u;
-        const unsigned s1 = a, s2 = a ^ b, s3 = b ^ 7u;   // the single-axis step of each path edge
-        auto axisOf = [](unsigned bit) { return bit == 1u ? 0 : bit == 2u ? 1 : 2; };
-        o0 = 6 * d.x + 2 * axisOf(s1) + 1; o1 = 6 * d.y + 2 * axisOf(s2) + 1; o2 = 6 * d.z + 2 * axisOf(s3) + 1;
+        const int n0 = g.x + (int)(code & 0x7FFFu);
+        d = kuhnNodes(type, n0, g.y, g.z);
+        int o[3];
+        kuhnOwners(type, n0, g.y, g.z, o);
+        o0 = o[0]; o1 = o[1]; o2 = o[2];
     } else {
         const int* o = m.tetOwner + 3 * k;
         d = m.tetIds[k];

@@ -251,6 +251,9 @@ static void bucket(const std::vector<int>& colour, int numColours, std::vector<i
 }
 
 static void resetPhysics() {
+    // a live physics session's shutdown restores the tissue material defaults (physics.cu:218 ->
+    // xpbd_shutdown, xpbd_solver.cu:3829); a material set before the first LCS_InitPhysics stays
+    if (S.physReady) { S.tissueHardening = 80.f; S.bulkDampingSeconds = 0.003125f; }
     S.physReady = false; S.frameReady = false; S.E = S.B = S.T = 0; S.toolArmed = false; S.grasping = false;
     S.livenessStale = true; S.livenessRevision = 0xffffffffu;
     S.volumePasses = 0; S.minVolume = 0; S.incOff.clear(); S.incTet.clear(); S.h = 0;
