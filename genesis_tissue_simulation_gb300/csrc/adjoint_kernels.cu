@@ -81,7 +81,7 @@ __device__ bool substepForward(const DeviceMesh& m, const DiffCoeffs& dc, const 
         for (int c = 0; c < m.nTetColors; c++) {
             int2 rg = m.tetRange[c];
             for (int k = rg.x + r; k < rg.y; k += R) {
-                TetRecord rec = loadTet(m, k);
+                TetRecord rec = loadTet(m, k, fc);
                 if (record && (rec.meta & 8)) {
                     float4* t = b.tapeTet + 4 * ((size_t)j * (m.tetRange[m.nTetColors - 1].y) + k);
                     t[0] = m.pos[rec.ids.x]; t[1] = m.pos[rec.ids.y]; t[2] = m.pos[rec.ids.z]; t[3] = m.pos[rec.ids.w];

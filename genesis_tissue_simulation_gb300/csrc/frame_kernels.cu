@@ -483,7 +483,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         auto loadFirstTet = [&]() {
             const int2 first = m.nTetColors > 0 ? m.tetRange[0] : make_int2(0, 0);
             hasNext = first.x + r < first.y;
-            if (hasNext) next = loadTet<Codes>(m, first.x + r);
+            if (hasNext) next = loadTet<Codes>(m, first.x + r, fc);
             tetLoaded = true;
         };
         if (fc.doEdges) {
@@ -535,7 +535,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
                 bool hasCur = hasNext;
                 int2 nrg = c + 1 < m.nTetColors ? m.tetRange[c + 1] : make_int2(0, 0);
                 hasNext = nrg.x + r < nrg.y;
-                if (hasNext) next = loadTet<Codes>(m, nrg.x + r);
+                if (hasNext) next = loadTet<Codes>(m, nrg.x + r, fc);
                 if (hasCur) applyTet<Dsm>(m, cur, fc, guarded);
                 for (int k = rg.x + r + R; k < rg.y; k += R) projectTet<Dsm, Codes>(m, k, fc, guarded);
                 if (!sync.sync()) return;

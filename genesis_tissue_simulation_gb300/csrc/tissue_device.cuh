@@ -311,8 +311,12 @@ __device__ __forceinline__ EdgeRecord loadEdge(const DeviceMesh& m, int e, const
     }
     r.ij.x = checkNode(m, r.ij.x, kSiteEdge); r.ij.y = checkNode(m, r.ij.y, kSiteEdge);
     r.rest = m.edgeRest[e];
-    r.qi = xyz(m.prev[r.ij.x]);
-    r.qj = xyz(m.prev[r.ij.y]);
+    if (fc.betaGammaHS != 0.f) {   // substep-start ends: only the damping term reads them
+        r.qi = xyz(m.prev[r.ij.x]);
+        r.qj = xyz(m.prev[r.ij.y]);
+    } else {
+        r.qi = r.qj = mk(0.f, 0.f, 0.f);
+    }
     return r;
 }
 
@@ -332,8 +336,9 @@ __device__ __forceinline__ bool solveEdge(const EdgeRecord& r, const FrameCoeffs
     f3 n = d * (1.f / L);
     float C = L - r.rest;
     float gamma = fc.betaGammaHS;
-    float gradDx = dot(n, (xyz(pi) - r.qi) - (xyz(pj) - r.qj));
-    float dl = (-C - gamma * gradDx) / ((1.f + gamma) * ws + alphaTilde);
+    // undamped (gamma = 0): the damping term is a zero and its gradient is not formed
+    float num = gamma != 0.f ? -C - gamma * dot(n, (xyz(pi) - r.qi) - (xyz(pj) - r.qj)) : -C;
+    float dl = num / ((1.f + gamma) * ws + alphaTilde);
     float ap = fc.omega * dl;
     f3 a = xyz(pi) + n * (wi * ap);
     f3 b = xyz(pj) - n * (wj * ap);
@@ -397,8 +402,13 @@ __device__ __forceinline__ void projectBend(const DeviceMesh& m, int e, const Fr
 // substep-start positions of its nodes.  Loading it ahead (before the barrier of the preceding
 // colour) takes two dependent L2 round trips off each colour's critical path.
 struct TetRecord { int4 ids; int meta; float2 alpha; f3 q[4]; };
+// Whether the tet projection has a damping term (Kelvin-Voigt strain damping, or the guarded
+// form's bulk damping); without one the substep-start positions are neither loaded nor used.
+__device__ __forceinline__ bool tetDamped(const FrameCoeffs& fc, bool guarded) {
+    return fc.dampingOverH != 0.f || (guarded && fc.bulkDampingOverH != 0.f);
+}
 template <bool Codes = false>
-__device__ __forceinline__ TetRecord loadTet(const DeviceMesh& m, int k) {
+__device__ __forceinline__ TetRecord loadTet(const DeviceMesh& m, int k, const FrameCoeffs& fc) {
     TetRecord t;
     if (Codes && m.tetCode) {   // implicit lattice: nodes from the code, compliances per instance and Kuhn type
         const unsigned code = m.tetCode[k];
@@ -414,7 +424,11 @@ __device__ __forceinline__ TetRecord loadTet(const DeviceMesh& m, int k) {
     }
     t.ids.x = checkNode(m, t.ids.x, kSiteTet); t.ids.y = checkNode(m, t.ids.y, kSiteTet);
     t.ids.z = checkNode(m, t.ids.z, kSiteTet); t.ids.w = checkNode(m, t.ids.w, kSiteTet);
-    t.q[0] = xyz(m.prev[t.ids.x]); t.q[1] = xyz(m.prev[t.ids.y]); t.q[2] = xyz(m.prev[t.ids.z]); t.q[3] = xyz(m.prev[t.ids.w]);
+    if (tetDamped(fc, fc.guarded != 0)) {
+        t.q[0] = xyz(m.prev[t.ids.x]); t.q[1] = xyz(m.prev[t.ids.y]); t.q[2] = xyz(m.prev[t.ids.z]); t.q[3] = xyz(m.prev[t.ids.w]);
+    } else {
+        t.q[0] = t.q[1] = t.q[2] = t.q[3] = mk(0.f, 0.f, 0.f);
+    }
     return t;
 }
 
@@ -456,15 +470,19 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
     }
     gd[0] = (gd[1] + gd[2] + gd[3]) * -1.f;
     gh[0] = (gh[1] + gh[2] + gh[3]) * -1.f;
+    // undamped: the velocity terms vd, vh enter multiplied by zero and are not formed
+    const bool damped = tetDamped(fc, guarded);
     float dd = 0.f, dh = 0.f, vd = 0.f, vh = 0.f, w[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         w[c] = P[c].w;
         dd += w[c] * dot(gd[c], gd[c]);
         dh += w[c] * dot(gd[c], gh[c]);
-        f3 dx = p[c] - t.q[c];
-        vd += dot(gd[c], dx);
-        vh += dot(gh[c], dx);
+        if (damped) {
+            f3 dx = p[c] - t.q[c];
+            vd += dot(gd[c], dx);
+            vh += dot(gh[c], dx);
+        }
     }
     // 1 / (1 + D/h) is a frame constant; one reciprocal of A serves gamma and dlD
     float bulkScale = guarded ? 1.f + fc.bulkDampingOverH : 1.f + fc.dampingOverH;
@@ -474,8 +492,8 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
     float schur = eAh + eAd * gamma * gamma;
 #pragma unroll
     for (int c = 0; c < 4; c++) { f3 r = gh[c] - gd[c] * gamma; schur += w[c] * dot(r, r); }
-    float rd = (-CD - fc.dampingOverH * vd) * invScale;
-    float rh = (-CH - (bulkScale - 1.f) * vh) * invBulk;
+    float rd = damped ? (-CD - fc.dampingOverH * vd) * invScale : -CD * invScale;
+    float rh = damped ? (-CH - (bulkScale - 1.f) * vh) * invBulk : -CH * invBulk;
     if (!(A > 0.f) || !(schur > 0.f)) return;
     float dlH = fc.omega * (rh - gamma * rd) / schur, dlD = (fc.omega * rd - Bc * dlH) * invA;
     if (!isfinite(dlD) || !isfinite(dlH)) return;
@@ -495,7 +513,7 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
 }
 template <bool Dsm = false, bool Codes = false>
 __device__ __forceinline__ void projectTet(const DeviceMesh& m, int k, const FrameCoeffs& fc, bool guardedForm = false) {
-    applyTet<Dsm>(m, loadTet<Codes>(m, k), fc, guardedForm);
+    applyTet<Dsm>(m, loadTet<Codes>(m, k, fc), fc, guardedForm);
 }
 
 // Liveness of one colour-ordered element from the live topology, k_RefreshLiveness

@@ -642,8 +642,14 @@ static void projectEdge(int e, Real alphaTilde, Real gamma, bool fallback, Real 
     if (L < Real(1e-9)) return;
     V3 n = d * (Real(1) / L);
     Real C = L - S.eRest[e];
+#ifdef ORACLE_AS_WRITTEN
     Real gradDx = dot(n, (S.pos[i] - S.prev[i]) - (S.pos[j] - S.prev[j]));
     Real dl = (-C - gamma * gradDx) / ((Real(1) + gamma) * ws + alphaTilde);
+#else
+    // the library's form: without edge damping (gamma = 0) the damping term is a zero and is not formed
+    Real num = gamma != Real(0) ? -C - gamma * dot(n, (S.pos[i] - S.prev[i]) - (S.pos[j] - S.prev[j])) : -C;
+    Real dl = num / ((Real(1) + gamma) * ws + alphaTilde);
+#endif
     Real ap = S.omega * dl;
     S.pos[i] = S.pos[i] + n * (wi * ap);
     S.pos[j] = S.pos[j] - n * (wj * ap);
@@ -717,12 +723,21 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
     }
     gd[0] = (gd[1] + gd[2] + gd[3]) * Real(-1);
     gh[0] = (gh[1] + gh[2] + gh[3]) * Real(-1);
+#ifdef ORACLE_AS_WRITTEN
+    const bool damped = true;
+#else
+    // the library's form: without strain (or guarded bulk) damping vd, vh enter multiplied by zero
+    // and are not formed
+    const bool damped = dampingOverH != Real(0) || (guarded && bulkDampingOverH != Real(0));
+#endif
     Real dd = 0, dh = 0, hh = 0, vd = 0, vh = 0, w[4];
     for (int k = 0; k < 4; k++) {
         w[k] = S.invMass[id[k]];
         dd += w[k] * dot(gd[k], gd[k]); dh += w[k] * dot(gd[k], gh[k]); hh += w[k] * dot(gh[k], gh[k]);
-        V3 dx = p[k] - S.prev[id[k]];
-        vd += dot(gd[k], dx); vh += dot(gh[k], dx);
+        if (damped) {
+            V3 dx = p[k] - S.prev[id[k]];
+            vd += dot(gd[k], dx); vh += dot(gh[k], dx);
+        }
     }
     (void)hh;
     Real scale = Real(1) + dampingOverH, bulkScale = guarded ? Real(1) + bulkDampingOverH : scale;
@@ -743,8 +758,8 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
     Real A = dd + eAd, invA = Real(1) / A, Bc = dh, gamma = Bc * invA;
     Real schur = eAh + eAd * gamma * gamma;
     for (int k = 0; k < 4; k++) { V3 r = gh[k] - gd[k] * gamma; schur += w[k] * dot(r, r); }
-    Real rd = (-CD - dampingOverH * vd) * invScale;
-    Real rh = (-CH - (bulkScale - Real(1)) * vh) * invBulk;
+    Real rd = damped ? (-CD - dampingOverH * vd) * invScale : -CD * invScale;
+    Real rh = damped ? (-CH - (bulkScale - Real(1)) * vh) * invBulk : -CH * invBulk;
     if (!(A > 0) || !(schur > 0)) return;
     Real dlH = S.omega * (rh - gamma * rd) / schur, dlD = (S.omega * rd - Bc * dlH) * invA;
 #endif
