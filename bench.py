@@ -589,6 +589,61 @@ def frames_measurement(lib, calls=50, warmup=3):
             "nodes_per_s": nodes / (ms / 1e3), "timing": f"wall clock around GBT_ComputeParticleFrames, median of {calls}"}
 
 
+def cut_topology_measurement(lib, frames=30, calls=10, warmup=2):
+    """The cut topology of the C3 lattice after `frames` blade frames (GBT_CutTopologyBuild: live
+    tets, vertex duplication, greedy re-colouring relaxed on the device): wall clock per build
+    (launches + the copies of its counts), median.  Returns the section and the neighbour table it
+    was built from (the CPU baseline leg times the oracle on the same table)."""
+    import ctypes
+
+    from genesis_tissue_simulation_gb300 import workloads as W
+
+    w = W.make("c3", steps=frames)
+    s = w.open(lib)
+    counts = np.zeros(4, dtype=np.int32)
+    try:
+        w.run(s, steps=frames)
+        times = []
+        for k in range(calls + warmup):
+            t0 = time.perf_counter()
+            s.check("GBT_CutTopologyBuild", counts.ctypes.data_as(ctypes.c_void_p))
+            if k >= warmup:
+                times.append(time.perf_counter() - t0)
+        nbr = s.neighbors()
+    finally:
+        s.close()
+    out = {"workload": f"c3 blade workload after {frames} frames, {len(w.grid.positions):,} lattice nodes",
+           "ms_per_build_wall": 1e3 * float(np.median(times)), "live_tets": int(counts[0]), "duplicated_vertices": int(counts[1]),
+           "colours": int(counts[2]), "relaxation_sweeps": int(counts[3]),
+           "timing": f"wall clock around GBT_CutTopologyBuild, median of {calls}"}
+    return out, nbr
+
+
+def cut_topology_cpu_sample(nbr, frames=30):
+    """CPU baseline of the cut topology: the sequential oracle builds the same product from the same
+    neighbour table (one host core)."""
+    import ctypes
+
+    from genesis_tissue_simulation_gb300 import workloads as W
+
+    w = W.make("c3", steps=frames)
+    o = w.open(str(ROOT / "oracle" / "_build" / "liboracle_f32.so"))
+    try:
+        f = o.dll.GBT_SetState
+        f.argtypes = (ctypes.c_void_p,) * 8 + (ctypes.c_int, ctypes.c_uint)
+        nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+        assert f(None, None, nbr.ctypes.data_as(ctypes.c_void_p), None, None, None, None, None, 0, 0) == 0
+        counts = np.zeros(4, dtype=np.int32)
+        t0 = time.perf_counter()
+        o.check("GBT_CutTopologyBuild", counts.ctypes.data_as(ctypes.c_void_p))
+        ms = 1e3 * (time.perf_counter() - t0)
+    finally:
+        o.close()
+    return {"value": ms, "unit": "ms per build", "cores": 1, "kind": "port",
+            "sample": f"one build of the c3 lattice's cut topology after {frames} blade frames",
+            "live_tets": int(counts[0]), "duplicated_vertices": int(counts[1]), "colours": int(counts[2])}
+
+
 def main():
     parser = argparse.ArgumentParser()
     parser.add_argument("--gpus", type=int, default=1)
@@ -600,7 +655,7 @@ def main():
     parser.add_argument("--no-batched", action="store_true")
     parser.add_argument("--no-adjoint", action="store_true")
     parser.add_argument("--no-workloads", action="store_true", help="skip the C1 and C3 lines")
-    parser.add_argument("--only", default="all", choices=("all", "batched", "adjoint", "finalize", "frames", "c1", "c3"),
+    parser.add_argument("--only", default="all", choices=("all", "batched", "adjoint", "finalize", "frames", "c1", "c3", "cut_topology"),
                         help="run one section alone and print its JSON object (for profiling)")
     parser.add_argument("--batched-frames", type=int, default=20)
     parser.add_argument("--launch-mode", type=int, default=0, choices=(0, 1, 2, 3),
@@ -629,6 +684,7 @@ def main():
         section = (batched_measurement(lib, args.batched_frames, max(args.warmup, 3)) if args.only == "batched"
                    else finalize_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1)) if args.only == "finalize"
                    else frames_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1)) if args.only == "frames"
+                   else cut_topology_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1))[0] if args.only == "cut_topology"
                    else workload_measurement(lib, args.only, max(args.steps, 1), args.warmup, cpu_budget_s=0.0,
                                              launch_mode=args.launch_mode) if args.only in ("c1", "c3")
                    else adjoint_measurement(lib, reps=max(args.steps, 1)))
@@ -732,11 +788,14 @@ def main():
         line["adjoint"] = adjoint_measurement(lib)
     if not args.no_workloads:
         line["finalize"] = finalize_measurement(lib)
+        line["cut_topology"], cut_nbr = cut_topology_measurement(lib)
     if batched is not None:
         batched["roofline"].update(peak=peak, frac=batched["roofline"]["achieved"] / peak, peak_kind=peak_kind)
         line["batched"] = batched
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(args.workload)
+        if not args.no_workloads:
+            line["cpu_baseline"]["cut_topology"] = cut_topology_cpu_sample(cut_nbr)
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

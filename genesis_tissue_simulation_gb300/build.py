@@ -26,7 +26,7 @@ LIBRARY = BUILD / "libgbtissue.so"
 DEBUG_BUILD = CSRC / "_build_debug"
 DEBUG_LIBRARY = DEBUG_BUILD / "libgbtissue_debug.so"
 SOURCES = ("frame_kernels.cu", "lcs_api.cu", "mesh_build.cu", "batch_api.cu", "adjoint_kernels.cu", "adjoint_api.cu",
-           "surface_kernels.cu")
+           "surface_kernels.cu", "cut_topology.cu")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -1,0 +1,419 @@
+// Cut topology of the live mesh: vertex duplication and greedy re-colouring on the device.
+//
+// A product of this library with no counterpart in the reference.  The reference's cut severs
+// lattice links (V/cut.cu:719-746); a tet with a severed axis edge or an inactive corner stops
+// being projected (k_RefreshLiveness, xpbd_solver.cu:429-466), so crossed tets are removed, and the
+// colouring stays the one built at bind time (xpbd_solver.cu:1738-1780).  GBT_CutTopologyBuild
+// turns the current topology into an unstructured tet mesh a consumer can take as it is:
+//
+//   live tets      those the liveness rule keeps, in emission order (corner-0 node ascending, then
+//                  Kuhn type: the order the reference colours in), addressed by key = 6 node + type;
+//   duplication    around every node its live tets are grouped by shared faces through the node
+//                  (joined when they share the node and two more); groups are ranked by their first
+//                  tet, the first keeps the node, group j >= 1 becomes vertex N + base(node) + j - 1
+//                  with base the exclusive prefix sum of (groups - 1) in node order;
+//   re-colouring   the reference's greedy first-fit colouring re-run on the live tets over the
+//                  duplicated vertices: in emission order each tet takes the smallest colour that no
+//                  earlier tet sharing one of its vertices holds.  This is computed in parallel as
+//                  the fixed point of c(t) = mex{c(u) : u earlier than t, u shares a vertex with t},
+//                  relaxed in place from the bind-time colours until a whole sweep changes nothing.
+//                  The recurrence has exactly one solution (induction over emission order), so the
+//                  result is the sequential colouring whatever order the sweeps ran in.  With nothing
+//                  cut it is the bind-time colouring itself.
+//
+// The CPU restatement (oracle/cut_topology_oracle.inc) computes the same product sequentially.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "../../include/gbtissue.h"
+#include "grid_sync.cuh"
+#include "session_view.h"
+
+namespace gbt {
+namespace {
+
+#define CT_CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return -(int)e_; } while (0)
+
+constexpr int kThreads = 256;
+constexpr int kMaxAround = 24;      // live tets around a lattice node: 6 + 6 (corners 0, 7) + 6 x 2
+constexpr int kMaxColours = 128;    // colour masks are two 64-bit words
+
+template <class T> struct DBuf {
+    T* p = nullptr; size_t n = 0;
+    cudaError_t ensure(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        release();
+        n = count;
+        return cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+};
+
+// Buffers live from the first build until the session ends (releaseCutTopology, called by the
+// session's shutdown); per-session tables are rebuilt when a new session appears.
+struct CutTopologyState {
+    unsigned long long generation = 0;       // session the tables below describe
+    int N = 0, T = 0, keys = 0;
+    DBuf<int> slotOfKey, storageOfSlot;      // key -> colour slot (-1: no tet); colour slot -> storage index
+    DBuf<unsigned char> colourOfSlot;        // bind-time colour of each colour slot
+    DBuf<int> liveKey, rankOfKey, groupCount, dupBase, blockSums, totals;
+    DBuf<unsigned char> groupOf;             // [keys][4]: group of the tet at each corner node
+    DBuf<int> tetNodes, tetSource, dupParent, nbrCount, nbrOff, nbrList;
+    DBuf<unsigned char> colour;
+    DBuf<unsigned> sync;                     // relaxation kernel: [0] barrier counter, [1] status, [2..4] change counters, [5] sweeps, [6] overflow
+    int live = 0, duplicates = 0, colours = 0, sweeps = 0;
+    bool built = false;
+} C;
+
+__host__ __device__ __forceinline__ int cornerPosition(int type, unsigned corner) {
+    // position of Kuhn corner `corner` in the node list of a type-`type` tet (0, a, b, 7), or -1
+    const unsigned a = (unsigned)(kKuhnPath >> (6 * type)) & 7u, b = (unsigned)(kKuhnPath >> (6 * type + 3)) & 7u;
+    return corner == 0u ? 0 : corner == a ? 1 : corner == b ? 2 : corner == 7u ? 3 : -1;
+}
+
+// ---- session tables -------------------------------------------------------------------------
+__global__ void slotTableKernel(DeviceMesh m, int T, int* slotOfKey, unsigned char* colourOfSlot) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < T; k += gridDim.x * blockDim.x) {
+        slotOfKey[6 * m.tetIds[k].x + (m.tetMeta[k] & 7)] = k;
+        int c = 0;
+        while (c + 1 < m.nTetColors && k >= m.tetRange[c].y) c++;
+        colourOfSlot[k] = (unsigned char)c;
+    }
+}
+
+// ---- liveness of every key (the k_RefreshLiveness rule on the current topology) ----------------
+__global__ void liveKeyKernel(DeviceMesh m, int keys, const int* slotOfKey, int* liveKey) {
+    for (int key = blockIdx.x * blockDim.x + threadIdx.x; key < keys; key += gridDim.x * blockDim.x) {
+        const int k = slotOfKey[key];
+        int live = 0;
+        if (k >= 0) {
+            const int4 d = m.tetIds[k];
+            const int* o = m.tetOwner + 3 * k;
+            live = m.nbr[o[0]] >= 0 && m.nbr[o[1]] >= 0 && m.nbr[o[2]] >= 0 && m.active[d.x] != 0 && m.active[d.y] != 0 &&
+                   m.active[d.z] != 0 && m.active[d.w] != 0;
+        }
+        liveKey[key] = live;
+    }
+}
+
+// ---- exclusive prefix sums (three passes: block scans, a scan of the block sums, the carries) ----
+__device__ __forceinline__ int blockExclusiveScan(int v, int* total) {
+    __shared__ int warpSums[kThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) { int y = __shfl_up_sync(0xffffffffu, x, d); if (lane >= d) x += y; }
+    if (lane == 31) warpSums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < kThreads / 32 ? warpSums[lane] : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) { int y = __shfl_up_sync(0xffffffffu, w, d); if (lane >= d) w += y; }
+        if (lane < kThreads / 32) warpSums[lane] = w;
+    }
+    __syncthreads();
+    const int before = (warp > 0 ? warpSums[warp - 1] : 0) + x - v;
+    if (total) *total = warpSums[kThreads / 32 - 1];
+    __syncthreads();
+    return before;
+}
+__global__ void scanBlocksKernel(const int* in, int* out, int n, int* blockSums) {
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    int total;
+    const int v = i < n ? in[i] : 0;
+    const int e = blockExclusiveScan(v, &total);
+    if (i < n) out[i] = e;
+    if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
+}
+__global__ void scanSumsKernel(int* blockSums, int nb, int* grandTotal) {   // one block
+    int carry = 0;
+    for (int base = 0; base < nb; base += kThreads) {
+        const int i = base + threadIdx.x;
+        int total;
+        const int v = i < nb ? blockSums[i] : 0;
+        const int e = blockExclusiveScan(v, &total);
+        if (i < nb) blockSums[i] = carry + e;
+        carry += total;
+    }
+    if (threadIdx.x == 0) *grandTotal = carry;
+}
+__global__ void addCarryKernel(int* out, int n, const int* blockSums) {
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i < n) out[i] += blockSums[blockIdx.x];
+}
+int exclusiveScan(const int* in, int* out, int n, int* total, cudaStream_t s) {
+    const int nb = (n + kThreads - 1) / kThreads;
+    CT_CK(C.blockSums.ensure(nb));
+    if (n > 0) scanBlocksKernel<<<nb, kThreads, 0, s>>>(in, out, n, C.blockSums.p);
+    scanSumsKernel<<<1, kThreads, 0, s>>>(C.blockSums.p, nb, total);
+    if (n > 0) addCarryKernel<<<nb, kThreads, 0, s>>>(out, n, C.blockSums.p);
+    CT_CK(cudaGetLastError());
+    return 0;
+}
+
+// ---- the live tets around a node ------------------------------------------------------------
+struct Around { int key[kMaxAround]; unsigned char corner[kMaxAround]; int count; };
+// Live tets holding lattice node v, in emission (key) order, with v's position in each.
+__device__ __forceinline__ void liveAround(int v, int nx, int ny, int dx, int dy, int dz, const int* liveKey, Around& a) {
+    const int nxy = nx * ny;
+    const int vx = v % nx, vy = (v / nx) % ny, vz = v / nxy;
+    a.count = 0;
+    // corner c of the cell whose corner 0 is v - offset(c); cells in decreasing c have increasing keys
+    for (int c = 7; c >= 0; c--) {
+        const int cx = vx - (c & 1), cy = vy - ((c >> 1) & 1), cz = vz - ((c >> 2) & 1);
+        if (cx < 0 || cy < 0 || cz < 0 || cx >= dx || cy >= dy || cz >= dz) continue;
+        const int u = v - cornerOffset((unsigned)c, nx, nxy);
+        for (int t = 0; t < 6; t++) {
+            const int pos = cornerPosition(t, (unsigned)c);
+            if (pos < 0 || !liveKey[6 * u + t]) continue;
+            a.key[a.count] = 6 * u + t;
+            a.corner[a.count] = (unsigned char)pos;
+            a.count++;
+        }
+    }
+}
+
+// Groups of the live tets around every node: joined through shared faces (a second and a third
+// common node), ranked by their first tet in emission order.
+__global__ void groupKernel(int N, int nx, int ny, int dx, int dy, int dz, const int* liveKey, unsigned char* groupOf, int* groupCount) {
+    const int nxy = nx * ny;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x) {
+        Around a;
+        liveAround(v, nx, ny, dx, dy, dz, liveKey, a);
+        int4 nodes[kMaxAround];
+        unsigned char parent[kMaxAround];
+        for (int i = 0; i < a.count; i++) {
+            nodes[i] = kuhnNodes(a.key[i] % 6, a.key[i] / 6, nx, nxy);
+            parent[i] = (unsigned char)i;
+        }
+        auto find = [&](int i) { while (parent[i] != i) i = parent[i]; return i; };
+        for (int i = 0; i < a.count; i++)
+            for (int j = i + 1; j < a.count; j++) {
+                const int4 p = nodes[i], q = nodes[j];
+                const int common = (p.x == q.x) + (p.x == q.y) + (p.x == q.z) + (p.x == q.w) + (p.y == q.x) + (p.y == q.y) +
+                                   (p.y == q.z) + (p.y == q.w) + (p.z == q.x) + (p.z == q.y) + (p.z == q.z) + (p.z == q.w) +
+                                   (p.w == q.x) + (p.w == q.y) + (p.w == q.z) + (p.w == q.w);
+                if (common < 3) continue;
+                const int ri = find(i), rj = find(j);
+                if (ri != rj) parent[max(ri, rj)] = (unsigned char)min(ri, rj);   // a root is its group's first member
+            }
+        unsigned char label[kMaxAround];
+        int groups = 0;
+        for (int i = 0; i < a.count; i++) {
+            const int root = find(i);
+            label[i] = root == i ? (unsigned char)groups++ : label[root];
+            groupOf[4 * (size_t)a.key[i] + a.corner[i]] = label[i];
+        }
+        groupCount[v] = groups > 1 ? groups - 1 : 0;
+    }
+}
+
+// ---- the live tets in emission order over the duplicated vertices -----------------------------
+__device__ __forceinline__ int vertexOf(int node, int group, int N, const int* dupBase) {
+    return group == 0 ? node : N + dupBase[node] + group - 1;
+}
+__global__ void emitKernel(int keys, int N, int nx, int nxy, const int* liveKey, const int* rankOfKey, const int* slotOfKey,
+                           const int* storageOfSlot, const unsigned char* colourOfSlot, const unsigned char* groupOf,
+                           const int* dupBase, int* tetNodes, int* tetSource, unsigned char* colour) {
+    for (int key = blockIdx.x * blockDim.x + threadIdx.x; key < keys; key += gridDim.x * blockDim.x) {
+        if (!liveKey[key]) continue;
+        const int r = rankOfKey[key], slot = slotOfKey[key];
+        const int4 d = kuhnNodes(key % 6, key / 6, nx, nxy);
+        const int node[4] = {d.x, d.y, d.z, d.w};
+        for (int k = 0; k < 4; k++) tetNodes[4 * (size_t)r + k] = vertexOf(node[k], groupOf[4 * (size_t)key + k], N, dupBase);
+        tetSource[r] = storageOfSlot[slot];
+        colour[r] = colourOfSlot[slot];   // the relaxation starts from the bind-time colouring
+    }
+}
+__global__ void dupParentKernel(int N, const int* groupCount, const int* dupBase, int* dupParent) {
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x)
+        for (int j = 0; j < groupCount[v]; j++) dupParent[dupBase[v] + j] = v;
+}
+
+// Earlier live tets sharing a vertex with the tet of `key` (rank r): around each of its corners,
+// the tets of the same group.  Pass 1 counts (nbrOff == nullptr), pass 2 writes ranks at nbrOff[r].
+__global__ void neighbourKernel(int keys, int nx, int ny, int dx, int dy, int dz, const int* liveKey, const int* rankOfKey,
+                                const unsigned char* groupOf, int* nbrCount, const int* nbrOff, int* nbrList) {
+    const int nxy = nx * ny;
+    for (int key = blockIdx.x * blockDim.x + threadIdx.x; key < keys; key += gridDim.x * blockDim.x) {
+        if (!liveKey[key]) continue;
+        const int r = rankOfKey[key];
+        const int4 d = kuhnNodes(key % 6, key / 6, nx, nxy);
+        const int node[4] = {d.x, d.y, d.z, d.w};
+        int found[4 * kMaxAround];
+        int count = 0;
+        for (int k = 0; k < 4; k++) {
+            const unsigned char g = groupOf[4 * (size_t)key + k];
+            Around a;
+            liveAround(node[k], nx, ny, dx, dy, dz, liveKey, a);
+            for (int i = 0; i < a.count; i++) {
+                if (a.key[i] >= key || groupOf[4 * (size_t)a.key[i] + a.corner[i]] != g) continue;
+                const int u = rankOfKey[a.key[i]];
+                bool seen = false;
+                for (int q = 0; q < count && !seen; q++) seen = found[q] == u;
+                if (!seen) found[count++] = u;
+            }
+        }
+        if (!nbrOff) { nbrCount[r] = count; continue; }
+        int* out = nbrList + nbrOff[r];
+        for (int q = 0; q < count; q++) out[q] = found[q];
+    }
+}
+
+// In-place relaxation of c(t) = mex{c(u) : u in t's earlier neighbours} over the whole grid, one
+// sweep per grid barrier, until a sweep changes nothing.  Change counters rotate over three words:
+// sweep s counts into word s % 3, every block reads it after the sweep's barrier, and block 0
+// clears word (s + 1) % 3 during sweep s (its last reader finished before the previous barrier).
+__global__ void __launch_bounds__(kThreads) recolourKernel(int L, const int* nbrOff, const int* nbrList, unsigned char* colour,
+                                                          unsigned* sync, long long budget, int maxSweeps) {
+    GridSync g{sync, sync + 1, gridDim.x, 0u, budget, 0u};
+    const int R = gridDim.x * blockDim.x, r0 = blockIdx.x * blockDim.x + threadIdx.x;
+    volatile unsigned char* col = colour;
+    for (int s = 0; s < maxSweeps; s++) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) sync[2 + (s + 1) % 3] = 0u;
+        bool changed = false;
+        for (int t = r0; t < L; t += R) {
+            unsigned long long m0 = 0ull, m1 = 0ull;
+            for (int j = nbrOff[t]; j < nbrOff[t + 1]; j++) {
+                const unsigned c = col[nbrList[j]];
+                if (c < 64u) m0 |= 1ull << c; else m1 |= 1ull << (c - 64u);
+            }
+            const int mex = ~m0 ? __ffsll((long long)~m0) - 1 : (~m1 ? 64 + __ffsll((long long)~m1) - 1 : kMaxColours);
+            if (mex >= kMaxColours) { atomicOr(sync + 6, 1u); continue; }
+            if (mex != col[t]) { col[t] = (unsigned char)mex; changed = true; }
+        }
+        if (__syncthreads_or(changed) && threadIdx.x == 0) atomicAdd(sync + 2 + s % 3, 1u);
+        if (!g.sync()) return;
+        const unsigned any = *(volatile unsigned*)(sync + 2 + s % 3);
+        if (any == 0u || *(volatile unsigned*)(sync + 6) != 0u) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) sync[5] = (unsigned)(s + 1);
+            return;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) sync[5] = (unsigned)(maxSweeps + 1);   // not settled (cannot happen: maxSweeps > L)
+}
+
+int readTotal(int* dst, cudaStream_t s) {
+    CT_CK(cudaMemcpyAsync(dst, C.totals.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CT_CK(cudaStreamSynchronize(s));
+    return 0;
+}
+
+int build(const SessionView& v) {
+    const DeviceMesh& m = v.mesh;
+    const cudaStream_t s = v.stream;
+    const int N = v.N, T = v.T, keys = 6 * N;
+    const int nx = m.dx + 1, ny = m.dy + 1;
+    auto blocks = [&](long long n) { return (int)std::max(1LL, std::min<long long>((n + kThreads - 1) / kThreads, 16LL * v.smCount)); };
+    if (C.generation != v.generation || C.N != N || C.T != T) {   // per-session tables
+        C.built = false;
+        CT_CK(C.slotOfKey.ensure(keys)); CT_CK(C.colourOfSlot.ensure(T)); CT_CK(C.storageOfSlot.ensure(T));
+        CT_CK(cudaMemsetAsync(C.slotOfKey.p, 0xFF, (size_t)keys * sizeof(int), s));
+        CT_CK(cudaMemcpyAsync(C.storageOfSlot.p, v.tetColorOrder, (size_t)T * sizeof(int), cudaMemcpyHostToDevice, s));
+        if (T > 0) slotTableKernel<<<blocks(T), kThreads, 0, s>>>(m, T, C.slotOfKey.p, C.colourOfSlot.p);
+        CT_CK(cudaGetLastError());
+        CT_CK(cudaStreamSynchronize(s));   // the host table copied above is the session's, valid now
+        C.generation = v.generation; C.N = N; C.T = T; C.keys = keys;
+    }
+    CT_CK(C.liveKey.ensure(keys)); CT_CK(C.rankOfKey.ensure(keys)); CT_CK(C.groupOf.ensure((size_t)4 * keys));
+    CT_CK(C.groupCount.ensure(N)); CT_CK(C.dupBase.ensure(N)); CT_CK(C.totals.ensure(1)); CT_CK(C.sync.ensure(8));
+    liveKeyKernel<<<blocks(keys), kThreads, 0, s>>>(m, keys, C.slotOfKey.p, C.liveKey.p);
+    CT_CK(cudaGetLastError());
+    int rc = exclusiveScan(C.liveKey.p, C.rankOfKey.p, keys, C.totals.p, s);
+    if (rc) return rc;
+    int L = 0, D = 0, E = 0;
+    if ((rc = readTotal(&L, s))) return rc;
+    groupKernel<<<blocks(N), kThreads, 0, s>>>(N, nx, ny, m.dx, m.dy, m.dz, C.liveKey.p, C.groupOf.p, C.groupCount.p);
+    CT_CK(cudaGetLastError());
+    if ((rc = exclusiveScan(C.groupCount.p, C.dupBase.p, N, C.totals.p, s))) return rc;
+    if ((rc = readTotal(&D, s))) return rc;
+    CT_CK(C.tetNodes.ensure((size_t)4 * L)); CT_CK(C.tetSource.ensure(L)); CT_CK(C.colour.ensure(L)); CT_CK(C.dupParent.ensure(D));
+    CT_CK(C.nbrCount.ensure(L)); CT_CK(C.nbrOff.ensure((size_t)L + 1));
+    emitKernel<<<blocks(keys), kThreads, 0, s>>>(keys, N, nx, nx * ny, C.liveKey.p, C.rankOfKey.p, C.slotOfKey.p, C.storageOfSlot.p,
+                                                  C.colourOfSlot.p, C.groupOf.p, C.dupBase.p, C.tetNodes.p, C.tetSource.p, C.colour.p);
+    dupParentKernel<<<blocks(N), kThreads, 0, s>>>(N, C.groupCount.p, C.dupBase.p, C.dupParent.p);
+    neighbourKernel<<<blocks(keys), kThreads, 0, s>>>(keys, nx, ny, m.dx, m.dy, m.dz, C.liveKey.p, C.rankOfKey.p, C.groupOf.p,
+                                                       C.nbrCount.p, nullptr, nullptr);
+    CT_CK(cudaGetLastError());
+    if ((rc = exclusiveScan(C.nbrCount.p, C.nbrOff.p, L, C.totals.p, s))) return rc;
+    if ((rc = readTotal(&E, s))) return rc;
+    CT_CK(cudaMemcpyAsync(C.nbrOff.p + L, &E, sizeof(int), cudaMemcpyHostToDevice, s));
+    CT_CK(C.nbrList.ensure(E));
+    neighbourKernel<<<blocks(keys), kThreads, 0, s>>>(keys, nx, ny, m.dx, m.dy, m.dz, C.liveKey.p, C.rankOfKey.p, C.groupOf.p,
+                                                       C.nbrCount.p, C.nbrOff.p, C.nbrList.p);
+    CT_CK(cudaGetLastError());
+    unsigned sweeps = 0, overflow = 0;
+    if (L > 0) {
+        CT_CK(cudaMemsetAsync(C.sync.p, 0, 8 * sizeof(unsigned), s));
+        int perSm = 0;
+        CT_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, recolourKernel, kThreads, 0));
+        const int grid = std::max(1, std::min(perSm * v.smCount, (L + kThreads - 1) / kThreads));
+        long long budget = (long long)(v.syncBudgetSeconds * 1e3 * (double)v.clockKHz);
+        int Lk = L, maxSweeps = L + 1;
+        const int* off = C.nbrOff.p; const int* list = C.nbrList.p; unsigned char* col = C.colour.p; unsigned* sy = C.sync.p;
+        void* args[] = {&Lk, &off, &list, &col, &sy, &budget, &maxSweeps};
+        CT_CK(cudaLaunchCooperativeKernel((const void*)recolourKernel, dim3(grid), dim3(kThreads), args, 0, s));
+        unsigned h[8];
+        CT_CK(cudaMemcpyAsync(h, C.sync.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+        CT_CK(cudaStreamSynchronize(s));
+        if (h[1] != 0u) return LCS_ERR_DEVICE_TIMEOUT;
+        sweeps = h[5]; overflow = h[6];
+        if (overflow || sweeps > (unsigned)L + 1u) return XPBD_ERR_COLOR_OVERFLOW;
+    }
+    // colour count: the largest colour + 1 (read back with the colours by the getter)
+    std::vector<unsigned char> host(L);
+    if (L > 0) {
+        CT_CK(cudaMemcpyAsync(host.data(), C.colour.p, (size_t)L, cudaMemcpyDeviceToHost, s));
+        CT_CK(cudaStreamSynchronize(s));
+    }
+    int colours = 0;
+    for (unsigned char c : host) colours = std::max(colours, (int)c + 1);
+    C.live = L; C.duplicates = D; C.colours = colours; C.sweeps = (int)sweeps; C.built = true;
+    return 0;
+}
+
+}  // namespace
+
+void releaseCutTopology() {
+    for (auto* b : {&C.slotOfKey, &C.storageOfSlot, &C.liveKey, &C.rankOfKey, &C.groupCount, &C.dupBase, &C.blockSums, &C.totals,
+                    &C.tetNodes, &C.tetSource, &C.dupParent, &C.nbrCount, &C.nbrOff, &C.nbrList}) b->release();
+    C.colourOfSlot.release(); C.groupOf.release(); C.colour.release(); C.sync.release();
+    C.generation = 0; C.built = false; C.live = C.duplicates = C.colours = C.sweeps = 0;
+}
+
+}  // namespace gbt
+
+using namespace gbt;
+
+LCS_API int GBT_CutTopologyBuild(int* counts4) {
+    if (!counts4) return XPBD_ERR_BAD_ARG;
+    SessionView v{};
+    int rc = sessionView(&v);
+    if (rc) return rc;
+    C.built = false;
+    rc = build(v);
+    if (rc) return rc;
+    counts4[0] = C.live; counts4[1] = C.duplicates; counts4[2] = C.colours; counts4[3] = C.sweeps;
+    return 0;
+}
+
+LCS_API int GBT_GetCutTopology(int* tetNodes4L, int* tetSourceL, int* tetColourL, int* dupParentD) {
+    SessionView v{};
+    int rc = sessionView(&v);
+    if (rc) return rc;
+    if (!C.built || C.generation != v.generation) return XPBD_ERR_NOT_READY;
+    if (!tetNodes4L || !tetSourceL || !tetColourL || (C.duplicates > 0 && !dupParentD)) return XPBD_ERR_BAD_ARG;
+    const size_t L = (size_t)C.live;
+    std::vector<unsigned char> colour(L);
+    if (L > 0) {
+        CT_CK(cudaMemcpyAsync(tetNodes4L, C.tetNodes.p, 4 * L * sizeof(int), cudaMemcpyDeviceToHost, v.stream));
+        CT_CK(cudaMemcpyAsync(tetSourceL, C.tetSource.p, L * sizeof(int), cudaMemcpyDeviceToHost, v.stream));
+        CT_CK(cudaMemcpyAsync(colour.data(), C.colour.p, L, cudaMemcpyDeviceToHost, v.stream));
+    }
+    if (C.duplicates > 0)
+        CT_CK(cudaMemcpyAsync(dupParentD, C.dupParent.p, (size_t)C.duplicates * sizeof(int), cudaMemcpyDeviceToHost, v.stream));
+    CT_CK(cudaStreamSynchronize(v.stream));
+    for (size_t t = 0; t < L; t++) tetColourL[t] = colour[t];
+    return 0;
+}

@@ -141,6 +141,7 @@ void freeCut() {
 }
 void freePhysics() {
     freeCut();
+    releaseCutTopology();
     for (auto* b : {&S.prev, &S.vel, &S.ext}) b->release();
     for (auto* b : {&S.pinned, &S.active, &S.nbr, &S.edgeColorOffD, &S.bendColorOffD, &S.tetColorOffD, &S.edgeOwner, &S.edgeLive,
                     &S.bendSrc, &S.bendLive, &S.tetMeta, &S.tetOwner, &S.edgeSupport}) b->release();
@@ -1282,5 +1283,6 @@ int gbt::sessionView(SessionView* v) {
     v->cp = S.cp;
     v->tetColorOrder = S.tetColorOrder.data();
     v->state = S.state.p;
+    v->generation = S.generation;
     return 0;
 }

@@ -16,9 +16,13 @@ struct SessionView {
     ContactParams cp;
     const int* tetColorOrder;          // host [T]: colour slot -> storage index
     unsigned* state;                   // device: [0] liveness revision, [1] barrier counter, [2] status
+    unsigned long long generation;     // changes with every new physics session
 };
 
 // 0 and the view when physics is initialised, else a negative status.
 int sessionView(SessionView* v);
+
+// Frees the cut-topology product's device buffers (cut_topology.cu); called when a session ends.
+void releaseCutTopology();
 
 }  // namespace gbt

@@ -193,7 +193,7 @@ EXTENSION_SIGNATURES = (
     ("LCS_EdgeColorCount", (), I), ("LCS_EdgeCount", (), I), ("LCS_GetTetIds", (P,), I),
     ("LCS_GetTetColors", (P,), I), ("LCS_GetEdgeColors", (P,), I), ("LCS_GetVelocities", (P,), I),
     ("LCS_GetBendPairs", (P,), I), ("LCS_GetVoxelCutMask", (P,), I), ("GBT_GetParticleRot", (P,), I),
-    ("GBT_GetSurfaceTriangles", (P,), I),
+    ("GBT_GetSurfaceTriangles", (P,), I), ("GBT_CutTopologyBuild", (P,), I), ("GBT_GetCutTopology", (P, P, P, P), I),
 )
 UNIFIED_SIGNATURES = (
     ("LCS_PressureBladeAbiVersion", (), I), ("LCS_SetPressureBlade", (P,), I),
@@ -393,6 +393,25 @@ class PlainTissue(_Session):
         out = np.empty(self.tet_count, dtype=np.int32)
         self.check("LCS_GetTetColors", pointer(out))
         return out
+
+    def cut_topology(self):
+        """The cut topology of the live mesh (GBT_CutTopologyBuild, GBT_GetCutTopology; this library's
+        own product, the reference keeps a static colouring and one vertex per lattice node): the live
+        tets in emission order as vertex quadruples over the lattice nodes and their duplicates
+        (``tet_nodes`` [L, 4]), each tet's storage index (``tet_source``), its colour in the greedy
+        re-colouring (``tet_colour``), the lattice node of every duplicated vertex (``dup_parent``,
+        vertex N + j duplicates node dup_parent[j]), the colour count and, from the CUDA library, the
+        relaxation sweeps its colouring took."""
+        counts = np.zeros(4, dtype=np.int32)
+        self.check("GBT_CutTopologyBuild", pointer(counts))
+        live, dups = int(counts[0]), int(counts[1])
+        nodes = np.empty((live, 4), dtype=np.int32)
+        source = np.empty(live, dtype=np.int32)
+        colour = np.empty(live, dtype=np.int32)
+        parent = np.empty(max(dups, 1), dtype=np.int32)
+        self.check("GBT_GetCutTopology", pointer(nodes), pointer(source), pointer(colour), pointer(parent))
+        return dict(tet_nodes=nodes, tet_source=source, tet_colour=colour, dup_parent=parent[:dups],
+                    colours=int(counts[2]), sweeps=int(counts[3]))
 
     def edge_colors(self):
         out = np.empty((len(self.grid.positions), 6), dtype=np.int32)

@@ -158,6 +158,20 @@ LCS_API int LCS_GetTetColors(int* outT);         /* greedy colour of each tet, s
 LCS_API int LCS_GetEdgeColors(int* out6N);       /* colour of each lattice edge at its owner slot, else -1 */
 LCS_API int LCS_GetBendPairs(void* out);         /* the live 32-byte bend records */
 LCS_API int LCS_GetVoxelCutMask(unsigned* outV); /* cumulative 12-bit cut mask per voxel */
+/* Cut topology of the live mesh, an unstructured tet mesh built on the device from the current
+ * topology (no counterpart in the reference, whose cut severs links, V/cut.cu:719-746, and keeps the
+ * bind-time colouring, xpbd_solver.cu:1738-1780).  Live tets are those the liveness rule keeps
+ * (xpbd_solver.cu:429-466: crossed tets are removed), in emission order (corner-0 node, then Kuhn
+ * type).  Around every node the live tets are grouped by shared faces through the node; group
+ * j >= 1 of node v becomes vertex N + base(v) + j - 1 (base: exclusive prefix sum of groups - 1
+ * over nodes).  Colours: the reference's greedy first-fit colouring re-run in emission order over
+ * those vertices (with nothing cut, the bind-time colouring).
+ * GBT_CutTopologyBuild computes it and writes counts4 = {live tets L, duplicated vertices D,
+ * colours, relaxation sweeps of the colouring}; GBT_GetCutTopology copies tetNodes4L[4L] (vertex
+ * ids), tetSourceL[L] (storage index, the order of LCS_GetTetIds), tetColourL[L] and dupParentD[D]
+ * (the lattice node of vertex N + j).  -1003 (XPBD_ERR_COLOR_OVERFLOW): more than 128 colours. */
+LCS_API int GBT_CutTopologyBuild(int* counts4);
+LCS_API int GBT_GetCutTopology(int* tetNodes4L, int* tetSourceL, int* tetColourL, int* dupParentD);
 LCS_API int GBT_GetActive(int* outN);           /* physics_active (V/physics.h:69): the live active flags */
 /* Restore of the state one LCS_Step hands to the next (no LCS_ export in the reference, which keeps
  * it behind physics_vel / physics_nbr_idx / physics_bend_pairs / physics_active / physics_particle_rot,

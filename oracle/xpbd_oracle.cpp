@@ -31,6 +31,7 @@
 //     607-681 TearOverstretch, 719-746 SeverLinks, 1105-1226 init/set_tool,
 //     1235-1254 detect, 1303-1431 ribbon tick;  V/cut.cuh:113-188 lattice helpers, Moller-Trumbore
 //   V/dc_recon.cu:543-620 (recon_init: positions, rest snapshot, skin crossing fractions)
+//   cut_topology_oracle.inc: the library's cut-topology product (no reference counterpart)
 #include <algorithm>
 #include <array>
 #include <chrono>
@@ -40,6 +41,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -1470,6 +1472,9 @@ API int ORC_Threads() {
     return 1;
 #endif
 }
+
+// cut topology of the live mesh: vertex duplication and re-colouring (a feature of this library)
+#include "cut_topology_oracle.inc"
 
 // differentiable rollout and its adjoint
 #include "diff_oracle.inc"
