@@ -59,8 +59,8 @@ struct CutTopologyState {
     DBuf<unsigned char> colourOfSlot;        // bind-time colour of each colour slot
     DBuf<int> liveKey, rankOfKey, groupCount, dupBase, blockSums, totals;
     DBuf<unsigned char> groupOf;             // [keys][4]: group of the tet at each corner node
-    DBuf<int> tetNodes, tetSource, dupParent, nbrCount, nbrOff, nbrList;
-    DBuf<unsigned char> colour;
+    DBuf<int> tetNodes, tetSource, dupParent, nbrCount, nbrOff, nbrList, upCount, upOff, upList;
+    DBuf<unsigned char> colour, marks;
     DBuf<unsigned> sync;                     // relaxation kernel: [0] barrier counter, [1] status, [2..4] change counters, [5] sweeps, [6] overflow
     int live = 0, duplicates = 0, colours = 0, sweeps = 0;
     bool built = false;
@@ -261,19 +261,42 @@ __global__ void neighbourKernel(int keys, int nx, int ny, int dx, int dy, int dz
     }
 }
 
+// Later neighbours (the reverse of the earlier-neighbour lists): counts, then positions by atomic
+// cursors (their order is irrelevant: they only mark tets for re-evaluation).
+__global__ void upperCountKernel(int L, const int* nbrOff, const int* nbrList, int* upCount) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < L; t += gridDim.x * blockDim.x)
+        for (int j = nbrOff[t]; j < nbrOff[t + 1]; j++) atomicAdd(upCount + nbrList[j], 1);
+}
+__global__ void upperFillKernel(int L, const int* nbrOff, const int* nbrList, const int* upOff, int* upCursor, int* upList) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < L; t += gridDim.x * blockDim.x)
+        for (int j = nbrOff[t]; j < nbrOff[t + 1]; j++) {
+            const int u = nbrList[j];
+            upList[upOff[u] + atomicAdd(upCursor + u, 1)] = t;
+        }
+}
+
 // In-place relaxation of c(t) = mex{c(u) : u in t's earlier neighbours} over the whole grid, one
-// sweep per grid barrier, until a sweep changes nothing.  Change counters rotate over three words:
-// sweep s counts into word s % 3, every block reads it after the sweep's barrier, and block 0
-// clears word (s + 1) % 3 during sweep s (its last reader finished before the previous barrier).
-__global__ void __launch_bounds__(kThreads) recolourKernel(int L, const int* nbrOff, const int* nbrList, unsigned char* colour,
+// sweep per grid barrier, until a sweep changes nothing.  Only marked tets are evaluated: every tet
+// in the first sweep, afterwards those with an earlier neighbour that changed in the previous sweep
+// (a tet whose earlier neighbours kept their colours since it was evaluated still satisfies the
+// recurrence; a change after its evaluation marks it again).  Marks alternate between two byte
+// arrays by sweep parity.  Change counters rotate over three words: sweep s counts into word s % 3,
+// every block reads it after the sweep's barrier, and block 0 clears word (s + 1) % 3 during sweep
+// s (its last reader finished before the previous barrier).
+__global__ void __launch_bounds__(kThreads) recolourKernel(int L, const int* nbrOff, const int* nbrList, const int* upOff,
+                                                          const int* upList, unsigned char* colour, unsigned char* marks,
                                                           unsigned* sync, long long budget, int maxSweeps) {
     GridSync g{sync, sync + 1, gridDim.x, 0u, budget, 0u};
     const int R = gridDim.x * blockDim.x, r0 = blockIdx.x * blockDim.x + threadIdx.x;
     volatile unsigned char* col = colour;
     for (int s = 0; s < maxSweeps; s++) {
         if (blockIdx.x == 0 && threadIdx.x == 0) sync[2 + (s + 1) % 3] = 0u;
+        unsigned char* cur = marks + (size_t)(s & 1) * L;
+        unsigned char* next = marks + (size_t)((s + 1) & 1) * L;
         bool changed = false;
         for (int t = r0; t < L; t += R) {
+            if (!cur[t]) continue;
+            cur[t] = 0;
             unsigned long long m0 = 0ull, m1 = 0ull;
             for (int j = nbrOff[t]; j < nbrOff[t + 1]; j++) {
                 const unsigned c = col[nbrList[j]];
@@ -281,7 +304,11 @@ __global__ void __launch_bounds__(kThreads) recolourKernel(int L, const int* nbr
             }
             const int mex = ~m0 ? __ffsll((long long)~m0) - 1 : (~m1 ? 64 + __ffsll((long long)~m1) - 1 : kMaxColours);
             if (mex >= kMaxColours) { atomicOr(sync + 6, 1u); continue; }
-            if (mex != col[t]) { col[t] = (unsigned char)mex; changed = true; }
+            if (mex != col[t]) {
+                col[t] = (unsigned char)mex;
+                changed = true;
+                for (int j = upOff[t]; j < upOff[t + 1]; j++) next[upList[j]] = 1;
+            }
         }
         if (__syncthreads_or(changed) && threadIdx.x == 0) atomicAdd(sync + 2 + s % 3, 1u);
         if (!g.sync()) return;
@@ -345,14 +372,27 @@ int build(const SessionView& v) {
     CT_CK(cudaGetLastError());
     unsigned sweeps = 0, overflow = 0;
     if (L > 0) {
+        CT_CK(C.upCount.ensure(L)); CT_CK(C.upOff.ensure((size_t)L + 1)); CT_CK(C.upList.ensure(E)); CT_CK(C.marks.ensure((size_t)2 * L));
+        CT_CK(cudaMemsetAsync(C.upCount.p, 0, (size_t)L * sizeof(int), s));
+        upperCountKernel<<<blocks(L), kThreads, 0, s>>>(L, C.nbrOff.p, C.nbrList.p, C.upCount.p);
+        CT_CK(cudaGetLastError());
+        if ((rc = exclusiveScan(C.upCount.p, C.upOff.p, L, C.totals.p, s))) return rc;
+        CT_CK(cudaMemcpyAsync(C.upOff.p + L, &E, sizeof(int), cudaMemcpyHostToDevice, s));
+        CT_CK(cudaMemsetAsync(C.upCount.p, 0, (size_t)L * sizeof(int), s));   // now the fill cursors
+        upperFillKernel<<<blocks(L), kThreads, 0, s>>>(L, C.nbrOff.p, C.nbrList.p, C.upOff.p, C.upCount.p, C.upList.p);
+        CT_CK(cudaGetLastError());
+        CT_CK(cudaMemsetAsync(C.marks.p, 1, (size_t)L, s));                    // the first sweep evaluates every tet
+        CT_CK(cudaMemsetAsync(C.marks.p + L, 0, (size_t)L, s));
         CT_CK(cudaMemsetAsync(C.sync.p, 0, 8 * sizeof(unsigned), s));
         int perSm = 0;
         CT_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, recolourKernel, kThreads, 0));
-        const int grid = std::max(1, std::min(perSm * v.smCount, (L + kThreads - 1) / kThreads));
+        // two CTAs per SM: after the first sweep few tets are marked, and every CTA arrives at each barrier
+        const int grid = std::max(1, std::min(std::min(perSm, 2) * v.smCount, (L + kThreads - 1) / kThreads));
         long long budget = (long long)(v.syncBudgetSeconds * 1e3 * (double)v.clockKHz);
         int Lk = L, maxSweeps = L + 1;
-        const int* off = C.nbrOff.p; const int* list = C.nbrList.p; unsigned char* col = C.colour.p; unsigned* sy = C.sync.p;
-        void* args[] = {&Lk, &off, &list, &col, &sy, &budget, &maxSweeps};
+        const int* off = C.nbrOff.p; const int* list = C.nbrList.p; const int* uoff = C.upOff.p; const int* ulist = C.upList.p;
+        unsigned char* col = C.colour.p; unsigned char* mk = C.marks.p; unsigned* sy = C.sync.p;
+        void* args[] = {&Lk, &off, &list, &uoff, &ulist, &col, &mk, &sy, &budget, &maxSweeps};
         CT_CK(cudaLaunchCooperativeKernel((const void*)recolourKernel, dim3(grid), dim3(kThreads), args, 0, s));
         unsigned h[8];
         CT_CK(cudaMemcpyAsync(h, C.sync.p, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -377,8 +417,8 @@ int build(const SessionView& v) {
 
 void releaseCutTopology() {
     for (auto* b : {&C.slotOfKey, &C.storageOfSlot, &C.liveKey, &C.rankOfKey, &C.groupCount, &C.dupBase, &C.blockSums, &C.totals,
-                    &C.tetNodes, &C.tetSource, &C.dupParent, &C.nbrCount, &C.nbrOff, &C.nbrList}) b->release();
-    C.colourOfSlot.release(); C.groupOf.release(); C.colour.release(); C.sync.release();
+                    &C.tetNodes, &C.tetSource, &C.dupParent, &C.nbrCount, &C.nbrOff, &C.nbrList, &C.upCount, &C.upOff, &C.upList}) b->release();
+    C.colourOfSlot.release(); C.groupOf.release(); C.colour.release(); C.marks.release(); C.sync.release();
     C.generation = 0; C.built = false; C.live = C.duplicates = C.colours = C.sweeps = 0;
 }
 

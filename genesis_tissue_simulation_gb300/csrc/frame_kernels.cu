@@ -25,8 +25,18 @@ namespace gbt {
 // The substep's instrument frame (contactFrame) lives in tissue_device.cuh: batches evaluate it on
 // the host, single meshes on the device, with the same operations.
 // The contact of one mobile node (wc > 0) at p moving with the substep's predicted velocity v.
+// Warp-level early-out of the capsule test: a node outside the box of the shaft segment grown by the
+// radius (and a margin far above the rounding of the exact distance) cannot be inside the capsule,
+// where the exact test would change nothing; a warp with no node inside that box skips the test
+// (one ballot), the others run it exactly as before, so the result is the same bit for bit.
+__device__ __forceinline__ bool nearCapsule(f3 p, const ContactFrame& f) {
+    const float r = f.shaftR * 1.0001f + 1e-5f;
+    return p.x >= fminf(f.sa.x, f.sb.x) - r && p.x <= fmaxf(f.sa.x, f.sb.x) + r && p.y >= fminf(f.sa.y, f.sb.y) - r &&
+           p.y <= fmaxf(f.sa.y, f.sb.y) + r && p.z >= fminf(f.sa.z, f.sb.z) - r && p.z <= fmaxf(f.sa.z, f.sb.z) + r;
+}
 __device__ __forceinline__ f3 contactPoint(f3 p, float wc, f3 v, const ContactFrame& f, const ContactParams& cp) {
-    {
+    const bool near = nearCapsule(p, f);
+    if (__ballot_sync(__activemask(), near) != 0u && near) {
         f3 ab = f.sb - f.sa;
         float ab2 = dot(ab, ab);
         float tt = ab2 > 1e-12f ? dot(p - f.sa, ab) / ab2 : 0.f;
