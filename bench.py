@@ -51,6 +51,33 @@ def ncu_traffic_per_launch(name):
     return None
 
 
+def issue_roof(ms_per_launch, name="ncu_batch_frame_c4", schedulers=4):
+    """The instruction-issue roof of the batched frame kernel: its warp instructions per launch (from
+    the committed ncu summary) issued at one per scheduler per cycle on every SM at the maximum SM
+    clock, against the measured launch time."""
+    path = ROOT / "profiles" / f"{name}.md"
+    instructions = None
+    if path.exists():
+        for line in path.read_text().splitlines():
+            if line.startswith("warp_instructions_per_launch:"):
+                instructions = float(line.split(":", 1)[1].split()[0])
+    if instructions is None:
+        return None
+    import torch
+    props = torch.cuda.get_device_properties(0)
+    sms = props.multi_processor_count
+    mhz = 2070.0
+    try:
+        out = subprocess.run(["nvidia-smi", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits", "-i", "0"],
+                             capture_output=True, text=True, timeout=20).stdout.split()
+        mhz = float(out[0]) if out else mhz
+    except (OSError, ValueError, subprocess.TimeoutExpired):
+        pass
+    limit_ms = instructions / (sms * schedulers * mhz * 1e6) * 1e3
+    return {"bound": "issue", "warp_instructions_per_launch": instructions, "issue_limit_ms": limit_ms,
+            "ms_per_launch": ms_per_launch, "frac": limit_ms / ms_per_launch, "sms": sms, "sm_max_mhz": mhz}
+
+
 class ClockSampler:
     """nvidia-smi clock and throttle-reason samples every 50 ms.  The sampler is started, and its
     first sample awaited, before the timed region opens, so nvidia-smi's start-up (which briefly
@@ -446,6 +473,7 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, ra
            if gathered is not None else {}),
         "roofline": {"bound": "hbm", "achieved": achieved, "unit": "GB/s", "algorithmic_bytes_per_launch": w.substeps * bytes_per_substep,
                      "traffic": ncu_traffic_per_launch("ncu_batch_frame_c4")},
+        "issue_roof": issue_roof(1e3 * device_s / frames),
     }
 
 
