@@ -1,10 +1,11 @@
 // CPU ORACLE — test infrastructure only.  Nothing in the product links or calls this file; the
-// tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it as the checker.
+// tests and __graft_entry__.smoke() load it to check the CUDA library against it, and bench.py's
+// CPU-baseline leg times it.
 //
 // A plain restatement, on the CPU, of the reference's plain XPBD tissue step and its geometric
 // cut, exporting the same LCS_* C ABI as the reference plugin
 // (endoscopic_tissue/native/vendor/src/plugin_api.cpp) so one Python harness drives the oracle,
-// the CUDA library and (on a GPU machine) the reference build identically.
+// the CUDA library and (on a machine with a GPU) the reference build identically.
 //
 // Built three times from this one source:
 //   liboracle_f32.so  ORACLE_REAL=float   FP32, the arithmetic the reference performs, in the CUDA

@@ -1,7 +1,7 @@
 """CUDA path against the CPU oracle, through the LCS_* C ABI on both sides.
 
 The CUDA kernels evaluate every projection in the oracle's operation order without multiply-add
-contraction, so the FP32 trajectories agree bit for bit; the benchmark spec's tolerance (1e-4 of the
+contraction, so the FP32 trajectories agree bit for bit; the parity tolerance (1e-4 of the
 bounding-box diagonal after 100 steps) is asserted as well, and the FP64 oracle error is reported.
 """
 import numpy as np

@@ -1,7 +1,7 @@
 """CPU checks of the replay harness (tests/replay_harness.py) and of GBT_SetState on the oracle: a
 state captured and loaded back is the identity, a step from a loaded state equals the step the
 session would have taken, the voxel mask rebuilt from the edge fractions equals the oracle's own,
-and the FP32 oracles replayed against the FP64 oracle stay within the benchmark spec's tolerance with
+and the FP32 oracles replayed against the FP64 oracle stay within the parity tolerance with
 identical topology."""
 import ctypes
 

@@ -4,7 +4,7 @@ reference's sources by oracle/build_ref.sh), at every step of each scenario.
 The reference build free-runs a scenario; the CUDA library, the FP32 oracle (the library's operation
 order) and the as-written FP32 oracle (the reference's divisions, library power and logarithm) each
 step from the reference's state of every step under the same commands (tests/replay_harness.py).
-Asserted at every replayed step: positions within the benchmark spec's tolerance, 1e-4 of the bounding-box
+Asserted at every replayed step: positions within the parity tolerance, 1e-4 of the bounding-box
 diagonal, of the reference's next state; the integer topology (neighbour table, bend liveness,
 active flags, voxel cut mask, cut edges, topology revision) identical; the CUDA library bit-identical
 to the FP32 oracle in positions, velocities and topology.  Free-running differences over the whole
