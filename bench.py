@@ -32,6 +32,12 @@ METRIC = "XPBD steps/s & constraint proj/s, batched vs plain; adjoint/forward ti
 FALLBACK_HBM_GBS = 6800.0
 
 
+# The CPU baseline: the FP32 restatement of the path in the reference's own operation order (its
+# divisions, library power and logarithm, no fused multiply-adds; the oracle's as-written build), on
+# the host's cores.  The reference itself has no CPU implementation of the step.
+CPU_REFERENCE = ROOT / "oracle" / "_build" / "liboracle_f32w.so"
+
+
 def measured_peak():
     path = ROOT / "MEASURED_PEAKS.json"
     if path.exists():
@@ -161,7 +167,7 @@ def run_reference_arm(args, world, rank):
         return
     from genesis_tissue_simulation_gb300 import workloads as W
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
-    lib = ROOT / "oracle" / "_build" / "liboracle_f32.so"
+    lib = CPU_REFERENCE
     w = W.make(args.workload)
     session = w.open(lib)
     tets, edges = session.tet_count, int(session.functions["LCS_EdgeCount"]())
@@ -184,7 +190,7 @@ def run_reference_arm(args, world, rank):
             "config": workload_config(args, w, tets, edges, int((w.grid.active != 0).sum()), world),
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} full steps of {w.name} after {args.warmup} warm-up steps, "
-                                       f"CPU restatement (FP32, OpenMP within each colour, {threads} threads), "
+                                       f"CPU restatement in the reference's operation order (FP32, OpenMP within each colour, {threads} threads), "
                                        "wall clock per step (the CPU path has no L2 flush or CUDA events)"},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -300,7 +306,7 @@ def workload_measurement(lib, name, steps, warmup, cpu_budget_s=6.0, launch_mode
         return out
     # CPU restatement, bounded sample
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
-    s = w.open(ROOT / "oracle" / "_build" / "liboracle_f32.so")
+    s = w.open(CPU_REFERENCE)
     try:
         threads = int(s.dll.ORC_Threads())
         s.step(detect_cut=w.command(s, 0))
@@ -312,7 +318,7 @@ def workload_measurement(lib, name, steps, warmup, cpu_budget_s=6.0, launch_mode
     finally:
         s.close()
     out["cpu_baseline"] = {"value": cpu, "unit": "steps/s", "cores": threads, "kind": "port",
-                           "sample": f"steps 2..{n + 1} of {w.name}, CPU restatement FP32, OpenMP {threads} threads"}
+                           "sample": f"steps 2..{n + 1} of {w.name}, CPU restatement FP32 in the reference's operation order, OpenMP {threads} threads"}
     out["gpu_over_cpu"] = out["value"] / cpu
     return out
 
@@ -321,7 +327,7 @@ def cpu_baseline_sample(workload_name, budget_s=15.0, max_steps=40):
     """Time the CPU restatement on a bounded sample of the workload: consecutive steps from the start."""
     from genesis_tissue_simulation_gb300 import workloads as W
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
-    lib = ROOT / "oracle" / "_build" / "liboracle_f32.so"
+    lib = CPU_REFERENCE
     w = W.make(workload_name)
     session = w.open(lib)
     try:
@@ -337,7 +343,7 @@ def cpu_baseline_sample(workload_name, budget_s=15.0, max_steps=40):
     finally:
         session.close()
     return {"value": n / elapsed, "unit": "steps/s", "cores": threads, "kind": "port",
-            "sample": f"steps 2..{n + 1} of {w.name} (one warm-up step), CPU restatement FP32, OpenMP {threads} threads, {elapsed:.1f} s"}
+            "sample": f"steps 2..{n + 1} of {w.name} (one warm-up step), CPU restatement FP32 in the reference's operation order, OpenMP {threads} threads, {elapsed:.1f} s"}
 
 
 def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, rank=0, world=1):
@@ -655,7 +661,7 @@ def cut_topology_cpu_sample(nbr, frames=30):
     from genesis_tissue_simulation_gb300 import workloads as W
 
     w = W.make("c3", steps=frames)
-    o = w.open(str(ROOT / "oracle" / "_build" / "liboracle_f32.so"))
+    o = w.open(str(CPU_REFERENCE))
     try:
         f = o.dll.GBT_SetState
         f.argtypes = (ctypes.c_void_p,) * 8 + (ctypes.c_int, ctypes.c_uint)

@@ -3,8 +3,9 @@
 Two translation units are compiled in parallel with nvcc and linked into
 ``csrc/_build/libgbtissue.so``.  Flags that matter for results:
 
-* ``-fmad=false``: no multiply-add contraction, so every projection rounds exactly as the FP32
-  CPU restatement does (both follow the reference's operation order);
+* ``-fmad=false``: no implicit multiply-add contraction; the projections contract explicitly
+  (``fmaf``) exactly where the FP32 CPU restatement calls ``std::fma``, so every projection rounds as
+  it does;
 * ``-Xcompiler -ffp-contract=off``: the host-side coefficient arithmetic (h, compliances, rest
   shapes) rounds identically on x86-64 and aarch64 hosts.
 """

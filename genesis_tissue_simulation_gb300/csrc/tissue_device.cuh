@@ -11,8 +11,10 @@
 //   topology: nbr int[6N] (slot 2a = -a, 2a+1 = +a, -1 severed), bend pairs 32 B records.
 //
 // Every projection below evaluates the reference kernel's expression in the reference's operation
-// order, with no contraction of multiply-add pairs (the library is compiled with -fmad=false), so
-// results are rounded exactly as the CPU restatement rounds them.
+// order.  The compiler contracts nothing (the library is compiled with -fmad=false); the edge and tet
+// projections contract chosen products into explicit fused multiply-adds (fmv, dotF, crossF, fmaf),
+// and the CPU restatement calls std::fma at the same sites, so results round exactly as it rounds
+// them.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -202,6 +204,14 @@ GBT_HD float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 GBT_HD f3 cross(f3 a, f3 b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
 GBT_HD float len(f3 a) { return sqrtf(dot(a, a)); }
 GBT_HD float comp(f3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+// Fused multiply-adds of the projections (one rounding each; the CPU restatement calls std::fma at
+// the same sites, so both sides still round identically): a s + c, the dot product
+// (a.x b.x + a.y b.y) + a.z b.z and the cross product, each with its products contracted.
+GBT_HD f3 fmv(f3 a, float s, f3 c) { return mk(fmaf(a.x, s, c.x), fmaf(a.y, s, c.y), fmaf(a.z, s, c.z)); }
+GBT_HD float dotF(f3 a, f3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
+GBT_HD f3 crossF(f3 a, f3 b) {
+    return mk(fmaf(a.y, b.z, -(a.z * b.y)), fmaf(a.z, b.x, -(a.x * b.z)), fmaf(a.x, b.y, -(a.y * b.x)));
+}
 
 // Instrument frame of one substep, contact model 0 (xpbd_solver.cu:3467-3483, 3573-3580): the shaft
 // capsule and jaw box interpolated linearly from the previous frame's command to the current one,
@@ -231,7 +241,8 @@ GBT_HD ContactFrame contactFrame(const ToolPose& a, const ToolPose& b, float t, 
     return f;
 }
 
-// J^(-2/3): inverse cube root by four Newton steps in correction form y <- y + y(1 - J y^3)(1/3) from a
+// J^(-2/3): inverse cube root by four Newton steps in correction form y <- y + y(1 - J y^3)(1/3) (both
+// updates fused multiply-adds) from a
 // bit-level seed (the exponent trick of the fast inverse square root applied to the -1/3 power,
 // constant 0x54A23000 fitted on [0.05, 1e6]), squared.  <= 2.4 ulp from the exact power; the same
 // sequence of correctly rounded operations runs on the host, so both sides agree bit for bit.
@@ -242,8 +253,8 @@ __device__ __forceinline__ float powMinusTwoThirds(float J) {
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         float y3 = (y * y) * y;
-        float r = 1.f - J * y3;
-        y = y + (y * r) * kOneThird;
+        float r = fmaf(-J, y3, 1.f);
+        y = fmaf(y * r, kOneThird, y);
     }
     return y * y;
 }
@@ -331,17 +342,17 @@ __device__ __forceinline__ bool solveEdge(const EdgeRecord& r, const FrameCoeffs
     float wi = pi.w, wj = pj.w, ws = wi + wj;
     if (ws <= 0.f) return false;
     f3 d = xyz(pi) - xyz(pj);
-    float L = len(d);
+    float L = sqrtf(dotF(d, d));
     if (L < 1e-9f) return false;
     f3 n = d * (1.f / L);
     float C = L - r.rest;
     float gamma = fc.betaGammaHS;
     // undamped (gamma = 0): the damping term is a zero and its gradient is not formed
-    float num = gamma != 0.f ? -C - gamma * dot(n, (xyz(pi) - r.qi) - (xyz(pj) - r.qj)) : -C;
-    float dl = num / ((1.f + gamma) * ws + alphaTilde);
+    float num = gamma != 0.f ? fmaf(-gamma, dotF(n, (xyz(pi) - r.qi) - (xyz(pj) - r.qj)), -C) : -C;
+    float dl = num / fmaf(1.f + gamma, ws, alphaTilde);
     float ap = fc.omega * dl;
-    f3 a = xyz(pi) + n * (wi * ap);
-    f3 b = xyz(pj) - n * (wj * ap);
+    f3 a = fmv(n, wi * ap, xyz(pi));
+    f3 b = fmv(n, -(wj * ap), xyz(pj));
     oi = make_float4(a.x, a.y, a.z, wi);
     oj = make_float4(b.x, b.y, b.z, wj);
     return true;
@@ -448,13 +459,13 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
     f3 e1 = p[1] - p[0], e2 = p[2] - p[0], e3 = p[3] - p[0];
     f3 F[3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) F[c] = e1 * comp(br[0], c) + e2 * comp(br[1], c) + e3 * comp(br[2], c);
-    float I1 = dot(F[0], F[0]) + dot(F[1], F[1]) + dot(F[2], F[2]);
-    f3 cof[3] = {cross(F[1], F[2]), cross(F[2], F[0]), cross(F[0], F[1])};
+    for (int c = 0; c < 3; c++) F[c] = fmv(e3, comp(br[2], c), fmv(e2, comp(br[1], c), e1 * comp(br[0], c)));
+    float I1 = dotF(F[0], F[0]) + dotF(F[1], F[1]) + dotF(F[2], F[2]);
+    f3 cof[3] = {crossF(F[1], F[2]), crossF(F[2], F[0]), crossF(F[0], F[1])};
     float ad = t.alpha.x, ah = t.alpha.y;
-    float J = dot(F[0], cof[0]), pJ = fmaxf(J, .05f);
+    float J = dotF(F[0], cof[0]), pJ = fmaxf(J, .05f);
     float iso = powMinusTwoThirds(pJ);
-    float q = fmaxf(iso * I1 - 3.f, 0.f);
+    float q = fmaxf(fmaf(iso, I1, -3.f), 0.f);
     float CD = sqrtf(fmaxf(q, 1e-12f));
     float devScale = 1.f / CD;
     float volGrad = J > .05f ? iso * I1 / (3.f * pJ) : 0.f;
@@ -464,8 +475,8 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
 #pragma unroll
     for (int c = 1; c < 4; c++) {
         f3 b = br[c - 1];
-        gh[c] = cof[0] * b.x + cof[1] * b.y + cof[2] * b.z;
-        gd[c] = ((F[0] * b.x + F[1] * b.y + F[2] * b.z) * iso - gh[c] * volGrad) * devScale;
+        gh[c] = fmv(cof[2], b.z, fmv(cof[1], b.y, cof[0] * b.x));
+        gd[c] = fmv(fmv(F[2], b.z, fmv(F[1], b.y, F[0] * b.x)), iso, gh[c] * -volGrad) * devScale;
         if (guarded) gh[c] = gh[c] * (1.f / pJ);
     }
     gd[0] = (gd[1] + gd[2] + gd[3]) * -1.f;
@@ -476,12 +487,12 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         w[c] = P[c].w;
-        dd += w[c] * dot(gd[c], gd[c]);
-        dh += w[c] * dot(gd[c], gh[c]);
+        dd = fmaf(w[c], dotF(gd[c], gd[c]), dd);
+        dh = fmaf(w[c], dotF(gd[c], gh[c]), dh);
         if (damped) {
             f3 dx = p[c] - t.q[c];
-            vd += dot(gd[c], dx);
-            vh += dot(gh[c], dx);
+            vd += dotF(gd[c], dx);
+            vh += dotF(gh[c], dx);
         }
     }
     // 1 / (1 + D/h) is a frame constant; one reciprocal of A serves gamma and dlD
@@ -489,25 +500,25 @@ __device__ __forceinline__ void applyTet(const DeviceMesh& m, const TetRecord& t
     float invScale = fc.invScale, invBulk = guarded ? fc.invBulkScale : fc.invScale;
     float eAd = ad * invScale, eAh = ah * invBulk;
     float A = dd + eAd, invA = 1.f / A, Bc = dh, gamma = Bc * invA;
-    float schur = eAh + eAd * gamma * gamma;
+    float schur = fmaf(eAd * gamma, gamma, eAh);
 #pragma unroll
-    for (int c = 0; c < 4; c++) { f3 r = gh[c] - gd[c] * gamma; schur += w[c] * dot(r, r); }
-    float rd = damped ? (-CD - fc.dampingOverH * vd) * invScale : -CD * invScale;
-    float rh = damped ? (-CH - (bulkScale - 1.f) * vh) * invBulk : -CH * invBulk;
+    for (int c = 0; c < 4; c++) { f3 r = fmv(gd[c], -gamma, gh[c]); schur = fmaf(w[c], dotF(r, r), schur); }
+    float rd = damped ? fmaf(-fc.dampingOverH, vd, -CD) * invScale : -CD * invScale;
+    float rh = damped ? fmaf(-(bulkScale - 1.f), vh, -CH) * invBulk : -CH * invBulk;
     if (!(A > 0.f) || !(schur > 0.f)) return;
-    float dlH = fc.omega * (rh - gamma * rd) / schur, dlD = (fc.omega * rd - Bc * dlH) * invA;
+    float dlH = fc.omega * fmaf(-gamma, rd, rh) / schur, dlD = fmaf(-Bc, dlH, fc.omega * rd) * invA;
     if (!isfinite(dlD) || !isfinite(dlH)) return;
     if (guarded) {
         float largest = 0.f;
 #pragma unroll
-        for (int c = 0; c < 4; c++) largest = fmaxf(largest, len((gd[c] * dlD + gh[c] * dlH) * w[c]));
+        for (int c = 0; c < 4; c++) largest = fmaxf(largest, len(fmv(gd[c], dlD, gh[c] * dlH) * w[c]));
         float limit = .15f / fmaxf(len(br[0]), fmaxf(len(br[1]), len(br[2])));
         float accepted = largest > limit ? limit / largest : 1.f;
         dlD *= accepted; dlH *= accepted;
     }
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-        f3 o = p[c] + (gd[c] * dlD + gh[c] * dlH) * w[c];
+        f3 o = fmv(fmv(gd[c], dlD, gh[c] * dlH), w[c], p[c]);
         posRef<Dsm>(m, id[c]) = make_float4(o.x, o.y, o.z, w[c]);
     }
 }

@@ -95,6 +95,19 @@ static inline V3 operator*(V3 a, Real s) { return v3(a.x * s, a.y * s, a.z * s);
 static inline Real dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 static inline V3 cross(V3 a, V3 b) { return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
 static inline Real len(V3 a) { return std::sqrt(dot(a, a)); }
+// The fused multiply-adds the CUDA library's edge and tet projections use (std::fma: one rounding,
+// as the device's fmaf), at the same sites; the as-written build evaluates the same expressions
+// unfused, which is exactly the reference's order (a s + c and c + a s round alike).
+#ifdef ORACLE_AS_WRITTEN
+static inline Real fmaR(Real a, Real b, Real c) { return a * b + c; }
+#else
+static inline Real fmaR(Real a, Real b, Real c) { return std::fma(a, b, c); }
+#endif
+static inline V3 fmv(V3 a, Real s, V3 c) { return v3(fmaR(a.x, s, c.x), fmaR(a.y, s, c.y), fmaR(a.z, s, c.z)); }
+static inline Real dotF(V3 a, V3 b) { return fmaR(a.z, b.z, fmaR(a.y, b.y, a.x * b.x)); }
+static inline V3 crossF(V3 a, V3 b) {
+    return v3(fmaR(a.y, b.z, -(a.z * b.y)), fmaR(a.z, b.x, -(a.x * b.z)), fmaR(a.x, b.y, -(a.y * b.x)));
+}
 static inline Real comp(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
 static inline bool isFin(Real x) { return std::isfinite(x); }
 
@@ -111,8 +124,8 @@ static inline float powMinusTwoThirds(float J) {
     std::memcpy(&y, &bits, 4);
     for (int k = 0; k < 4; k++) {
         float y3 = (y * y) * y;
-        float r = 1.f - J * y3;
-        y = y + (y * r) * 0.333333343f;   // 1/3 rounded to FP32
+        float r = std::fma(-J, y3, 1.f);
+        y = std::fma(y * r, 0.333333343f, y);   // 1/3 rounded to FP32
     }
     return y * y;
 }
@@ -641,7 +654,7 @@ static void projectEdge(int e, Real alphaTilde, Real gamma, bool fallback, Real 
     Real wi = S.invMass[i], wj = S.invMass[j], ws = wi + wj;
     if (ws <= 0) return;
     V3 d = S.pos[i] - S.pos[j];
-    Real L = len(d);
+    Real L = std::sqrt(dotF(d, d));
     if (L < Real(1e-9)) return;
     V3 n = d * (Real(1) / L);
     Real C = L - S.eRest[e];
@@ -650,12 +663,12 @@ static void projectEdge(int e, Real alphaTilde, Real gamma, bool fallback, Real 
     Real dl = (-C - gamma * gradDx) / ((Real(1) + gamma) * ws + alphaTilde);
 #else
     // the library's form: without edge damping (gamma = 0) the damping term is a zero and is not formed
-    Real num = gamma != Real(0) ? -C - gamma * dot(n, (S.pos[i] - S.prev[i]) - (S.pos[j] - S.prev[j])) : -C;
-    Real dl = num / ((Real(1) + gamma) * ws + alphaTilde);
+    Real num = gamma != Real(0) ? fmaR(-gamma, dotF(n, (S.pos[i] - S.prev[i]) - (S.pos[j] - S.prev[j])), -C) : -C;
+    Real dl = num / fmaR(Real(1) + gamma, ws, alphaTilde);
 #endif
     Real ap = S.omega * dl;
-    S.pos[i] = S.pos[i] + n * (wi * ap);
-    S.pos[j] = S.pos[j] - n * (wj * ap);
+    S.pos[i] = fmv(n, wi * ap, S.pos[i]);
+    S.pos[j] = fmv(n, -(wj * ap), S.pos[j]);
 }
 
 static void projectBend(int e) {
@@ -695,18 +708,18 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
     V3 br[3] = {v3(Bm[0][0], Bm[0][1], Bm[0][2]), v3(Bm[1][0], Bm[1][1], Bm[1][2]), v3(Bm[2][0], Bm[2][1], Bm[2][2])};
     V3 e1 = p[1] - p[0], e2 = p[2] - p[0], e3 = p[3] - p[0];
     V3 F[3];
-    for (int c = 0; c < 3; c++) F[c] = e1 * comp(br[0], c) + e2 * comp(br[1], c) + e3 * comp(br[2], c);
-    Real I1 = dot(F[0], F[0]) + dot(F[1], F[1]) + dot(F[2], F[2]);
-    V3 cof[3] = {cross(F[1], F[2]), cross(F[2], F[0]), cross(F[0], F[1])};
+    for (int c = 0; c < 3; c++) F[c] = fmv(e3, comp(br[2], c), fmv(e2, comp(br[1], c), e1 * comp(br[0], c)));
+    Real I1 = dotF(F[0], F[0]) + dotF(F[1], F[1]) + dotF(F[2], F[2]);
+    V3 cof[3] = {crossF(F[1], F[2]), crossF(F[2], F[0]), crossF(F[0], F[1])};
     Real ad = S.aDev[e], ah = S.aHyd[e];
-    Real J = dot(F[0], cof[0]), pJ = std::fmax(J, Real(0.05));
+    Real J = dotF(F[0], cof[0]), pJ = std::fmax(J, Real(0.05));
 #ifdef ORACLE_AS_WRITTEN
     // the reference's own operations (xpbd_solver.cu:773, 781): the library power and logarithm
     Real iso = std::pow(pJ, Real(-2.f / 3.f));
 #else
     Real iso = powMinusTwoThirds(pJ);
 #endif
-    Real q = std::fmax(iso * I1 - Real(3), Real(0));
+    Real q = std::fmax(fmaR(iso, I1, Real(-3)), Real(0));
     Real CD = std::sqrt(std::fmax(q, Real(1e-12)));
     Real devScale = Real(1) / CD;
     Real volGrad = J > Real(0.05) ? iso * I1 / (Real(3) * pJ) : Real(0);
@@ -720,8 +733,8 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
     V3 gd[4], gh[4];
     for (int k = 1; k < 4; k++) {
         V3 b = br[k - 1];
-        gh[k] = cof[0] * b.x + cof[1] * b.y + cof[2] * b.z;
-        gd[k] = ((F[0] * b.x + F[1] * b.y + F[2] * b.z) * iso - gh[k] * volGrad) * devScale;
+        gh[k] = fmv(cof[2], b.z, fmv(cof[1], b.y, cof[0] * b.x));
+        gd[k] = fmv(fmv(F[2], b.z, fmv(F[1], b.y, F[0] * b.x)), iso, gh[k] * -volGrad) * devScale;
         if (guarded) gh[k] = gh[k] * (Real(1) / pJ);
     }
     gd[0] = (gd[1] + gd[2] + gd[3]) * Real(-1);
@@ -736,10 +749,10 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
     Real dd = 0, dh = 0, hh = 0, vd = 0, vh = 0, w[4];
     for (int k = 0; k < 4; k++) {
         w[k] = S.invMass[id[k]];
-        dd += w[k] * dot(gd[k], gd[k]); dh += w[k] * dot(gd[k], gh[k]); hh += w[k] * dot(gh[k], gh[k]);
+        dd = fmaR(w[k], dotF(gd[k], gd[k]), dd); dh = fmaR(w[k], dotF(gd[k], gh[k]), dh); hh += w[k] * dot(gh[k], gh[k]);
         if (damped) {
             V3 dx = p[k] - S.prev[id[k]];
-            vd += dot(gd[k], dx); vh += dot(gh[k], dx);
+            vd += dotF(gd[k], dx); vh += dotF(gh[k], dx);
         }
     }
     (void)hh;
@@ -759,22 +772,22 @@ static void projectTet(int e, Real dampingOverH, Real bulkDampingOverH) {
     Real invScale = Real(1) / scale, invBulk = Real(1) / bulkScale;
     Real eAd = ad * invScale, eAh = ah * invBulk;
     Real A = dd + eAd, invA = Real(1) / A, Bc = dh, gamma = Bc * invA;
-    Real schur = eAh + eAd * gamma * gamma;
-    for (int k = 0; k < 4; k++) { V3 r = gh[k] - gd[k] * gamma; schur += w[k] * dot(r, r); }
-    Real rd = damped ? (-CD - dampingOverH * vd) * invScale : -CD * invScale;
-    Real rh = damped ? (-CH - (bulkScale - Real(1)) * vh) * invBulk : -CH * invBulk;
+    Real schur = fmaR(eAd * gamma, gamma, eAh);
+    for (int k = 0; k < 4; k++) { V3 r = fmv(gd[k], -gamma, gh[k]); schur = fmaR(w[k], dotF(r, r), schur); }
+    Real rd = damped ? fmaR(-dampingOverH, vd, -CD) * invScale : -CD * invScale;
+    Real rh = damped ? fmaR(-(bulkScale - Real(1)), vh, -CH) * invBulk : -CH * invBulk;
     if (!(A > 0) || !(schur > 0)) return;
-    Real dlH = S.omega * (rh - gamma * rd) / schur, dlD = (S.omega * rd - Bc * dlH) * invA;
+    Real dlH = S.omega * fmaR(-gamma, rd, rh) / schur, dlD = fmaR(-Bc, dlH, S.omega * rd) * invA;
 #endif
     if (!isFin(dlD) || !isFin(dlH)) return;
     if (guarded) {   // trust region on the update: no corner moves more than 0.15 of the shortest rest edge scale
         Real largest = 0;
-        for (int k = 0; k < 4; k++) largest = std::fmax(largest, len((gd[k] * dlD + gh[k] * dlH) * w[k]));
+        for (int k = 0; k < 4; k++) largest = std::fmax(largest, len(fmv(gd[k], dlD, gh[k] * dlH) * w[k]));
         Real limit = Real(0.15) / std::fmax(len(br[0]), std::fmax(len(br[1]), len(br[2])));
         Real accepted = largest > limit ? limit / largest : Real(1);
         dlD *= accepted; dlH *= accepted;
     }
-    for (int k = 0; k < 4; k++) S.pos[id[k]] = p[k] + (gd[k] * dlD + gh[k] * dlH) * w[k];
+    for (int k = 0; k < 4; k++) S.pos[id[k]] = fmv(fmv(gd[k], dlD, gh[k] * dlH), w[k], p[k]);
 }
 
 // Tensile reinforcement of one live tet (projectTensile, xpbd_solver.cu:592-620): each of the six
