@@ -72,15 +72,15 @@ __device__ __forceinline__ EdgeAdjoint edgeVJP(float4 Pi, float4 Pj, f3 qi, f3 q
     if (ws <= 0.f) return o;
     f3 pi = xyz(Pi), pj = xyz(Pj);
     f3 d = pi - pj;
-    float L = len(d);
+    float L = sqrtf(dotF(d, d));   // the forward's operations (solveEdge), fused where it fuses
     if (L < 1e-9f) return o;
     float inv = 1.f / L;
     f3 n = d * inv;
     float C = L - rest;
     f3 u = (pi - qi) - (pj - qj);
-    float gdx = dot(n, u);
-    float den = (1.f + gamma) * ws + alphaTilde;
-    float dl = (-C - gamma * gdx) / den;
+    float gdx = dotF(n, u);
+    float den = fmaf(1.f + gamma, ws, alphaTilde);
+    float dl = (gamma != 0.f ? fmaf(-gamma, gdx, -C) : -C) / den;
     float ap = omega * dl;
     // a = pi + n (wi ap), b = pj - n (wj ap)
     f3 gn = ga * (wi * ap) - gb * (wj * ap);
@@ -123,12 +123,12 @@ __device__ __forceinline__ void tetVJP(const float* Bm, const float4 P[4], const
     f3 e[3] = {p[1] - p[0], p[2] - p[0], p[3] - p[0]};
     f3 F[3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) F[c] = e[0] * comp(br[0], c) + e[1] * comp(br[1], c) + e[2] * comp(br[2], c);
-    float I1 = dot(F[0], F[0]) + dot(F[1], F[1]) + dot(F[2], F[2]);
-    f3 cof[3] = {cross(F[1], F[2]), cross(F[2], F[0]), cross(F[0], F[1])};
-    float J = dot(F[0], cof[0]), pJ = fmaxf(J, .05f);
+    for (int c = 0; c < 3; c++) F[c] = fmv(e[2], comp(br[2], c), fmv(e[1], comp(br[1], c), e[0] * comp(br[0], c)));
+    float I1 = dotF(F[0], F[0]) + dotF(F[1], F[1]) + dotF(F[2], F[2]);
+    f3 cof[3] = {crossF(F[1], F[2]), crossF(F[2], F[0]), crossF(F[0], F[1])};
+    float J = dotF(F[0], cof[0]), pJ = fmaxf(J, .05f);
     float iso = powMinusTwoThirds(pJ);
-    float qv = iso * I1 - 3.f;
+    float qv = fmaf(iso, I1, -3.f);
     float q0 = fmaxf(qv, 0.f);
     float CD = sqrtf(fmaxf(q0, 1e-12f));
     float devScale = 1.f / CD;
@@ -138,9 +138,9 @@ __device__ __forceinline__ void tetVJP(const float* Bm, const float4 P[4], const
 #pragma unroll
     for (int c = 1; c < 4; c++) {
         f3 b = br[c - 1];
-        gh[c] = cof[0] * b.x + cof[1] * b.y + cof[2] * b.z;
-        G[c] = F[0] * b.x + F[1] * b.y + F[2] * b.z;
-        gd[c] = (G[c] * iso - gh[c] * volGrad) * devScale;
+        gh[c] = fmv(cof[2], b.z, fmv(cof[1], b.y, cof[0] * b.x));
+        G[c] = fmv(F[2], b.z, fmv(F[1], b.y, F[0] * b.x));
+        gd[c] = fmv(G[c], iso, gh[c] * -volGrad) * devScale;
     }
     gd[0] = (gd[1] + gd[2] + gd[3]) * -1.f;
     gh[0] = (gh[1] + gh[2] + gh[3]) * -1.f;
@@ -149,23 +149,24 @@ __device__ __forceinline__ void tetVJP(const float* Bm, const float4 P[4], const
 #pragma unroll
     for (int c = 0; c < 4; c++) {
         w[c] = P[c].w;
-        dd += w[c] * dot(gd[c], gd[c]);
-        dh += w[c] * dot(gd[c], gh[c]);
+        dd = fmaf(w[c], dotF(gd[c], gd[c]), dd);
+        dh = fmaf(w[c], dotF(gd[c], gh[c]), dh);
         dx[c] = p[c] - q[c];
-        vd += dot(gd[c], dx[c]);
-        vh += dot(gh[c], dx[c]);
+        vd += dotF(gd[c], dx[c]);
+        vh += dotF(gh[c], dx[c]);
     }
     float scale = 1.f + dampingOverH, invScale = 1.f / scale;
     float eAd = ad * invScale, eAh = ah * invScale;
     float A = dd + eAd, invA = 1.f / A, Bc = dh, gamma = Bc * invA;
-    float schur = eAh + eAd * gamma * gamma;
+    float schur = fmaf(eAd * gamma, gamma, eAh);
     f3 r[4];
 #pragma unroll
-    for (int c = 0; c < 4; c++) { r[c] = gh[c] - gd[c] * gamma; schur += w[c] * dot(r[c], r[c]); }
-    float rd = (-CD - dampingOverH * vd) * invScale;
-    float rh = (-CH - (scale - 1.f) * vh) * invScale;
+    for (int c = 0; c < 4; c++) { r[c] = fmv(gd[c], -gamma, gh[c]); schur = fmaf(w[c], dotF(r[c], r[c]), schur); }
+    const bool damped = dampingOverH != 0.f;
+    float rd = damped ? fmaf(-dampingOverH, vd, -CD) * invScale : -CD * invScale;
+    float rh = damped ? fmaf(-(scale - 1.f), vh, -CH) * invScale : -CH * invScale;
     if (!(A > 0.f) || !(schur > 0.f)) return;
-    float dlH = omega * (rh - gamma * rd) / schur, dlD = (omega * rd - Bc * dlH) * invA;
+    float dlH = omega * fmaf(-gamma, rd, rh) / schur, dlD = fmaf(-Bc, dlH, omega * rd) * invA;
     if (!isfinite(dlD) || !isfinite(dlH)) return;
     // ---- reverse ----
     // o_c = p_c + (gd_c dlD + gh_c dlH) w_c
