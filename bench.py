@@ -465,7 +465,10 @@ def batched_measurement(lib, frames, warmup, plain_sample=16, plain_frames=6, ra
         "proj_per_s": value * w.substeps * (info["edges"] + info["tets"]) / count,
         "instances": count, "lattice_nodes": info["nodes"], "active_nodes": n_active, "tets": info["tets"],
         "edges": info["edges"], "substeps": w.substeps, "launch": {"mode": tune["mode"], "threads": tune["threads"],
+                                                                    "packing": tune["packing"],
                                                                     "autotune_ms_per_frame": tune["ms_per_frame"],
+                                                                    "autotune_trials": [[t["mode"], t["threads"], t["packing"], t["element_tables"],
+                                                                                         round(t["ms_per_frame"], 3)] for t in tune["trials"]],
                                                                     "element_tables": tables,
                                                                     "explicit_tables_ms_per_frame": explicit_ms},
         "plain_instance_steps_per_s": plain_rate, "plain_sample": f"{len(picks)} instances spread over the size order, "

@@ -34,6 +34,7 @@ SIGNATURES = (
     ("GBT_BatchSetLaunch", (I, I), I), ("GBT_BatchAutotune", (F, I, P, P, P), I), ("GBT_BatchProfileEnable", (I,), None),
     ("GBT_BatchProfileRead", (P,), I), ("GBT_BatchShutdown", (), None),
     ("GBT_BatchSetElementTables", (I,), I), ("GBT_BatchElementTables", (), I),
+    ("GBT_BatchSetPacking", (I,), I), ("GBT_BatchPacking", (), I), ("GBT_BatchAutotuneTable", (I, P, P), I),
 )
 
 
@@ -144,10 +145,28 @@ class TissueBatch:
     def set_launch(self, mode, threads=256):
         self.check("GBT_BatchSetLaunch", mode, threads)
 
+    def set_packing(self, packing):
+        """Instance packing of the per-instance shapes: 0 LPT on tets, 1 LPT on tets + edges + nodes,
+        2 size-ordered serpentine deal."""
+        self.check("GBT_BatchSetPacking", int(packing))
+
+    def packing(self) -> int:
+        return int(self.f["GBT_BatchPacking"]())
+
     def autotune(self, trial_steps=3):
+        """Time every launch configuration and keep the fastest.  Returns the chosen mode and threads,
+        the best ms per frame of each of the six launch shapes, and every trial (mode, threads,
+        packing, element tables, ms per frame; -1 where it cannot run this batch)."""
         mode, threads, ms = I(), I(), (F * 6)()
         self.check("GBT_BatchAutotune", self.dt, trial_steps, ct.byref(mode), ct.byref(threads), ms)
-        return {"mode": mode.value, "threads": threads.value, "ms_per_frame": [float(v) for v in ms]}
+        n = int(self.f["GBT_BatchAutotuneTable"](0, None, None))
+        shape = np.zeros((max(n, 1), 4), dtype=np.int32)
+        times = np.zeros(max(n, 1), dtype=np.float32)
+        self.f["GBT_BatchAutotuneTable"](n, pointer(shape), pointer(times))
+        trials = [{"mode": int(r[0]), "threads": int(r[1]), "packing": int(r[2]), "element_tables": "implicit" if r[3] else "explicit",
+                   "ms_per_frame": float(t)} for r, t in zip(shape[:n], times[:n])]
+        return {"mode": mode.value, "threads": threads.value, "packing": self.packing(), "element_tables": self.element_tables(),
+                "ms_per_frame": [float(v) for v in ms], "trials": trials}
 
     def positions(self, out=None):
         """Every instance's node positions [total_nodes, 3]; into `out` when given (float32, C order)."""

@@ -72,6 +72,9 @@ struct Batch {
     float lastH = -1.f;
     // launch
     int mode = 0, threads = 256, ctas = 0;            // mode 0 lockstep grid, 1 one CTA per instance, 2 clusters
+    int packing = 0;                                  // modes 1, 2: how instances are dealt to CTAs / clusters (packInstances)
+    struct Trial { int mode, threads, packing, tables; float ms; };
+    std::vector<Trial> trials;                        // the last autotune's table
     int clusterLogK = 1, clusterSlots = 0;            // mode 2: CTAs per cluster (2^logK), shared-memory slots per CTA
     cudaGraphExec_t graph = nullptr; int graphSteps = 0; int graphMode = -1; float graphDt = 0.f;
     bool profile = false; std::vector<cudaEvent_t> events;
@@ -98,6 +101,7 @@ void releaseAll() {
     for (cudaEvent_t e : G.events) cudaEventDestroy(e);
     G.events.clear();
     G.ready = false; G.armed = false; G.lastH = -1.f;
+    G.packing = 0; G.trials.clear();
 }
 
 int ensureDevice() {
@@ -114,18 +118,32 @@ int ensureDevice() {
     return 0;
 }
 
-// Longest-processing-time packing of instances (by tet count) over `ctas` CTAs.
+// Instances dealt to `ctas` CTAs (or clusters), by G.packing:
+//   0  longest processing time first on tet counts (the heaviest instance to the least loaded CTA);
+//   1  the same on a work estimate that counts every element a frame sweeps (tets + edges + nodes);
+//   2  instances in decreasing size dealt round-robin in serpentine order (no load accounting).
+// Every packing gives the same results: an instance is advanced by one CTA or cluster either way.
 int packInstances(int ctas) {
     ctas = std::max(1, std::min(ctas, G.count));
+    auto work = [](int i) -> long long {
+        return G.packing == 1 ? (long long)G.tetCount[i] + G.edgeCount[i] + G.nodeCount[i] : (long long)G.tetCount[i];
+    };
     std::vector<int> byWork(G.count);
     std::iota(byWork.begin(), byWork.end(), 0);
-    std::stable_sort(byWork.begin(), byWork.end(), [](int a, int b) { return G.tetCount[a] > G.tetCount[b]; });
+    std::stable_sort(byWork.begin(), byWork.end(), [&](int a, int b) { return work(a) > work(b); });
     std::vector<long long> load(ctas, 0);
     std::vector<std::vector<int>> lists(ctas);
-    for (int i : byWork) {
-        int best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    for (size_t k = 0; k < byWork.size(); k++) {
+        const int i = byWork[k];
+        int best;
+        if (G.packing == 2) {
+            const int lap = (int)(k / ctas), at = (int)(k % ctas);
+            best = (lap & 1) ? ctas - 1 - at : at;
+        } else {
+            best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        }
         lists[best].push_back(i);
-        load[best] += G.tetCount[i] + 1;
+        load[best] += work(i) + 1;
     }
     std::vector<int> order, start(1, 0);
     for (auto& l : lists) { order.insert(order.end(), l.begin(), l.end()); start.push_back((int)order.size()); }
@@ -648,6 +666,22 @@ LCS_API int GBT_BatchSetLaunch(int mode, int threads) {
 // the state back (all shapes give bit-identical results, so the trial frames leave no trace).
 // Out: mode, threads, and the ms per frame of each candidate (kAutotuneShapes floats; a shape the
 // batch cannot use, e.g. a cluster too small for its largest instance, reports -1).
+// Instance packing of the modes that give an instance to one CTA or cluster (0, 1, 2 as in
+// packInstances); takes effect at once for the current launch shape.
+LCS_API int GBT_BatchSetPacking(int packing) {
+    if (!G.ready || packing < 0 || packing > 2) return XPBD_ERR_BAD_ARG;
+    G.packing = packing;
+    return G.mode == 0 ? 0 : GBT_BatchSetLaunch(G.mode, G.threads);
+}
+LCS_API int GBT_BatchPacking() { return G.ready ? G.packing : -1; }
+
+// Try every launch configuration for `trialSteps` frames from the current state, keep the fastest, and
+// put the state back (all configurations give bit-identical results, so the trial frames leave no
+// trace).  Searched: the lockstep grid on either element-table form; one CTA per instance at 256 and
+// 512 threads and clusters of 2, 4 and 8 CTAs, each with the three instance packings.  (A colour
+// sweep closes with one synchronisation per colour in every shape: a colour reads what the
+// previous one wrote.)  msOut6 gets the best time of each of the six launch shapes {0/256, 1/256,
+// 1/512, 2/2, 2/4, 2/8}, -1 where a shape cannot run; GBT_BatchAutotuneTable returns every trial.
 LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threadsOut, float* msOut6) {
     if (!G.ready || trialSteps <= 0) return XPBD_ERR_BAD_ARG;
     Buf<float4> savePos, savePrev, saveVel;
@@ -656,13 +690,28 @@ LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threa
     CK(cudaMemcpyAsync(savePrev.p, G.prev.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
     CK(cudaMemcpyAsync(saveVel.p, G.vel.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
     std::vector<ToolPose> keepFrom = G.toolFrom, keepTool = G.tool;
-    const int modes[6][2] = {{0, 256}, {1, 256}, {1, 512}, {2, 2}, {2, 4}, {2, 8}};
-    float best = 1e30f; int bestK = 0;
+    const int shapes[6][2] = {{0, 256}, {1, 256}, {1, 512}, {2, 2}, {2, 4}, {2, 8}};
+    std::vector<Batch::Trial> plan;
+    for (int k = 0; k < 6; k++) {
+        if (shapes[k][0] == 0) {
+            if (G.codesAvailable) plan.push_back({0, 256, 0, 1, -1.f});
+            plan.push_back({0, 256, 0, 0, -1.f});
+        } else {
+            for (int pk = 0; pk < 3; pk++) plan.push_back({shapes[k][0], shapes[k][1], pk, G.useCodes ? 1 : 0, -1.f});
+        }
+    }
+    const bool keepCodes = G.useCodes;
+    float best = 1e30f; int bestK = -1;
+    if (msOut6) for (int k = 0; k < 6; k++) msOut6[k] = -1.f;
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a)); CK(cudaEventCreate(&b));
-    for (int k = 0; k < 6; k++) {
-        int rc = GBT_BatchSetLaunch(modes[k][0], modes[k][1]);
-        if (rc == LCS_ERR_UNSUPPORTED) { if (msOut6) msOut6[k] = -1.f; continue; }
+    for (size_t k = 0; k < plan.size(); k++) {
+        Batch::Trial& t = plan[k];
+        int rc = GBT_BatchSetElementTables(t.tables);
+        if (rc) return rc;
+        G.packing = t.packing;
+        rc = GBT_BatchSetLaunch(t.mode, t.threads);
+        if (rc == LCS_ERR_UNSUPPORTED) continue;
         if (rc) return rc;
         rc = stepFrames(dt, 1, nullptr, false);   // warm-up
         if (rc) return rc;
@@ -672,9 +721,10 @@ LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threa
         CK(cudaEventSynchronize(b));
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, a, b));
-        ms /= trialSteps;
-        if (msOut6) msOut6[k] = ms;
-        if (ms < best) { best = ms; bestK = k; }
+        t.ms = ms / trialSteps;
+        for (int q = 0; q < 6 && msOut6; q++)
+            if (shapes[q][0] == t.mode && shapes[q][1] == t.threads && (msOut6[q] < 0.f || t.ms < msOut6[q])) msOut6[q] = t.ms;
+        if (t.ms < best) { best = t.ms; bestK = (int)k; }
         CK(cudaMemcpyAsync(G.pos.p, savePos.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
         CK(cudaMemcpyAsync(G.prev.p, savePrev.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
         CK(cudaMemcpyAsync(G.vel.p, saveVel.p, G.N * sizeof(float4), cudaMemcpyDeviceToDevice, G.stream));
@@ -682,12 +732,32 @@ LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threa
     }
     cudaEventDestroy(a); cudaEventDestroy(b);
     savePos.release(); savePrev.release(); saveVel.release();
-    int rc = GBT_BatchSetLaunch(modes[bestK][0], modes[bestK][1]);
+    G.trials = plan;
+    if (bestK < 0) { GBT_BatchSetElementTables(keepCodes ? 1 : 0); return LCS_ERR_UNSUPPORTED; }
+    const Batch::Trial& w = plan[bestK];
+    int rc = GBT_BatchSetElementTables(w.tables);
     if (rc) return rc;
-    if (modeOut) *modeOut = modes[bestK][0];
-    if (threadsOut) *threadsOut = modes[bestK][1];
+    G.packing = w.packing;
+    rc = GBT_BatchSetLaunch(w.mode, w.threads);
+    if (rc) return rc;
+    if (modeOut) *modeOut = w.mode;
+    if (threadsOut) *threadsOut = w.threads;
     CK(cudaStreamSynchronize(G.stream));
     return 0;
+}
+
+// The last autotune's trials: up to `capacity` rows of (mode, threads, packing, element tables) in
+// shape4 and their ms per frame (-1: the configuration cannot run this batch); returns the number of
+// trials.
+LCS_API int GBT_BatchAutotuneTable(int capacity, int* shape4, float* ms) {
+    if (!G.ready || capacity < 0 || (capacity > 0 && (!shape4 || !ms))) return XPBD_ERR_BAD_ARG;
+    const int n = (int)G.trials.size();
+    for (int k = 0; k < n && k < capacity; k++) {
+        const Batch::Trial& t = G.trials[k];
+        shape4[4 * k] = t.mode; shape4[4 * k + 1] = t.threads; shape4[4 * k + 2] = t.packing; shape4[4 * k + 3] = t.tables;
+        ms[k] = t.ms;
+    }
+    return n;
 }
 
 LCS_API void GBT_BatchProfileEnable(int enabled) {

@@ -224,9 +224,20 @@ LCS_API int GBT_BatchInfo(int* counts8);                               /* instan
  * 2 one thread-block cluster per instance list with positions in distributed shared memory
  * (`threads` = CTAs per cluster: 2 | 4 | 8; -4001 when the largest instance does not fit). */
 LCS_API int GBT_BatchSetLaunch(int mode, int threads);
-/* Times the six shapes {0/256, 1/256, 1/512, 2/2, 2/4, 2/8} and keeps the fastest; msPerFrame6 gets
- * each one's ms per frame (-1: not usable for this batch). */
+/* Instance packing of the shapes that give an instance to one CTA or cluster (modes 1, 2): 0 longest
+ * processing time first on tet counts (the default), 1 the same on tets + edges + nodes, 2 instances
+ * in decreasing size dealt round-robin in serpentine order.  Identical results in every packing. */
+LCS_API int GBT_BatchSetPacking(int packing);
+LCS_API int GBT_BatchPacking(void);
+/* Times every configuration for trialSteps frames from the current state (put back afterwards) and
+ * keeps the fastest: the lockstep grid on each element-table form, one CTA per instance at 256 and
+ * 512 threads and clusters of 2, 4 and 8 CTAs, each with the three packings.  msPerFrame6 gets the
+ * best ms per frame of each shape {0/256, 1/256, 1/512, 2/2, 2/4, 2/8} (-1: not usable for this
+ * batch).  GBT_BatchAutotuneTable copies up to `capacity` trials -- (mode, threads, packing,
+ * implicit element tables) in shape4, ms per frame in ms (-1: not usable) -- and returns how many
+ * the last autotune ran. */
 LCS_API int GBT_BatchAutotune(float dt, int trialSteps, int* modeOut, int* threadsOut, float* msPerFrame6);
+LCS_API int GBT_BatchAutotuneTable(int capacity, int* shape4, float* ms);
 /* Element tables of the frame kernels: 1 implicit lattice codes -- 4 bytes per tet and per edge (plus
  * the edge rest length), nodes and compliances derived from the instance's lattice strides and
  * Kuhn type -- used by default when every instance qualifies (instances of < 32,768 nodes, fewer

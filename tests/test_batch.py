@@ -85,6 +85,33 @@ def test_autotune_keeps_state(gpu_lib, small_batch):
         assert len(choice["ms_per_frame"]) == 6 and all(ms > 0 or ms == -1 for ms in choice["ms_per_frame"])
         assert all(ms > 0 for ms in choice["ms_per_frame"][:3])
         assert np.array_equal(b.positions(), before)
+        # the search: lockstep on both element-table forms, every per-instance shape with three packings
+        trials = choice["trials"]
+        assert len(trials) == 2 + 2 * 3 + 3 * 3
+        assert {(t["mode"], t["threads"], t["packing"]) for t in trials if t["mode"] > 0} == \
+            {(m, th, pk) for m, ths in ((1, (256, 512)), (2, (2, 4, 8))) for th in ths for pk in range(3)}
+        usable = [t for t in trials if t["ms_per_frame"] > 0]
+        fastest = min(usable, key=lambda t: t["ms_per_frame"])
+        assert (choice["mode"], choice["threads"], choice["element_tables"]) == (fastest["mode"], fastest["threads"], fastest["element_tables"])
+        assert choice["mode"] == 0 or choice["packing"] == fastest["packing"]
+
+
+@pytest.mark.parametrize("mode,threads,packing", [(1, 256, 1), (1, 512, 2), (2, 4, 1), (2, 2, 2)])
+def test_packings_match_lockstep(gpu_lib, small_batch, mode, threads, packing):
+    """Every instance packing advances every instance exactly as the lockstep grid does."""
+    runs = []
+    for m, th, pk in ((0, 256, 0), (mode, threads, packing)):
+        with BT.TissueBatch(small_batch.grids, dt=1 / 60, substeps=small_batch.substeps, ks=1e6,
+                            stiffness_scale=small_batch.stiffness_scale(), grasp_params=GraspParams(**GRASP), dll_path=gpu_lib) as b:
+            b.set_packing(pk)
+            b.set_launch(m, th)
+            assert b.packing() == pk
+            b.set_gravity(0.0, -981.0, 0.0)
+            b.set_capsules(small_batch.capsules_at(0))
+            for k in range(STEPS):
+                b.step_many([small_batch.capsules_at(k + 1)], use_graph=k % 2 == 0)
+            runs.append(b.positions())
+    assert np.array_equal(runs[0], runs[1])
 
 
 def test_graph_follows_grasp_param_changes(gpu_lib, small_batch):
