@@ -626,33 +626,49 @@ def frames_measurement(lib, calls=50, warmup=3):
             "nodes_per_s": nodes / (ms / 1e3), "timing": f"wall clock around GBT_ComputeParticleFrames, median of {calls}"}
 
 
-def cut_topology_measurement(lib, frames=30, calls=10, warmup=2):
-    """The cut topology of the C3 lattice after `frames` blade frames (GBT_CutTopologyBuild: live
-    tets, vertex duplication, greedy re-colouring relaxed on the device): wall clock per build
-    (launches + the copies of its counts), median.  Returns the section and the neighbour table it
-    was built from (the CPU baseline leg times the oracle on the same table)."""
+def cut_topology_measurement(lib, frames=30, warmup=2):
+    """The cut topology of the C3 lattice (GBT_CutTopologyBuild: live tets, vertex duplication,
+    greedy re-colouring relaxed on the device).  One build before the blade (the session's tables;
+    nothing cut), `frames` blade frames, then the first build after them (the relaxation starts from
+    the uncut colouring, so every change since the start travels), then `frames` more frames with a
+    build after every step (each relaxation starts from the previous step's colouring).  Wall clock
+    around the builds and the steps.  Returns the section and the neighbour table of the first build
+    after the blade (the CPU baseline leg times the oracle on it)."""
     import ctypes
 
     from genesis_tissue_simulation_gb300 import workloads as W
 
-    w = W.make("c3", steps=frames)
+    w = W.make("c3", steps=2 * frames + warmup)
     s = w.open(lib)
     counts = np.zeros(4, dtype=np.int32)
+    build = lambda: s.check("GBT_CutTopologyBuild", counts.ctypes.data_as(ctypes.c_void_p))
     try:
+        build()
         w.run(s, steps=frames)
-        times = []
-        for k in range(calls + warmup):
-            t0 = time.perf_counter()
-            s.check("GBT_CutTopologyBuild", counts.ctypes.data_as(ctypes.c_void_p))
-            if k >= warmup:
-                times.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        build()
+        first_ms = 1e3 * (time.perf_counter() - t0)
+        first = counts.copy()
         nbr = s.neighbors()
+        w.run(s, steps=warmup, start=frames)
+        build()
+        step_ms, build_ms, sweeps = [], [], []
+        for k in range(frames + warmup, 2 * frames + warmup):
+            t0 = time.perf_counter()
+            s.step(detect_cut=w.command(s, k))
+            t1 = time.perf_counter()
+            build()
+            t2 = time.perf_counter()
+            step_ms.append(1e3 * (t1 - t0)); build_ms.append(1e3 * (t2 - t1)); sweeps.append(int(counts[3]))
     finally:
         s.close()
-    out = {"workload": f"c3 blade workload after {frames} frames, {len(w.grid.positions):,} lattice nodes",
-           "ms_per_build_wall": 1e3 * float(np.median(times)), "live_tets": int(counts[0]), "duplicated_vertices": int(counts[1]),
-           "colours": int(counts[2]), "relaxation_sweeps": int(counts[3]),
-           "timing": f"wall clock around GBT_CutTopologyBuild, median of {calls}"}
+    per_step = float(np.mean(step_ms)) + float(np.mean(build_ms))
+    out = {"workload": f"c3 blade workload, {len(w.grid.positions):,} lattice nodes",
+           "first_build_after_frames": frames, "ms_first_build_wall": first_ms, "live_tets": int(first[0]),
+           "duplicated_vertices": int(first[1]), "colours": int(first[2]), "relaxation_sweeps": int(first[3]),
+           "per_step": {"frames": frames, "ms_build_wall_mean": float(np.mean(build_ms)), "sweeps_mean": float(np.mean(sweeps)),
+                        "ms_step_wall_mean": float(np.mean(step_ms)), "steps_per_s_with_build": 1e3 / per_step},
+           "timing": "wall clock around GBT_CutTopologyBuild (and LCS_Step with the rod-phase detection), host synchronised"}
     return out, nbr
 
 
@@ -721,7 +737,7 @@ def main():
         section = (batched_measurement(lib, args.batched_frames, max(args.warmup, 3)) if args.only == "batched"
                    else finalize_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1)) if args.only == "finalize"
                    else frames_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1)) if args.only == "frames"
-                   else cut_topology_measurement(lib, calls=max(args.steps, 1), warmup=max(args.warmup, 1))[0] if args.only == "cut_topology"
+                   else cut_topology_measurement(lib, warmup=max(args.warmup, 1))[0] if args.only == "cut_topology"
                    else workload_measurement(lib, args.only, max(args.steps, 1), args.warmup, cpu_budget_s=0.0,
                                              launch_mode=args.launch_mode) if args.only in ("c1", "c3")
                    else adjoint_measurement(lib, reps=max(args.steps, 1)))

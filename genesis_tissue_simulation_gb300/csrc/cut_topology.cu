@@ -16,10 +16,12 @@
 //                  duplicated vertices: in emission order each tet takes the smallest colour that no
 //                  earlier tet sharing one of its vertices holds.  This is computed in parallel as
 //                  the fixed point of c(t) = mex{c(u) : u earlier than t, u shares a vertex with t},
-//                  relaxed in place from the bind-time colours until a whole sweep changes nothing.
-//                  The recurrence has exactly one solution (induction over emission order), so the
-//                  result is the sequential colouring whatever order the sweeps ran in.  With nothing
-//                  cut it is the bind-time colouring itself.
+//                  relaxed in place until a whole sweep changes nothing, starting from each tet's
+//                  colour in the previous build (the bind-time colour before the first).  The
+//                  recurrence has exactly one solution (induction over emission order), so the result
+//                  is the sequential colouring whatever the start and the order of the sweeps; the
+//                  start only decides how far changes travel, so a build after every step of cutting
+//                  relaxes just that step's changes.  With nothing cut it is the bind-time colouring.
 //
 // The CPU restatement (oracle/cut_topology_oracle.inc) computes the same product sequentially.
 #include <algorithm>
@@ -56,7 +58,7 @@ struct CutTopologyState {
     unsigned long long generation = 0;       // session the tables below describe
     int N = 0, T = 0, keys = 0;
     DBuf<int> slotOfKey, storageOfSlot;      // key -> colour slot (-1: no tet); colour slot -> storage index
-    DBuf<unsigned char> colourOfSlot;        // bind-time colour of each colour slot
+    DBuf<unsigned char> keyColour;           // each key's colour in the last build (bind-time before the first)
     DBuf<int> liveKey, rankOfKey, groupCount, dupBase, blockSums, totals;
     DBuf<unsigned char> groupOf;             // [keys][4]: group of the tet at each corner node
     DBuf<int> tetNodes, tetSource, dupParent, nbrCount, nbrOff, nbrList, upCount, upOff, upList;
@@ -73,12 +75,13 @@ __host__ __device__ __forceinline__ int cornerPosition(int type, unsigned corner
 }
 
 // ---- session tables -------------------------------------------------------------------------
-__global__ void slotTableKernel(DeviceMesh m, int T, int* slotOfKey, unsigned char* colourOfSlot) {
+__global__ void slotTableKernel(DeviceMesh m, int T, int* slotOfKey, unsigned char* keyColour) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < T; k += gridDim.x * blockDim.x) {
-        slotOfKey[6 * m.tetIds[k].x + (m.tetMeta[k] & 7)] = k;
+        const int key = 6 * m.tetIds[k].x + (m.tetMeta[k] & 7);
+        slotOfKey[key] = k;
         int c = 0;
         while (c + 1 < m.nTetColors && k >= m.tetRange[c].y) c++;
-        colourOfSlot[k] = (unsigned char)c;
+        keyColour[key] = (unsigned char)c;   // the bind-time colour
     }
 }
 
@@ -214,7 +217,7 @@ __device__ __forceinline__ int vertexOf(int node, int group, int N, const int* d
     return group == 0 ? node : N + dupBase[node] + group - 1;
 }
 __global__ void emitKernel(int keys, int N, int nx, int nxy, const int* liveKey, const int* rankOfKey, const int* slotOfKey,
-                           const int* storageOfSlot, const unsigned char* colourOfSlot, const unsigned char* groupOf,
+                           const int* storageOfSlot, const unsigned char* keyColour, const unsigned char* groupOf,
                            const int* dupBase, int* tetNodes, int* tetSource, unsigned char* colour) {
     for (int key = blockIdx.x * blockDim.x + threadIdx.x; key < keys; key += gridDim.x * blockDim.x) {
         if (!liveKey[key]) continue;
@@ -223,8 +226,16 @@ __global__ void emitKernel(int keys, int N, int nx, int nxy, const int* liveKey,
         const int node[4] = {d.x, d.y, d.z, d.w};
         for (int k = 0; k < 4; k++) tetNodes[4 * (size_t)r + k] = vertexOf(node[k], groupOf[4 * (size_t)key + k], N, dupBase);
         tetSource[r] = storageOfSlot[slot];
-        colour[r] = colourOfSlot[slot];   // the relaxation starts from the bind-time colouring
+        // the relaxation starts from the tet's colour in the previous build (the bind-time colour
+        // before the first): its fixed point does not depend on the start, and after one more step
+        // of cutting only the changes since that build have to travel
+        colour[r] = keyColour[key];
     }
+}
+__global__ void keepColoursKernel(int keys, const int* liveKey, const int* rankOfKey, const unsigned char* colour,
+                                  unsigned char* keyColour) {
+    for (int key = blockIdx.x * blockDim.x + threadIdx.x; key < keys; key += gridDim.x * blockDim.x)
+        if (liveKey[key]) keyColour[key] = colour[rankOfKey[key]];
 }
 __global__ void dupParentKernel(int N, const int* groupCount, const int* dupBase, int* dupParent) {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x)
@@ -335,10 +346,10 @@ int build(const SessionView& v) {
     auto blocks = [&](long long n) { return (int)std::max(1LL, std::min<long long>((n + kThreads - 1) / kThreads, 16LL * v.smCount)); };
     if (C.generation != v.generation || C.N != N || C.T != T) {   // per-session tables
         C.built = false;
-        CT_CK(C.slotOfKey.ensure(keys)); CT_CK(C.colourOfSlot.ensure(T)); CT_CK(C.storageOfSlot.ensure(T));
+        CT_CK(C.slotOfKey.ensure(keys)); CT_CK(C.keyColour.ensure(keys)); CT_CK(C.storageOfSlot.ensure(T));
         CT_CK(cudaMemsetAsync(C.slotOfKey.p, 0xFF, (size_t)keys * sizeof(int), s));
         CT_CK(cudaMemcpyAsync(C.storageOfSlot.p, v.tetColorOrder, (size_t)T * sizeof(int), cudaMemcpyHostToDevice, s));
-        if (T > 0) slotTableKernel<<<blocks(T), kThreads, 0, s>>>(m, T, C.slotOfKey.p, C.colourOfSlot.p);
+        if (T > 0) slotTableKernel<<<blocks(T), kThreads, 0, s>>>(m, T, C.slotOfKey.p, C.keyColour.p);
         CT_CK(cudaGetLastError());
         CT_CK(cudaStreamSynchronize(s));   // the host table copied above is the session's, valid now
         C.generation = v.generation; C.N = N; C.T = T; C.keys = keys;
@@ -358,7 +369,7 @@ int build(const SessionView& v) {
     CT_CK(C.tetNodes.ensure((size_t)4 * L)); CT_CK(C.tetSource.ensure(L)); CT_CK(C.colour.ensure(L)); CT_CK(C.dupParent.ensure(D));
     CT_CK(C.nbrCount.ensure(L)); CT_CK(C.nbrOff.ensure((size_t)L + 1));
     emitKernel<<<blocks(keys), kThreads, 0, s>>>(keys, N, nx, nx * ny, C.liveKey.p, C.rankOfKey.p, C.slotOfKey.p, C.storageOfSlot.p,
-                                                  C.colourOfSlot.p, C.groupOf.p, C.dupBase.p, C.tetNodes.p, C.tetSource.p, C.colour.p);
+                                                  C.keyColour.p, C.groupOf.p, C.dupBase.p, C.tetNodes.p, C.tetSource.p, C.colour.p);
     dupParentKernel<<<blocks(N), kThreads, 0, s>>>(N, C.groupCount.p, C.dupBase.p, C.dupParent.p);
     neighbourKernel<<<blocks(keys), kThreads, 0, s>>>(keys, nx, ny, m.dx, m.dy, m.dz, C.liveKey.p, C.rankOfKey.p, C.groupOf.p,
                                                        C.nbrCount.p, nullptr, nullptr);
@@ -400,6 +411,8 @@ int build(const SessionView& v) {
         if (h[1] != 0u) return LCS_ERR_DEVICE_TIMEOUT;
         sweeps = h[5]; overflow = h[6];
         if (overflow || sweeps > (unsigned)L + 1u) return XPBD_ERR_COLOR_OVERFLOW;
+        keepColoursKernel<<<blocks(keys), kThreads, 0, s>>>(keys, C.liveKey.p, C.rankOfKey.p, C.colour.p, C.keyColour.p);
+        CT_CK(cudaGetLastError());
     }
     // colour count: the largest colour + 1 (read back with the colours by the getter)
     std::vector<unsigned char> host(L);
@@ -418,7 +431,7 @@ int build(const SessionView& v) {
 void releaseCutTopology() {
     for (auto* b : {&C.slotOfKey, &C.storageOfSlot, &C.liveKey, &C.rankOfKey, &C.groupCount, &C.dupBase, &C.blockSums, &C.totals,
                     &C.tetNodes, &C.tetSource, &C.dupParent, &C.nbrCount, &C.nbrOff, &C.nbrList, &C.upCount, &C.upOff, &C.upList}) b->release();
-    C.colourOfSlot.release(); C.groupOf.release(); C.colour.release(); C.marks.release(); C.sync.release();
+    C.keyColour.release(); C.groupOf.release(); C.colour.release(); C.marks.release(); C.sync.release();
     C.generation = 0; C.built = false; C.live = C.duplicates = C.colours = C.sweeps = 0;
 }
 

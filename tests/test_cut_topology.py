@@ -221,3 +221,29 @@ def test_cuda_matches_oracle_on_blade_workload(gpu_lib, oracle_libs, scale, fram
     with open(results_dir() / "cut_topology.jsonl", "a") as f:
         f.write(json.dumps(dict(scale=scale, frames=frames, live=len(gpu["tet_source"]), duplicates=len(gpu["dup_parent"]),
                                 colours=gpu["colours"], sweeps=gpu["sweeps"], recoloured=changed)) + "\n")
+
+
+@pytest.mark.gpu
+def test_cuda_rebuilt_every_step_matches_oracle(gpu_lib, oracle_libs):
+    """Built after every step of the blade workload, each relaxation starting from the previous
+    step's colouring: at every fifth step the product equals the oracle's sequential build on the
+    same topology, and the last equals a single build of the same topology from the uncut colouring
+    (the fixed point does not depend on the start; the sweeps each took are recorded)."""
+    w = W.make("c3", scale=SMALL_C3, steps=40)
+    sweeps = []
+    with w.open(dll_path=gpu_lib) as s, w.open(dll_path=oracle_libs[0]) as o:
+        s.cut_topology()
+        for k in range(40):
+            s.step(detect_cut=w.command(s, k))
+            gpu = s.cut_topology()
+            sweeps.append(gpu["sweeps"])
+            if k % 5 == 4:
+                set_topology(o, s.neighbors())
+                assert_same(gpu, o.cut_topology())
+        assert s.topology_revision() > 0
+    with w.open(dll_path=gpu_lib) as fresh:     # the same topology from the uncut colouring in one build
+        w.run(fresh, steps=40)
+        scratch = fresh.cut_topology()
+    assert_same(gpu, scratch)
+    with open(results_dir() / "cut_topology.jsonl", "a") as f:
+        f.write(json.dumps(dict(per_step_sweeps=sweeps, from_uncut_sweeps=scratch["sweeps"])) + "\n")
