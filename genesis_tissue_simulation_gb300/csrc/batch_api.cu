@@ -61,6 +61,7 @@ struct Batch {
     // per-instance per-type stiffness and compliances; `useCodes` selects them over the explicit tables
     Buf<unsigned> tetCode, edgeCode; Buf<int4> instGeo; Buf<float2> instStiff, instAlpha;
     bool codesAvailable = false, useCodes = false;
+    Buf<int> mobile;                                 // nodes of positive inverse mass (lockstep node passes)
     Buf<ContactFrame> frames;
     unsigned* hostStatus = nullptr;
     ContactFrame* framesHost = nullptr; size_t framesHostCap = 0;
@@ -95,6 +96,7 @@ void releaseAll() {
     G.derived.release(); G.state.release(); G.frames.release(); G.bounds.release();
     G.tetCode.release(); G.edgeCode.release(); G.instGeo.release(); G.instStiff.release(); G.instAlpha.release();
     G.codesAvailable = G.useCodes = false;
+    G.mobile.release();
     if (G.framesHost) cudaFreeHost(G.framesHost);
     G.framesHost = nullptr; G.framesHostCap = 0;
     G.packedXyz.release();
@@ -169,6 +171,7 @@ DeviceMesh batchMesh() {
     std::memcpy(m.typeB, G.typeB, sizeof(G.typeB));
     m.bounds = G.bounds.p;
     if (G.useCodes) { m.tetCode = G.tetCode.p; m.edgeCode = G.edgeCode.p; m.instGeo = G.instGeo.p; m.instAlpha = G.instAlpha.p; }
+    if (G.mode == 0) { m.mobile = G.mobile.p; m.nMobile = (int)G.mobile.n; }   // the per-instance shapes sweep their ranges
     return m;
 }
 
@@ -549,6 +552,12 @@ LCS_API int GBT_BatchInit(int count, const GbtInstanceDesc* inst, const GbtBatch
     std::vector<unsigned> derived(count, ~0u), state(4, 0u);
     state[0] = ~0u;
     CK(G.pos.upload(pos.data(), G.N, G.stream)); CK(G.prev.upload(pos.data(), G.N, G.stream));
+    {   // prev starts equal to pos and vel at zero (below), so a node of inverse mass 0 never changes
+        std::vector<int> mob;
+        for (int i = 0; i < G.N; i++) if (pos[i].w > 0.f) mob.push_back(i);
+        CK(G.mobile.upload(mob.data(), mob.size(), G.stream));
+        G.mobile.n = mob.size();
+    }
     CK(G.packedXyz.alloc((size_t)3 * G.N));
     CK(G.vel.upload(zero4.data(), G.N, G.stream)); CK(G.ext.upload(ext.data(), G.N, G.stream));
     CK(G.pinned.upload(pinned.data(), G.N, G.stream)); CK(G.active.upload(active.data(), G.N, G.stream));

@@ -467,7 +467,15 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         const int nodeEnd = m.nodeBase + m.nNodes;
         // -- predict (k_predict), unless the previous substep's velocity pass already did it --
         // With Ahead a thread takes its nodes two at a time, both nodes' loads ahead of either's stores.
-        if (!predicted)
+        if (!predicted && Codes && m.mobile) {
+            for (int q = r; q < m.nMobile; q += R) {
+                const int i = m.mobile[q];
+                float4 Pi = posRef<Dsm>(m, i);
+                const float4 Vi = m.vel[i], Fi = m.ext[i];
+                if (stale) Pi.w = nodeInvMass(m, i);
+                predictNode<Dsm>(m, i, Pi, xyz(Vi), Fi, fc.h);
+            }
+        } else if (!predicted)
             for (int i = m.nodeBase + r; i < nodeEnd; i += (Ahead ? 2 : 1) * R) {
                 const int j = Ahead ? i + R : nodeEnd;
                 float4 Pi = posRef<Dsm>(m, i), Vi = m.vel[i], Fi = m.ext[i], Pj, Vj, Fj;
@@ -593,6 +601,14 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
             if (predicted) predictNode<Dsm>(m, i, P, v, F, fc.h);
             else if (touch) posRef<Dsm>(m, i) = P;
         };
+        if (Codes && m.mobile) {
+            for (int q = r; q < m.nMobile; q += R) {
+                const int i = m.mobile[q];
+                const float4 Pi = posRef<Dsm>(m, i), Qi = m.prev[i];
+                const float4 Vi = touch ? m.vel[i] : make_float4(0.f, 0.f, 0.f, 0.f), Fi = predicted ? m.ext[i] : Vi;
+                velocityNode(i, Pi, Qi, Vi, Fi);
+            }
+        } else
         for (int i = m.nodeBase + r; i < nodeEnd; i += (Ahead ? 2 : 1) * R) {
             const int j = Ahead ? i + R : nodeEnd;
             const float4 Pi = posRef<Dsm>(m, i), Qi = m.prev[i];

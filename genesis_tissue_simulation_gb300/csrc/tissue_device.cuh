@@ -71,6 +71,10 @@ struct DeviceMesh {
     // (instAlpha[6 i + type]).  Every node of a tet or edge follows from the code, so a colour sweep
     // streams 4 B per element besides the edge rest lengths.
     unsigned* tetCode; unsigned* edgeCode; const int4* instGeo; const float2* instAlpha;
+    // Batched lockstep grid: the nodes with a positive inverse mass, the only ones a node pass
+    // changes (a node of inverse mass 0 keeps its position, substep-start position and zero velocity
+    // from the start), so predict and velocity sweep this list; null: every node of the range.
+    const int* mobile; int nMobile;
 };
 
 // Corners a, b of Kuhn type t on its path 0 -> a -> b -> 7 (kKuhn in mesh_build.cu), 3 bits each,
