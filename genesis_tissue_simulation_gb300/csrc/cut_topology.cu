@@ -61,9 +61,10 @@ struct CutTopologyState {
     DBuf<unsigned char> keyColour;           // each key's colour in the last build (bind-time before the first)
     DBuf<int> liveKey, rankOfKey, groupCount, dupBase, blockSums, totals;
     DBuf<unsigned char> groupOf;             // [keys][4]: group of the tet at each corner node
-    DBuf<int> tetNodes, tetSource, dupParent, nbrCount, nbrOff, nbrList, upCount, upOff, upList;
+    DBuf<int> tetNodes, tetSource, dupParent;
+    DBuf<int> nbrCount, nbrRows, upCount, upRows;   // per live tet: earlier / later neighbours, kRow-entry rows
     DBuf<unsigned char> colour, marks;
-    DBuf<unsigned> sync;                     // relaxation kernel: [0] barrier counter, [1] status, [2..4] change counters, [5] sweeps, [6] overflow
+    DBuf<unsigned> sync;                     // relaxation kernel: [0] barrier counter, [1] status, [2..4] change counters, [5] sweeps, [6] overflow; [7] largest colour
     int live = 0, duplicates = 0, colours = 0, sweeps = 0;
     bool built = false;
 } C;
@@ -233,57 +234,67 @@ __global__ void emitKernel(int keys, int N, int nx, int nxy, const int* liveKey,
     }
 }
 __global__ void keepColoursKernel(int keys, const int* liveKey, const int* rankOfKey, const unsigned char* colour,
-                                  unsigned char* keyColour) {
+                                  unsigned char* keyColour, unsigned* largest) {
+    unsigned most = 0u;
     for (int key = blockIdx.x * blockDim.x + threadIdx.x; key < keys; key += gridDim.x * blockDim.x)
-        if (liveKey[key]) keyColour[key] = colour[rankOfKey[key]];
+        if (liveKey[key]) {
+            const unsigned char c = colour[rankOfKey[key]];
+            keyColour[key] = c;
+            most = max(most, (unsigned)c);
+        }
+    most = __reduce_max_sync(0xffffffffu, most);
+    if ((threadIdx.x & 31) == 0) atomicMax(largest, most);
 }
 __global__ void dupParentKernel(int N, const int* groupCount, const int* dupBase, int* dupParent) {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x)
         for (int j = 0; j < groupCount[v]; j++) dupParent[dupBase[v] + j] = v;
 }
 
-// Earlier live tets sharing a vertex with the tet of `key` (rank r): around each of its corners,
-// the tets of the same group.  Pass 1 counts (nbrOff == nullptr), pass 2 writes ranks at nbrOff[r].
+// Neighbours of every live tet that share one of its (duplicated) vertices, in one pass: the
+// earlier ones in emission order into its row of nbrRows (they decide its colour), the later ones
+// into its row of upRows (they are re-evaluated when its colour changes).  A tet sharing an edge or
+// a face appears once per shared vertex; the colour masks and the marks built from the rows are
+// idempotent, so the rows are not deduplicated.  A row holds at most 4 x (kMaxAround - 1) entries.
+// Around each corner the candidates (8 cells, the Kuhn types of each that hold the corner) are
+// unrolled, their liveness, group and rank loaded together.
+constexpr int kRow = 4 * kMaxAround;
 __global__ void neighbourKernel(int keys, int nx, int ny, int dx, int dy, int dz, const int* liveKey, const int* rankOfKey,
-                                const unsigned char* groupOf, int* nbrCount, const int* nbrOff, int* nbrList) {
+                                const unsigned char* groupOf, int* nbrCount, int* nbrRows, int* upCount, int* upRows) {
     const int nxy = nx * ny;
     for (int key = blockIdx.x * blockDim.x + threadIdx.x; key < keys; key += gridDim.x * blockDim.x) {
         if (!liveKey[key]) continue;
         const int r = rankOfKey[key];
         const int4 d = kuhnNodes(key % 6, key / 6, nx, nxy);
         const int node[4] = {d.x, d.y, d.z, d.w};
-        int found[4 * kMaxAround];
-        int count = 0;
+        int* down = nbrRows + (size_t)r * kRow;
+        int* up = upRows + (size_t)r * kRow;
+        int nd = 0, nu = 0;
         for (int k = 0; k < 4; k++) {
+            const int v = node[k];
             const unsigned char g = groupOf[4 * (size_t)key + k];
-            Around a;
-            liveAround(node[k], nx, ny, dx, dy, dz, liveKey, a);
-            for (int i = 0; i < a.count; i++) {
-                if (a.key[i] >= key || groupOf[4 * (size_t)a.key[i] + a.corner[i]] != g) continue;
-                const int u = rankOfKey[a.key[i]];
-                bool seen = false;
-                for (int q = 0; q < count && !seen; q++) seen = found[q] == u;
-                if (!seen) found[count++] = u;
+            const int vx = v % nx, vy = (v / nx) % ny, vz = v / nxy;
+#pragma unroll
+            for (int c = 7; c >= 0; c--) {
+                const int cx = vx - (c & 1), cy = vy - ((c >> 1) & 1), cz = vz - ((c >> 2) & 1);
+                const bool inside = cx >= 0 && cy >= 0 && cz >= 0 && cx < dx && cy < dy && cz < dz;
+                const int u = v - cornerOffset((unsigned)c, nx, nxy);
+#pragma unroll
+                for (int t = 0; t < 6; t++) {
+                    const int pos = cornerPosition(t, (unsigned)c);
+                    if (pos < 0) continue;
+                    const int kk = 6 * u + t;
+                    const int live = inside ? liveKey[kk] : 0;
+                    const unsigned char gg = inside ? groupOf[4 * (size_t)kk + pos] : (unsigned char)0xFF;
+                    const int rank = inside ? rankOfKey[kk] : 0;
+                    if (!live || kk == key || gg != g) continue;
+                    if (kk < key) down[nd++] = rank;
+                    else up[nu++] = rank;
+                }
             }
         }
-        if (!nbrOff) { nbrCount[r] = count; continue; }
-        int* out = nbrList + nbrOff[r];
-        for (int q = 0; q < count; q++) out[q] = found[q];
+        nbrCount[r] = nd;
+        upCount[r] = nu;
     }
-}
-
-// Later neighbours (the reverse of the earlier-neighbour lists): counts, then positions by atomic
-// cursors (their order is irrelevant: they only mark tets for re-evaluation).
-__global__ void upperCountKernel(int L, const int* nbrOff, const int* nbrList, int* upCount) {
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < L; t += gridDim.x * blockDim.x)
-        for (int j = nbrOff[t]; j < nbrOff[t + 1]; j++) atomicAdd(upCount + nbrList[j], 1);
-}
-__global__ void upperFillKernel(int L, const int* nbrOff, const int* nbrList, const int* upOff, int* upCursor, int* upList) {
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < L; t += gridDim.x * blockDim.x)
-        for (int j = nbrOff[t]; j < nbrOff[t + 1]; j++) {
-            const int u = nbrList[j];
-            upList[upOff[u] + atomicAdd(upCursor + u, 1)] = t;
-        }
 }
 
 // In-place relaxation of c(t) = mex{c(u) : u in t's earlier neighbours} over the whole grid, one
@@ -294,8 +305,26 @@ __global__ void upperFillKernel(int L, const int* nbrOff, const int* nbrList, co
 // arrays by sweep parity.  Change counters rotate over three words: sweep s counts into word s % 3,
 // every block reads it after the sweep's barrier, and block 0 clears word (s + 1) % 3 during sweep
 // s (its last reader finished before the previous barrier).
-__global__ void __launch_bounds__(kThreads) recolourKernel(int L, const int* nbrOff, const int* nbrList, const int* upOff,
-                                                          const int* upList, unsigned char* colour, unsigned char* marks,
+// A sweep lasts as long as its slowest thread, whose evaluations are chains of dependent loads (row
+// entry, then the colour it names).  Tets are dealt to threads with the grid's stride, which spreads
+// the marks (clustered in emission order around the cut) over the grid; a thread reads its kBatch
+// marks together and every row kBatch entries at a time, so an evaluation is a few round trips.
+constexpr int kBatch = 16;
+static_assert(kRow % kBatch == 0, "a batch never runs past its row");
+// kBatch entries of a row from `p` (16-byte aligned: rows are kRow ints, batches start at multiples
+// of kBatch), the first `valid` of them kept and the rest -1.
+__device__ __forceinline__ void loadRowBatch(const int* p, int valid, int (&out)[kBatch]) {
+#pragma unroll
+    for (int q = 0; q < kBatch / 4; q++) {
+        const int4 v = reinterpret_cast<const int4*>(p)[q];
+        out[4 * q] = 4 * q < valid ? v.x : -1;
+        out[4 * q + 1] = 4 * q + 1 < valid ? v.y : -1;
+        out[4 * q + 2] = 4 * q + 2 < valid ? v.z : -1;
+        out[4 * q + 3] = 4 * q + 3 < valid ? v.w : -1;
+    }
+}
+__global__ void __launch_bounds__(kThreads) recolourKernel(int L, const int* nbrCount, const int* nbrRows, const int* upCount,
+                                                          const int* upRows, unsigned char* colour, unsigned char* marks,
                                                           unsigned* sync, long long budget, int maxSweeps) {
     GridSync g{sync, sync + 1, gridDim.x, 0u, budget, 0u};
     const int R = gridDim.x * blockDim.x, r0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -305,20 +334,44 @@ __global__ void __launch_bounds__(kThreads) recolourKernel(int L, const int* nbr
         unsigned char* cur = marks + (size_t)(s & 1) * L;
         unsigned char* next = marks + (size_t)((s + 1) & 1) * L;
         bool changed = false;
-        for (int t = r0; t < L; t += R) {
-            if (!cur[t]) continue;
-            cur[t] = 0;
-            unsigned long long m0 = 0ull, m1 = 0ull;
-            for (int j = nbrOff[t]; j < nbrOff[t + 1]; j++) {
-                const unsigned c = col[nbrList[j]];
-                if (c < 64u) m0 |= 1ull << c; else m1 |= 1ull << (c - 64u);
-            }
-            const int mex = ~m0 ? __ffsll((long long)~m0) - 1 : (~m1 ? 64 + __ffsll((long long)~m1) - 1 : kMaxColours);
-            if (mex >= kMaxColours) { atomicOr(sync + 6, 1u); continue; }
-            if (mex != col[t]) {
+        for (long long t0 = r0; t0 < L; t0 += (long long)kBatch * R) {
+            unsigned marked = 0u;
+#pragma unroll
+            for (int u = 0; u < kBatch; u++)
+                if (t0 + (long long)u * R < L && cur[t0 + (long long)u * R]) marked |= 1u << u;
+            for (; marked; marked &= marked - 1u) {
+                const int t = (int)(t0 + (long long)(__ffs((int)marked) - 1) * R);
+                cur[t] = 0;
+                const int* nbrList = nbrRows + (size_t)t * kRow;
+                const int e = nbrCount[t];
+                const unsigned own = col[t];
+                unsigned long long m0 = 0ull, m1 = 0ull;
+                for (int j = 0; j < e; j += kBatch) {
+                    int nb[kBatch];
+                    loadRowBatch(nbrList + j, e - j, nb);
+                    unsigned c[kBatch];
+#pragma unroll
+                    for (int q = 0; q < kBatch; q++) c[q] = nb[q] >= 0 ? (unsigned)col[nb[q]] : 0xFFu;
+#pragma unroll
+                    for (int q = 0; q < kBatch; q++) {
+                        if (c[q] < 64u) m0 |= 1ull << c[q];
+                        else if (c[q] < 128u) m1 |= 1ull << (c[q] - 64u);
+                    }
+                }
+                const int mex = ~m0 ? __ffsll((long long)~m0) - 1 : (~m1 ? 64 + __ffsll((long long)~m1) - 1 : kMaxColours);
+                if (mex >= kMaxColours) { atomicOr(sync + 6, 1u); continue; }
+                if ((unsigned)mex == own) continue;
                 col[t] = (unsigned char)mex;
                 changed = true;
-                for (int j = upOff[t]; j < upOff[t + 1]; j++) next[upList[j]] = 1;
+                const int* upList = upRows + (size_t)t * kRow;
+                const int ue = upCount[t];
+                for (int j = 0; j < ue; j += kBatch) {
+                    int up[kBatch];
+                    loadRowBatch(upList + j, ue - j, up);
+#pragma unroll
+                    for (int q = 0; q < kBatch; q++)
+                        if (up[q] >= 0) next[up[q]] = 1;
+                }
             }
         }
         if (__syncthreads_or(changed) && threadIdx.x == 0) atomicAdd(sync + 2 + s % 3, 1u);
@@ -360,38 +413,24 @@ int build(const SessionView& v) {
     CT_CK(cudaGetLastError());
     int rc = exclusiveScan(C.liveKey.p, C.rankOfKey.p, keys, C.totals.p, s);
     if (rc) return rc;
-    int L = 0, D = 0, E = 0;
+    int L = 0, D = 0;
     if ((rc = readTotal(&L, s))) return rc;
     groupKernel<<<blocks(N), kThreads, 0, s>>>(N, nx, ny, m.dx, m.dy, m.dz, C.liveKey.p, C.groupOf.p, C.groupCount.p);
     CT_CK(cudaGetLastError());
     if ((rc = exclusiveScan(C.groupCount.p, C.dupBase.p, N, C.totals.p, s))) return rc;
     if ((rc = readTotal(&D, s))) return rc;
     CT_CK(C.tetNodes.ensure((size_t)4 * L)); CT_CK(C.tetSource.ensure(L)); CT_CK(C.colour.ensure(L)); CT_CK(C.dupParent.ensure(D));
-    CT_CK(C.nbrCount.ensure(L)); CT_CK(C.nbrOff.ensure((size_t)L + 1));
+    CT_CK(C.nbrCount.ensure(L)); CT_CK(C.nbrRows.ensure((size_t)kRow * L)); CT_CK(C.upCount.ensure(L)); CT_CK(C.upRows.ensure((size_t)kRow * L));
     emitKernel<<<blocks(keys), kThreads, 0, s>>>(keys, N, nx, nx * ny, C.liveKey.p, C.rankOfKey.p, C.slotOfKey.p, C.storageOfSlot.p,
                                                   C.keyColour.p, C.groupOf.p, C.dupBase.p, C.tetNodes.p, C.tetSource.p, C.colour.p);
     dupParentKernel<<<blocks(N), kThreads, 0, s>>>(N, C.groupCount.p, C.dupBase.p, C.dupParent.p);
     neighbourKernel<<<blocks(keys), kThreads, 0, s>>>(keys, nx, ny, m.dx, m.dy, m.dz, C.liveKey.p, C.rankOfKey.p, C.groupOf.p,
-                                                       C.nbrCount.p, nullptr, nullptr);
-    CT_CK(cudaGetLastError());
-    if ((rc = exclusiveScan(C.nbrCount.p, C.nbrOff.p, L, C.totals.p, s))) return rc;
-    if ((rc = readTotal(&E, s))) return rc;
-    CT_CK(cudaMemcpyAsync(C.nbrOff.p + L, &E, sizeof(int), cudaMemcpyHostToDevice, s));
-    CT_CK(C.nbrList.ensure(E));
-    neighbourKernel<<<blocks(keys), kThreads, 0, s>>>(keys, nx, ny, m.dx, m.dy, m.dz, C.liveKey.p, C.rankOfKey.p, C.groupOf.p,
-                                                       C.nbrCount.p, C.nbrOff.p, C.nbrList.p);
+                                                       C.nbrCount.p, C.nbrRows.p, C.upCount.p, C.upRows.p);
     CT_CK(cudaGetLastError());
     unsigned sweeps = 0, overflow = 0;
+    int colours = 0;
     if (L > 0) {
-        CT_CK(C.upCount.ensure(L)); CT_CK(C.upOff.ensure((size_t)L + 1)); CT_CK(C.upList.ensure(E)); CT_CK(C.marks.ensure((size_t)2 * L));
-        CT_CK(cudaMemsetAsync(C.upCount.p, 0, (size_t)L * sizeof(int), s));
-        upperCountKernel<<<blocks(L), kThreads, 0, s>>>(L, C.nbrOff.p, C.nbrList.p, C.upCount.p);
-        CT_CK(cudaGetLastError());
-        if ((rc = exclusiveScan(C.upCount.p, C.upOff.p, L, C.totals.p, s))) return rc;
-        CT_CK(cudaMemcpyAsync(C.upOff.p + L, &E, sizeof(int), cudaMemcpyHostToDevice, s));
-        CT_CK(cudaMemsetAsync(C.upCount.p, 0, (size_t)L * sizeof(int), s));   // now the fill cursors
-        upperFillKernel<<<blocks(L), kThreads, 0, s>>>(L, C.nbrOff.p, C.nbrList.p, C.upOff.p, C.upCount.p, C.upList.p);
-        CT_CK(cudaGetLastError());
+        CT_CK(C.marks.ensure((size_t)2 * L));
         CT_CK(cudaMemsetAsync(C.marks.p, 1, (size_t)L, s));                    // the first sweep evaluates every tet
         CT_CK(cudaMemsetAsync(C.marks.p + L, 0, (size_t)L, s));
         CT_CK(cudaMemsetAsync(C.sync.p, 0, 8 * sizeof(unsigned), s));
@@ -401,27 +440,22 @@ int build(const SessionView& v) {
         const int grid = std::max(1, std::min(std::min(perSm, 2) * v.smCount, (L + kThreads - 1) / kThreads));
         long long budget = (long long)(v.syncBudgetSeconds * 1e3 * (double)v.clockKHz);
         int Lk = L, maxSweeps = L + 1;
-        const int* off = C.nbrOff.p; const int* list = C.nbrList.p; const int* uoff = C.upOff.p; const int* ulist = C.upList.p;
+        const int* cnt = C.nbrCount.p; const int* rows = C.nbrRows.p; const int* ucnt = C.upCount.p; const int* urows = C.upRows.p;
         unsigned char* col = C.colour.p; unsigned char* mk = C.marks.p; unsigned* sy = C.sync.p;
-        void* args[] = {&Lk, &off, &list, &uoff, &ulist, &col, &mk, &sy, &budget, &maxSweeps};
+        void* args[] = {&Lk, &cnt, &rows, &ucnt, &urows, &col, &mk, &sy, &budget, &maxSweeps};
         CT_CK(cudaLaunchCooperativeKernel((const void*)recolourKernel, dim3(grid), dim3(kThreads), args, 0, s));
+        // the colours become the next build's start (any start relaxes to the same colouring) and
+        // their largest + 1 the colour count
+        keepColoursKernel<<<blocks(keys), kThreads, 0, s>>>(keys, C.liveKey.p, C.rankOfKey.p, C.colour.p, C.keyColour.p, C.sync.p + 7);
+        CT_CK(cudaGetLastError());
         unsigned h[8];
         CT_CK(cudaMemcpyAsync(h, C.sync.p, sizeof(h), cudaMemcpyDeviceToHost, s));
         CT_CK(cudaStreamSynchronize(s));
         if (h[1] != 0u) return LCS_ERR_DEVICE_TIMEOUT;
         sweeps = h[5]; overflow = h[6];
         if (overflow || sweeps > (unsigned)L + 1u) return XPBD_ERR_COLOR_OVERFLOW;
-        keepColoursKernel<<<blocks(keys), kThreads, 0, s>>>(keys, C.liveKey.p, C.rankOfKey.p, C.colour.p, C.keyColour.p);
-        CT_CK(cudaGetLastError());
+        colours = (int)h[7] + 1;
     }
-    // colour count: the largest colour + 1 (read back with the colours by the getter)
-    std::vector<unsigned char> host(L);
-    if (L > 0) {
-        CT_CK(cudaMemcpyAsync(host.data(), C.colour.p, (size_t)L, cudaMemcpyDeviceToHost, s));
-        CT_CK(cudaStreamSynchronize(s));
-    }
-    int colours = 0;
-    for (unsigned char c : host) colours = std::max(colours, (int)c + 1);
     C.live = L; C.duplicates = D; C.colours = colours; C.sweeps = (int)sweeps; C.built = true;
     return 0;
 }
@@ -430,7 +464,7 @@ int build(const SessionView& v) {
 
 void releaseCutTopology() {
     for (auto* b : {&C.slotOfKey, &C.storageOfSlot, &C.liveKey, &C.rankOfKey, &C.groupCount, &C.dupBase, &C.blockSums, &C.totals,
-                    &C.tetNodes, &C.tetSource, &C.dupParent, &C.nbrCount, &C.nbrOff, &C.nbrList, &C.upCount, &C.upOff, &C.upList}) b->release();
+                    &C.tetNodes, &C.tetSource, &C.dupParent, &C.nbrCount, &C.nbrRows, &C.upCount, &C.upRows}) b->release();
     C.keyColour.release(); C.groupOf.release(); C.colour.release(); C.marks.release(); C.sync.release();
     C.generation = 0; C.built = false; C.live = C.duplicates = C.colours = C.sweeps = 0;
 }
