@@ -1,8 +1,8 @@
-"""CUDA path against the CPU oracle on lattices at the edges of the layout: one cell, a rod of
-cells along x, a one-cell column, a one-cell-thick sheet, an odd-sized capsule block, a thin sheet
-the blade cuts through and a small cube the blade misses.  Each runs in every launch shape (whole
-GPU, one CTA, one thread-block cluster) and must match the FP32 oracle bit for bit: positions,
-velocities and, for the blade, the neighbour table and topology revision.
+"""CUDA path against the CPU oracle on lattices at the edges of the layout (`edge_lattices.py`):
+the smallest block (2 x 2 x 2 cells), a rod along x, a column, a two-cell-thick sheet, an odd-sized
+capsule block, a thin sheet the blade cuts through and a small cube the blade misses.  Each runs in
+every launch shape (whole GPU, one CTA, one thread-block cluster) and must match the FP32 oracle bit
+for bit: positions, velocities and, for the blade, the neighbour table and topology revision.
 
 Few colours, colour ranges shorter than a warp, nodes of a colour spread over one or two CTAs and
 edges that end on the lattice margin are what these shapes exercise that the C1-C3 sizes do not.

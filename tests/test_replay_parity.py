@@ -134,6 +134,11 @@ def scenario(name):
         "c2_small_gate": lambda: _capsule_scenario("c2_small_gate", SMALL, 40, 0.5),
         "c3_small": lambda: _blade_scenario("c3_small", SMALL, 40),
         "c3_small_tear": lambda: _blade_scenario("c3_small_tear", SMALL, 20, tear=1.008),
+        # lattices at the edges of the layout: a 2 x 9 x 2 column bending under gravity, the capsule on
+        # an 8 x 5 x 6 block, the blade through a 10 x 3 x 9 sheet
+        "c1_column": lambda: Scenario("c1_column", build_grid(0.2, size=(0.2, 1.8, 0.2), density=1000.0), 20, _base()),
+        "c2_odd": lambda: _capsule_scenario("c2_odd", (1.5, 0.9, 1.1), 20, 0.0),
+        "c3_sheet": lambda: _blade_scenario("c3_sheet", (2.0, 0.4, 1.6), 20),
         "c2_full": lambda: _capsule_scenario("c2_full", None, 20, 0.0),
         "c3_full": lambda: _blade_scenario("c3_full", None, 30),
         "c1_guard_min0.15": lambda: _guard_scenario(0.15),
@@ -198,7 +203,7 @@ def run_scenario(sc, reference_lib, gpu_lib, oracle_libs):
 
 CASES = ["c1", "c1_damped", "c1_ks0", "c1_bending", "c1_perp_damping", "c2_small", "c2_small_gate", "c3_small",
          "c3_small_tear", "c1_guard_min0.15", "c1_guard_min0.9", "c1_friction_closing0", "c1_friction_closing1",
-         "c2_full", "c3_full"]
+         "c1_column", "c2_odd", "c3_sheet", "c2_full", "c3_full"]
 
 
 @pytest.mark.parametrize("case", CASES)
