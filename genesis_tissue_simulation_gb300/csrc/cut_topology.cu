@@ -407,6 +407,7 @@ int build(const SessionView& v) {
         CT_CK(cudaStreamSynchronize(s));   // the host table copied above is the session's, valid now
         C.generation = v.generation; C.N = N; C.T = T; C.keys = keys;
     }
+    C.built = false;   // until this build completes: a failed build leaves nothing for the getter
     CT_CK(C.liveKey.ensure(keys)); CT_CK(C.rankOfKey.ensure(keys)); CT_CK(C.groupOf.ensure((size_t)4 * keys));
     CT_CK(C.groupCount.ensure(N)); CT_CK(C.dupBase.ensure(N)); CT_CK(C.totals.ensure(1)); CT_CK(C.sync.ensure(8));
     liveKeyKernel<<<blocks(keys), kThreads, 0, s>>>(m, keys, C.slotOfKey.p, C.liveKey.p);
