@@ -631,7 +631,8 @@ def cut_topology_measurement(lib, frames=30, warmup=2):
     greedy re-colouring relaxed on the device).  One build before the blade (the session's tables;
     nothing cut), `frames` blade frames, then the first build after them (the relaxation starts from
     the uncut colouring, so every change since the start travels), then `frames` more frames with a
-    build after every step (each relaxation starts from the previous step's colouring).  Wall clock
+    build after every step (each relaxation starts from the previous step's colouring; a step that
+    severed nothing keeps the previous product, and the section counts both kinds of build).  Wall clock
     around the builds and the steps.  Returns the section and the neighbour table of the first build
     after the blade (the CPU baseline leg times the oracle on it)."""
     import ctypes
@@ -663,10 +664,14 @@ def cut_topology_measurement(lib, frames=30, warmup=2):
     finally:
         s.close()
     per_step = float(np.mean(step_ms)) + float(np.mean(build_ms))
+    rebuilt = [b for b, n in zip(build_ms, sweeps) if n > 0]
+    reused = [b for b, n in zip(build_ms, sweeps) if n == 0]
     out = {"workload": f"c3 blade workload, {len(w.grid.positions):,} lattice nodes",
            "first_build_after_frames": frames, "ms_first_build_wall": first_ms, "live_tets": int(first[0]),
            "duplicated_vertices": int(first[1]), "colours": int(first[2]), "relaxation_sweeps": int(first[3]),
            "per_step": {"frames": frames, "ms_build_wall_mean": float(np.mean(build_ms)), "sweeps_mean": float(np.mean(sweeps)),
+                        "builds_relaxed": len(rebuilt), "ms_build_wall_mean_relaxed": float(np.mean(rebuilt)) if rebuilt else None,
+                        "builds_kept": len(reused), "ms_build_wall_mean_kept": float(np.mean(reused)) if reused else None,
                         "ms_step_wall_mean": float(np.mean(step_ms)), "steps_per_s_with_build": 1e3 / per_step},
            "timing": "wall clock around GBT_CutTopologyBuild (and LCS_Step with the rod-phase detection), host synchronised"}
     return out, nbr

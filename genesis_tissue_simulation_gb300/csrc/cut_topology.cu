@@ -66,6 +66,7 @@ struct CutTopologyState {
     DBuf<unsigned char> colour, marks;
     DBuf<unsigned> sync;                     // relaxation kernel: [0] barrier counter, [1] status, [2..4] change counters, [5] sweeps, [6] overflow; [7] largest colour
     int live = 0, duplicates = 0, colours = 0, sweeps = 0;
+    unsigned revision = 0;                   // topology revision of the built product
     bool built = false;
 } C;
 
@@ -407,6 +408,18 @@ int build(const SessionView& v) {
         CT_CK(cudaStreamSynchronize(s));   // the host table copied above is the session's, valid now
         C.generation = v.generation; C.N = N; C.T = T; C.keys = keys;
     }
+    // The product depends on the neighbour table and the active flags alone.  Within one generation
+    // (a physics session, cut module or restored state) they change only by severing, which counts
+    // every link it removes in the revision: with the revision unchanged the last product stands.
+    unsigned revision = 0;
+    if (v.revision) {
+        CT_CK(cudaMemcpyAsync(&revision, v.revision, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        CT_CK(cudaStreamSynchronize(s));
+    }
+    if (C.built && revision == C.revision) {
+        C.sweeps = 0;
+        return 0;
+    }
     C.built = false;   // until this build completes: a failed build leaves nothing for the getter
     CT_CK(C.liveKey.ensure(keys)); CT_CK(C.rankOfKey.ensure(keys)); CT_CK(C.groupOf.ensure((size_t)4 * keys));
     CT_CK(C.groupCount.ensure(N)); CT_CK(C.dupBase.ensure(N)); CT_CK(C.totals.ensure(1)); CT_CK(C.sync.ensure(8));
@@ -457,7 +470,7 @@ int build(const SessionView& v) {
         if (overflow || sweeps > (unsigned)L + 1u) return XPBD_ERR_COLOR_OVERFLOW;
         colours = (int)h[7] + 1;
     }
-    C.live = L; C.duplicates = D; C.colours = colours; C.sweeps = (int)sweeps; C.built = true;
+    C.live = L; C.duplicates = D; C.colours = colours; C.sweeps = (int)sweeps; C.revision = revision; C.built = true;
     return 0;
 }
 
@@ -467,7 +480,7 @@ void releaseCutTopology() {
     for (auto* b : {&C.slotOfKey, &C.storageOfSlot, &C.liveKey, &C.rankOfKey, &C.groupCount, &C.dupBase, &C.blockSums, &C.totals,
                     &C.tetNodes, &C.tetSource, &C.dupParent, &C.nbrCount, &C.nbrRows, &C.upCount, &C.upRows}) b->release();
     C.keyColour.release(); C.groupOf.release(); C.colour.release(); C.marks.release(); C.sync.release();
-    C.generation = 0; C.built = false; C.live = C.duplicates = C.colours = C.sweeps = 0;
+    C.generation = 0; C.built = false; C.live = C.duplicates = C.colours = C.sweeps = 0; C.revision = 0;
 }
 
 }  // namespace gbt
@@ -479,7 +492,6 @@ LCS_API int GBT_CutTopologyBuild(int* counts4) {
     SessionView v{};
     int rc = sessionView(&v);
     if (rc) return rc;
-    C.built = false;
     rc = build(v);
     if (rc) return rc;
     counts4[0] = C.live; counts4[1] = C.duplicates; counts4[2] = C.colours; counts4[3] = C.sweeps;

@@ -796,6 +796,7 @@ LCS_API int LCS_InitCut(const CutInitDesc* desc, const void* conn4096, const voi
     S.tearLen2 = (tau >= 1.0f && tau == tau) ? (tau * desc->voxelL) * (tau * desc->voxelL) : 0.f;
     CK(cudaStreamSynchronize(S.stream));
     S.cutReady = true;
+    S.generation = ++g_sessionGeneration;   // the revision counter restarts at 0 with the cut module
     return 0;
 }
 LCS_API void LCS_SetTool(const CutToolDesc* tool) {
@@ -1284,5 +1285,6 @@ int gbt::sessionView(SessionView* v) {
     v->tetColorOrder = S.tetColorOrder.data();
     v->state = S.state.p;
     v->generation = S.generation;
+    v->revision = S.cutReady ? S.counters.p : nullptr;
     return 0;
 }

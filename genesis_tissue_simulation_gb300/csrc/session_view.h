@@ -16,7 +16,8 @@ struct SessionView {
     ContactParams cp;
     const int* tetColorOrder;          // host [T]: colour slot -> storage index
     unsigned* state;                   // device: [0] liveness revision, [1] barrier counter, [2] status
-    unsigned long long generation;     // changes with every new physics session
+    unsigned long long generation;     // changes with every new physics session, cut module and restored state
+    const unsigned* revision;          // device: links severed since the cut module was set up (null without one)
 };
 
 // 0 and the view when physics is initialised, else a negative status.

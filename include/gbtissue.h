@@ -167,7 +167,9 @@ LCS_API int LCS_GetVoxelCutMask(unsigned* outV); /* cumulative 12-bit cut mask p
  * over nodes).  Colours: the reference's greedy first-fit colouring re-run in emission order over
  * those vertices (with nothing cut, the bind-time colouring).
  * GBT_CutTopologyBuild computes it and writes counts4 = {live tets L, duplicated vertices D,
- * colours, relaxation sweeps of the colouring}; GBT_GetCutTopology copies tetNodes4L[4L] (vertex
+ * colours, relaxation sweeps of the colouring}; when no link has been severed since the previous
+ * build of the same session (and no LCS_InitCut or GBT_SetState came between), that product stands
+ * and the sweeps are 0.  GBT_GetCutTopology copies tetNodes4L[4L] (vertex
  * ids), tetSourceL[L] (storage index, the order of LCS_GetTetIds), tetColourL[L] and dupParentD[D]
  * (the lattice node of vertex N + j).  -1003 (XPBD_ERR_COLOR_OVERFLOW): more than 128 colours. */
 LCS_API int GBT_CutTopologyBuild(int* counts4);

@@ -207,11 +207,12 @@ def test_cuda_matches_oracle_on_blade_workload(gpu_lib, oracle_libs, scale, fram
         assert before["sweeps"] == 1 and len(before["dup_parent"]) == 0
         w.run(s, steps=frames)
         gpu = s.cut_topology()
-        again = s.cut_topology()
+        again = s.cut_topology()     # nothing severed since: the product stands, no relaxation
         nbr = s.neighbors()
         prior = np.full(s.tet_count, -1)
         prior[before["tet_source"]] = before["tet_colour"]
     assert_same(gpu, again)
+    assert gpu["sweeps"] >= 1 and again["sweeps"] == 0
     with w.open(dll_path=oracle_libs[0]) as o:
         set_topology(o, nbr)
         cpu = o.cut_topology()
@@ -228,15 +229,20 @@ def test_cuda_rebuilt_every_step_matches_oracle(gpu_lib, oracle_libs):
     """Built after every step of the blade workload, each relaxation starting from the previous
     step's colouring: at every fifth step the product equals the oracle's sequential build on the
     same topology, and the last equals a single build of the same topology from the uncut colouring
-    (the fixed point does not depend on the start; the sweeps each took are recorded)."""
+    (the fixed point does not depend on the start; the sweeps each took are recorded).  A step that
+    severs nothing keeps the previous product without a relaxation (0 sweeps)."""
     w = W.make("c3", scale=SMALL_C3, steps=40)
     sweeps = []
     with w.open(dll_path=gpu_lib) as s, w.open(dll_path=oracle_libs[0]) as o:
         s.cut_topology()
+        revision = s.topology_revision()
         for k in range(40):
             s.step(detect_cut=w.command(s, k))
             gpu = s.cut_topology()
             sweeps.append(gpu["sweeps"])
+            severed = s.topology_revision() != revision
+            revision = s.topology_revision()
+            assert (gpu["sweeps"] > 0) == severed, (k, gpu["sweeps"], severed)
             if k % 5 == 4:
                 set_topology(o, s.neighbors())
                 assert_same(gpu, o.cut_topology())
