@@ -793,6 +793,9 @@ def main():
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - e0
         assert np.isfinite(positions).all(), "non-finite tissue state"
+        # the phase floor: grid barriers per frame launch and one barrier's latency with no work
+        barriers = session.frame_barriers()
+        barrier_us = session.grid_barrier_floor(20000) if barriers else None
     finally:
         session.close()
 
@@ -829,6 +832,11 @@ def main():
                      "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": substeps * bytes_per_substep},
         "clocks": clocks.summary(),
     }
+    if barriers:
+        floor_ms = barriers * barrier_us / 1e3
+        line["sync_floor"] = {"bound": "grid barrier latency", "barriers_per_launch": barriers, "us_per_barrier": barrier_us,
+                              "floor_ms": floor_ms, "ms_per_launch": 1e3 * launch_s, "frac": floor_ms / (1e3 * launch_s),
+                              "measured": "GBT_GridBarrierFloor: 20,000 back-to-back barriers on the frame kernel's grid"}
     if not args.no_workloads:
         line["workloads"] = {"c1": workload_measurement(lib, "c1", 100, 5), "c3": workload_measurement(lib, "c3", 30, 3)}
         # the reference's own CUDA build on the same box and plugin call sequence, against ours

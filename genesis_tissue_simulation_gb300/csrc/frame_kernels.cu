@@ -919,6 +919,12 @@ __global__ void detectQuadKernel(DeviceMesh m, CutParams cu, QuadTool tool, cons
     markEdge(m, cu, rot, g, a, b, tr, O + D * tr, tool.ncut);
 }
 
+__global__ void __launch_bounds__(kFrameThreads) barrierFloorKernel(unsigned* sync, int barriers, long long budget) {
+    GridSync g{sync, sync + 1, gridDim.x, 0u, budget, 0u};
+    for (int k = 0; k < barriers; k++)
+        if (!g.sync()) return;
+}
+
 __global__ void severKernel(DeviceMesh m, CutParams cu) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= cu.nGridEdges) return;

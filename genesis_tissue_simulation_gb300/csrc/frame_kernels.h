@@ -52,5 +52,7 @@ __global__ void unpackXyzKernel(int n, const float* in, float4* out);
 struct QuadTool { f3 t1[3], t2[3], lo, hi, ncut; int valid; };
 __global__ void detectQuadKernel(DeviceMesh m, CutParams cu, QuadTool tool, const float* rot);
 __global__ void severKernel(DeviceMesh m, CutParams cu);
+// `barriers` grid barriers and nothing else (the latency floor of a frame phase); sync = {counter, status}
+__global__ void barrierFloorKernel(unsigned* sync, int barriers, long long budget);
 
 }  // namespace gbt

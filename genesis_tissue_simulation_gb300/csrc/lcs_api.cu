@@ -113,6 +113,8 @@ struct Session {
     int maxStageBytes = 0;                  // shared memory one CTA may stage the node state in
     int maxClusterBytes = 0;                // dynamic shared memory of a session-cluster CTA
     int syncTestExtra = 0; float syncBudgetSeconds = 2.f;
+    int lastFrameBlocks = 0;                // CTAs of the last frame if it ran on the whole-GPU grid, else 0
+    DBuf<unsigned> floorSync;               // barrier-floor measurement: counter, status
     bool profile = false; std::vector<cudaEvent_t> events; int profiledSteps = 0;
     // section profiler (xpbd_profile_sections, xpbd_solver.cu:30-60): device time per phase kind
     bool sections = false; DBuf<unsigned long long> phaseClock; std::vector<unsigned long long> phaseHost;
@@ -146,7 +148,8 @@ void freePhysics() {
     for (auto* b : {&S.pinned, &S.active, &S.nbr, &S.edgeColorOffD, &S.bendColorOffD, &S.tetColorOffD, &S.edgeOwner, &S.edgeLive,
                     &S.bendSrc, &S.bendLive, &S.tetMeta, &S.tetOwner, &S.edgeSupport}) b->release();
     S.edgeEnds.release(); S.edgeRest.release(); S.bendIJK.release(); S.bendPairs.release(); S.tetIds.release();
-    S.tetAlpha.release(); S.tetStiff.release(); S.state.release(); S.bounds.release();
+    S.tetAlpha.release(); S.tetStiff.release(); S.state.release(); S.bounds.release(); S.floorSync.release();
+    S.lastFrameBlocks = 0;
     S.fiberLambda.release(); S.feasTarget.release(); S.needed.release(); S.incOff.release(); S.incTet.release(); S.guardFlags.release();
     S.rotA.release(); S.rotB.release(); S.rotParity = 0;
     S.volumePasses = 0; S.minVolume = 0.f;
@@ -401,6 +404,7 @@ int launchShape(int shape, const Shapes& u, const FrameCoeffs& fc, const DeviceM
         CK(cudaLaunchCooperativeKernel(ext ? (const void*)frameKernelGridExt : (const void*)frameKernelGrid, dim3(ext ? S.gridBlocksExt : S.gridBlocks),
                                        dim3(kFrameThreads), args, 0, S.stream));
     }
+    S.lastFrameBlocks = shape == kShapeGrid ? (ext ? S.gridBlocksExt : S.gridBlocks) : 0;
     if (shape != kShapeGrid && fc.rotations) {   // the closing particle-frame pass, on the whole GPU
         particleRotKernel<<<(S.N + 255) / 256, 256, 0, S.stream>>>(m, state + 3, 0);
         CK(cudaGetLastError());
@@ -1196,6 +1200,7 @@ LCS_API int LCS_StepNoAlloc(float dt) {
     const int shape = requestedShape(u);   // no timed trials here: they would create events
     bool followUp = false;
     int rc = launchShape(shape, u, fc, m, state, &followUp);
+    S.lastFrameBlocks = 0;   // its barrier counter lives in the static scratch, not the session state
     if (rc) return rc;
     unsigned words[2] = {0u, 0u};   // status, current particle-frame buffer
     CK(cudaMemcpyAsync(words, state + 2, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
@@ -1261,6 +1266,48 @@ LCS_API int LCS_SetBarrierTest(int extraArrivals, float budgetSeconds) {
     S.syncBudgetSeconds = budgetSeconds;
     return 0;
 }
+// Grid barriers the last LCS_Step frame executed (its arrival counter over its CTAs), when that
+// frame ran on the whole-GPU grid; the section a barrier closes is one phase of the frame.
+LCS_API int GBT_FrameBarriers(unsigned* barriers) {
+    if (!barriers) return XPBD_ERR_BAD_ARG;
+    if (!S.physReady || S.lastFrameBlocks <= 0) return XPBD_ERR_NOT_READY;
+    CK(cudaMemcpyAsync(S.hostState + 5, S.state.p + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream));
+    CK(cudaStreamSynchronize(S.stream));
+    *barriers = S.hostState[5] / (unsigned)S.lastFrameBlocks;
+    return 0;
+}
+
+// Latency of this library's grid barrier alone: one cooperative launch of the whole-GPU frame
+// kernel's grid doing `barriers` barriers and nothing else, timed with CUDA events on the session
+// stream (the launch itself included, amortised over the barriers).
+LCS_API int GBT_GridBarrierFloor(int barriers, float* usPerBarrier) {
+    if (!usPerBarrier || barriers < 1 || barriers > 1000000) return XPBD_ERR_BAD_ARG;
+    if (!S.physReady) return XPBD_ERR_NOT_READY;
+    if (!S.floorSync.p) CK(S.floorSync.alloc(2));
+    CK(cudaMemsetAsync(S.floorSync.p, 0, 2 * sizeof(unsigned), S.stream));
+    cudaEvent_t ev[2];
+    CK(cudaEventCreate(&ev[0]));
+    CK(cudaEventCreate(&ev[1]));
+    unsigned* sync = S.floorSync.p;
+    int n = barriers;
+    long long budget = (long long)((double)S.syncBudgetSeconds * 1e3 * S.clockKHz);
+    void* args[] = {&sync, &n, &budget};
+    cudaError_t e = cudaEventRecord(ev[0], S.stream);
+    if (e == cudaSuccess)
+        e = cudaLaunchCooperativeKernel((const void*)barrierFloorKernel, dim3(S.gridBlocks), dim3(kFrameThreads), args, 0, S.stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], S.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(S.hostState + 5, sync + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, S.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(S.stream);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    if (e != cudaSuccess) return -(int)e;
+    if (S.hostState[5] != 0u) return LCS_ERR_DEVICE_TIMEOUT;
+    *usPerBarrier = 1e3f * ms / (float)barriers;
+    return 0;
+}
+
 LCS_API void LCS_Shutdown() {
     if (S.stream) cudaStreamSynchronize(S.stream);
     LCS_ProfileEnable(0);

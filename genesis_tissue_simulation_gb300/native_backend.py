@@ -413,6 +413,30 @@ class PlainTissue(_Session):
         return dict(tet_nodes=nodes, tet_source=source, tet_colour=colour, dup_parent=parent[:dups],
                     colours=int(counts[2]), sweeps=int(counts[3]))
 
+    def frame_barriers(self):
+        """Grid barriers the last frame executed on the whole-GPU grid (GBT_FrameBarriers; CUDA
+        library only), or None when that frame ran in another launch shape."""
+        f = self.dll.GBT_FrameBarriers
+        f.argtypes, f.restype = (ct.c_void_p,), ct.c_int
+        out = ct.c_uint(0)
+        rc = f(ct.byref(out))
+        if rc == XPBD_ERR_NOT_READY:
+            return None
+        if rc != 0:
+            raise RuntimeError(f"GBT_FrameBarriers failed with native status {rc}")
+        return int(out.value)
+
+    def grid_barrier_floor(self, barriers=20000):
+        """Microseconds per grid barrier with no work between barriers, on the whole-GPU frame grid
+        (GBT_GridBarrierFloor; CUDA library only)."""
+        f = self.dll.GBT_GridBarrierFloor
+        f.argtypes, f.restype = (ct.c_int, ct.c_void_p), ct.c_int
+        out = ct.c_float(0.0)
+        rc = f(int(barriers), ct.byref(out))
+        if rc != 0:
+            raise RuntimeError(f"GBT_GridBarrierFloor failed with native status {rc}")
+        return float(out.value)
+
     def edge_colors(self):
         out = np.empty((len(self.grid.positions), 6), dtype=np.int32)
         self.check("LCS_GetEdgeColors", pointer(out))

@@ -198,6 +198,12 @@ LCS_API int LCS_SetLaunchMode(int mode);         /* 0 automatic, 1 whole-GPU coo
  * never come and gives up after `budgetSeconds` (normal budget 2 s); LCS_Step then returns -4002 and
  * the context stays usable.  (0, 2.0) restores normal operation. */
 LCS_API int LCS_SetBarrierTest(int extraArrivals, float budgetSeconds);
+/* Diagnostics of the whole-GPU frame (no counterpart in the reference).  GBT_FrameBarriers: the grid
+ * barriers the last LCS_Step frame executed when it ran on the whole-GPU grid (-1000 otherwise); each
+ * closes one phase.  GBT_GridBarrierFloor: microseconds per barrier of `barriers` (1..1e6) back-to-back
+ * barriers on the same grid with no work between them, the latency floor of a phase. */
+LCS_API int GBT_FrameBarriers(unsigned* barriers);
+LCS_API int GBT_GridBarrierFloor(int barriers, float* usPerBarrier);
 
 /* ---- batched instances (no counterpart in the reference, which has one session per process) ----
  * Many independent tissue meshes, each with the topology its own plain session would build, are

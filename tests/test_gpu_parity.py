@@ -164,3 +164,29 @@ def test_c3_full_size_topology_bit_exact(gpu_lib, oracle_libs):
         assert a["rev"] == b["rev"] == severed_edges(w.grid.neighbors, a["nbr"])
         for key in ("nbr", "mask", "frac", "bends", "dbg", "pos", "vel"):
             assert np.array_equal(a[key], b[key]), key
+
+
+def test_frame_barrier_count_and_floor(gpu_lib):
+    """The whole-GPU frame reports the grid barriers it ran (one per phase: at least the edge and tet
+    colours of every substep) and the barrier floor is measured on the same grid; a frame in another
+    launch shape reports none."""
+    import ctypes
+    w = W.make("c1", steps=2)
+    dll = ctypes.CDLL(str(gpu_lib))
+    try:
+        dll.LCS_SetLaunchMode(1)
+        with w.open(gpu_lib) as s:
+            assert s.frame_barriers() is None      # no frame yet
+            s.step()
+            colours = s.functions["LCS_EdgeColorCount"]() + s.functions["LCS_TetColorCount"]()
+            substeps = int(w.params["substeps"])
+            barriers = s.frame_barriers()
+            assert substeps * colours <= barriers <= substeps * (colours + 6) + 4, (barriers, substeps, colours)
+            us = s.grid_barrier_floor(2000)
+            assert 0.0 < us < 50.0, us
+        dll.LCS_SetLaunchMode(2)
+        with w.open(gpu_lib) as s:
+            s.step()
+            assert s.frame_barriers() is None
+    finally:
+        dll.LCS_SetLaunchMode(0)
