@@ -85,7 +85,7 @@ __device__ __forceinline__ void contactNode(const DeviceMesh& m, int c, const Co
 // k_predict on one node whose position P (w = inverse mass), velocity V and external force F are
 // in registers: x_prev = x; v += h f w; x += h v.
 template <bool Dsm = false>
-__device__ __forceinline__ void predictNode(const DeviceMesh& m, int i, float4 P, f3 V, float4 F, float h) {
+__device__ __forceinline__ float4 predictNode(const DeviceMesh& m, int i, float4 P, f3 V, float4 F, float h) {
     m.prev[i] = make_float4(P.x, P.y, P.z, 0.f);
     if (P.w > 0.f) {
         f3 a = mk(F.x, F.y, F.z) * P.w;
@@ -95,6 +95,7 @@ __device__ __forceinline__ void predictNode(const DeviceMesh& m, int i, float4 P
         P = make_float4(x.x, x.y, x.z, P.w);
     }
     posRef<Dsm>(m, i) = P;
+    return P;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -435,6 +436,7 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
     const bool rotations = Rotations && fc.rotations != 0;
     int rotParity = fc.rotParity;
     bool predicted = false;   // the substep's predict already ran in the previous substep's velocity pass
+    bool edge0Done = false;   // ... and so did its colour-0 edges
     auto framePass = [&]() {
         const float* prevRot = m.particleRot[rotParity];
         float* rot = m.particleRot[rotParity ^ 1];
@@ -504,16 +506,18 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
             if (hasNext) next = loadTet<Codes>(m, first.x + r, fc);
             tetLoaded = true;
         };
+        const int firstEdgeColour = edge0Done ? 1 : 0;
+        edge0Done = false;
         if (fc.doEdges) {
             EdgeRecord n0, n1;
             bool h0 = false, h1 = false;
-            if (Ahead && EdgeGroup == 2 && m.nEdgeColors > 0) {
-                const int2 g0 = m.edgeRange[0];
+            if (Ahead && EdgeGroup == 2 && m.nEdgeColors > firstEdgeColour) {
+                const int2 g0 = m.edgeRange[firstEdgeColour];
                 h0 = g0.x + r < g0.y; h1 = g0.x + r + R < g0.y;
                 if (h0) n0 = loadEdge<Codes>(m, g0.x + r, fc);
                 if (h1) n1 = loadEdge<Codes>(m, g0.x + r + R, fc);
             }
-            for (int c = 0; c < m.nEdgeColors; c++) {
+            for (int c = firstEdgeColour; c < m.nEdgeColors; c++) {
                 int2 rg = m.edgeRange[c];
                 if (Ahead && EdgeGroup == 2) {
                     const EdgeRecord c0 = n0, c1 = n1;
@@ -601,7 +605,50 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
             if (predicted) predictNode<Dsm>(m, i, P, v, F, fc.h);
             else if (touch) posRef<Dsm>(m, i) = P;
         };
-        if (Codes && m.mobile) {
+        // Colour 0 of the edges is a matching: a thread that runs this pass for both ends of a
+        // colour-0 edge predicts the next substep for them and projects the edge on the spot, from
+        // its registers, with the substep-start positions it just wrote as the damping term's.  Each
+        // node and edge sees the operations it would see with a barrier between the two phases, in
+        // the same order; the next substep starts its edge sweep at colour 1.
+        const bool fuse = !Codes && !Dsm && !Extended && predicted && m.fuseEdge0 && fc.doEdges && m.nEdgeColors > 0;
+        if (fuse) {
+            auto velocityPredict = [&](int i, float4 P, float4 Q, float4 V, float4 F, f3& start) {
+                if (touch && P.w > 0.f) {
+                    const f3 p = contactPoint(xyz(P), P.w, xyz(V), cf, cp);
+                    P = make_float4(p.x, p.y, p.z, P.w);
+                }
+                f3 v = P.w > 0.f ? (xyz(P) - xyz(Q)) * fc.invH : mk(0.f, 0.f, 0.f);
+                v = P.w > 0.f ? v * fc.velScale : mk(0.f, 0.f, 0.f);
+                if (!(P.w > 0.f)) m.vel[i] = make_float4(v.x, v.y, v.z, 0.f);
+                start = xyz(P);
+                return predictNode<Dsm>(m, i, P, v, F, fc.h);
+            };
+            FrameCoeffs noStart = fc;
+            noStart.betaGammaHS = 0.f;   // the record's substep-start ends come from the registers below
+            const int2 g0 = m.edgeRange[0];
+            for (int e = g0.x + r; e < g0.y; e += R) {
+                EdgeRecord er = loadEdge<false>(m, e, noStart);
+                const int a = er.ij.x, b = er.ij.y;
+                const float4 Pa = posRef<Dsm>(m, a), Qa = m.prev[a], Pb = posRef<Dsm>(m, b), Qb = m.prev[b];
+                const float4 Va = touch ? m.vel[a] : make_float4(0.f, 0.f, 0.f, 0.f), Fa = m.ext[a];
+                const float4 Vb = touch ? m.vel[b] : make_float4(0.f, 0.f, 0.f, 0.f), Fb = m.ext[b];
+                const float4 Na = velocityPredict(a, Pa, Qa, Va, Fa, er.qi);
+                const float4 Nb = velocityPredict(b, Pb, Qb, Vb, Fb, er.qj);
+                float4 oa, ob;
+                if (solveEdge(er, fc, Na, Nb, oa, ob)) {
+                    posRef<Dsm>(m, a) = oa;
+                    posRef<Dsm>(m, b) = ob;
+                }
+            }
+            for (int q = r; q < m.nUncovered0; q += R) {
+                const int i = m.uncovered0[q];
+                const float4 Pi = posRef<Dsm>(m, i), Qi = m.prev[i];
+                const float4 Vi = touch ? m.vel[i] : make_float4(0.f, 0.f, 0.f, 0.f), Fi = m.ext[i];
+                f3 start;
+                velocityPredict(i, Pi, Qi, Vi, Fi, start);
+            }
+            edge0Done = true;
+        } else if (Codes && m.mobile) {
             for (int q = r; q < m.nMobile; q += R) {
                 const int i = m.mobile[q];
                 const float4 Pi = posRef<Dsm>(m, i), Qi = m.prev[i];

@@ -115,6 +115,7 @@ struct Session {
     int syncTestExtra = 0; float syncBudgetSeconds = 2.f;
     int lastFrameBlocks = 0;                // CTAs of the last frame if it ran on the whole-GPU grid, else 0
     DBuf<unsigned> floorSync;               // barrier-floor measurement: counter, status
+    DBuf<int> uncovered0; bool fuseEdge0 = false;   // nodes ending no colour-0 edge; colour 0 is a matching
     bool profile = false; std::vector<cudaEvent_t> events; int profiledSteps = 0;
     // section profiler (xpbd_profile_sections, xpbd_solver.cu:30-60): device time per phase kind
     bool sections = false; DBuf<unsigned long long> phaseClock; std::vector<unsigned long long> phaseHost;
@@ -149,6 +150,7 @@ void freePhysics() {
                     &S.bendSrc, &S.bendLive, &S.tetMeta, &S.tetOwner, &S.edgeSupport}) b->release();
     S.edgeEnds.release(); S.edgeRest.release(); S.bendIJK.release(); S.bendPairs.release(); S.tetIds.release();
     S.tetAlpha.release(); S.tetStiff.release(); S.state.release(); S.bounds.release(); S.floorSync.release();
+    S.uncovered0.release(); S.fuseEdge0 = false;
     S.lastFrameBlocks = 0;
     S.fiberLambda.release(); S.feasTarget.release(); S.needed.release(); S.incOff.release(); S.incTet.release(); S.guardFlags.release();
     S.rotA.release(); S.rotB.release(); S.rotParity = 0;
@@ -303,6 +305,7 @@ DeviceMesh deviceMesh() {
     m.pinned = S.pinned.p; m.active = S.active.p; m.nbr = S.nbr.p;
     m.nEdgeColors = (int)S.edgeColorOff.size() - 1; m.edgeRange = (const int2*)S.edgeColorOffD.p;
     m.edgeEnds = S.edgeEnds.p; m.edgeRest = S.edgeRest.p; m.edgeOwner = S.edgeOwner.p; m.edgeLive = S.edgeLive.p;
+    m.uncovered0 = S.uncovered0.p; m.nUncovered0 = (int)S.uncovered0.n; m.fuseEdge0 = S.fuseEdge0 ? 1 : 0;
     m.nBendColors = (int)S.bendColorOff.size() - 1; m.bendRange = (const int2*)S.bendColorOffD.p;
     m.bendIJK = S.bendIJK.p; m.bendSrc = S.bendSrc.p; m.bendLive = S.bendLive.p; m.bendPairs = S.bendPairs.p;
     m.nBendPairs = (int)S.bendPairs.n;
@@ -584,6 +587,19 @@ LCS_API int LCS_InitPhysics(const PhysicsInitDesc* desc, const float* mass, cons
                      tetRanges = colourRanges(S.tetColorOff);
     CK(S.edgeColorOffD.upload(edgeRanges.data(), edgeRanges.size(), S.stream));
     CK(S.edgeEnds.upload(hm.edgeEnds.data(), E, S.stream));
+    {   // nodes that end no colour-0 edge; the fusion needs colour 0 to be a matching
+        std::vector<unsigned char> ends(cc, 0);
+        bool matching = S.edgeColorOff.size() > 1;
+        for (int e = matching ? S.edgeColorOff[0] : 0; matching && e < S.edgeColorOff[1]; e++) {
+            const int2 ij = hm.edgeEnds[e];
+            if (ij.x < 0 || ij.y < 0 || ij.x >= (int)cc || ij.y >= (int)cc || ends[ij.x] || ends[ij.y]) matching = false;
+            else ends[ij.x] = ends[ij.y] = 1;
+        }
+        std::vector<int> rest;
+        for (int i = 0; matching && i < (int)cc; i++) if (!ends[i]) rest.push_back(i);
+        CK(S.uncovered0.upload(rest.data(), rest.size(), S.stream));
+        S.fuseEdge0 = matching;
+    }
     CK(S.edgeRest.upload(hm.edgeRest.data(), E, S.stream));
     CK(S.edgeOwner.upload(hm.edgeOwner.data(), E, S.stream));
     std::vector<int> ones(std::max(std::max(E, B), 1), 1);

@@ -75,6 +75,9 @@ struct DeviceMesh {
     // changes (a node of inverse mass 0 keeps its position, substep-start position and zero velocity
     // from the start), so predict and velocity sweep this list; null: every node of the range.
     const int* mobile; int nMobile;
+    // single sessions: the nodes that end no edge of colour 0 (colour 0 is a matching), for the
+    // velocity pass that predicts the next substep and projects its colour-0 edges in one phase
+    const int* uncovered0; int nUncovered0; int fuseEdge0;
 };
 
 // Corners a, b of Kuhn type t on its path 0 -> a -> b -> 7 (kKuhn in mesh_build.cu), 3 bits each,
