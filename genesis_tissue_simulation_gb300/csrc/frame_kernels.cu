@@ -469,7 +469,35 @@ __device__ void runFrame(const DeviceMesh& m, const FrameCoeffs& fc, const ToolP
         const int nodeEnd = m.nodeBase + m.nNodes;
         // -- predict (k_predict), unless the previous substep's velocity pass already did it --
         // With Ahead a thread takes its nodes two at a time, both nodes' loads ahead of either's stores.
-        if (!predicted && Codes && m.mobile) {
+        // As in the velocity pass below, the ends of each colour-0 edge are predicted by one thread,
+        // which projects the edge on the spot (not while the liveness flags are derived again: edge
+        // support comes from every tet's refresh, which only the barrier orders before the edge).
+        if (!Codes && !Dsm && !Extended && !predicted && !stale && m.fuseEdge0 && fc.doEdges && m.nEdgeColors > 0) {
+            FrameCoeffs noStart = fc;
+            noStart.betaGammaHS = 0.f;   // the record's substep-start ends come from the registers below
+            const int2 g0 = m.edgeRange[0];
+            for (int e = g0.x + r; e < g0.y; e += R) {
+                EdgeRecord er = loadEdge<false>(m, e, noStart);
+                const int a = er.ij.x, b = er.ij.y;
+                const float4 Pa = posRef<Dsm>(m, a), Va = m.vel[a], Fa = m.ext[a];
+                const float4 Pb = posRef<Dsm>(m, b), Vb = m.vel[b], Fb = m.ext[b];
+                er.qi = xyz(Pa);
+                er.qj = xyz(Pb);
+                const float4 Na = predictNode<Dsm>(m, a, Pa, xyz(Va), Fa, fc.h);
+                const float4 Nb = predictNode<Dsm>(m, b, Pb, xyz(Vb), Fb, fc.h);
+                float4 oa, ob;
+                if (solveEdge(er, fc, Na, Nb, oa, ob)) {
+                    posRef<Dsm>(m, a) = oa;
+                    posRef<Dsm>(m, b) = ob;
+                }
+            }
+            for (int q = r; q < m.nUncovered0; q += R) {
+                const int i = m.uncovered0[q];
+                const float4 Pi = posRef<Dsm>(m, i), Vi = m.vel[i], Fi = m.ext[i];
+                predictNode<Dsm>(m, i, Pi, xyz(Vi), Fi, fc.h);
+            }
+            edge0Done = true;
+        } else if (!predicted && Codes && m.mobile) {
             for (int q = r; q < m.nMobile; q += R) {
                 const int i = m.mobile[q];
                 float4 Pi = posRef<Dsm>(m, i);
